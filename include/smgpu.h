@@ -1,0 +1,138 @@
+/*
+ * smgpu.h — C ABI of libsmgpu.so, a GB300 (sm_103a) M-scheme shell-model
+ * eigensolver that drops in for NuclearToolkit.jl's `main_sm` path.
+ *
+ * Every entry point is plain C: opaque handles, plain pointers and sizes,
+ * integer status codes.  Each declaration names the reference interface it
+ * replaces (paths relative to the NuclearToolkit.jl source tree).
+ *
+ * Conventions
+ *  - Basis order is the reference's: block-major over (Mp,Mn) blocks ordered
+ *    by ascending proton M, proton-major inside a block
+ *    (M = tdims[b] + p*nn[b] + n, 0-based), Slater determinants in descending
+ *    bit-string order (m-state 1 = most significant bit).
+ *  - Host buffers are owned by the caller; device memory is owned by the
+ *    handle.  One handle is used by one host thread at a time; different
+ *    handles are independent.
+ *  - Status: 0 = success, negative = error class.  smgpu_last_error() gives
+ *    the message of the last failure on that handle (or of the last failed
+ *    create call when given NULL).
+ */
+#ifndef SMGPU_H
+#define SMGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct smgpu_problem smgpu_problem;
+
+enum smgpu_status_code {
+  SMGPU_OK = 0,
+  SMGPU_ERR_ARG = -1,       /* invalid argument */
+  SMGPU_ERR_IO = -2,        /* cannot read the interaction file */
+  SMGPU_ERR_PARSE = -3,     /* malformed snt content */
+  SMGPU_ERR_NUCLEUS = -4,   /* nucleus name / valence numbers invalid */
+  SMGPU_ERR_CUDA = -5,      /* CUDA runtime error (no device, launch failure, ...) */
+  SMGPU_ERR_NOMEM = -6,     /* host or device allocation failed */
+  SMGPU_ERR_LIMIT = -7,     /* problem exceeds a table-packing limit */
+  SMGPU_ERR_NOCONV = -8,    /* Lanczos stopped at max_restarts before convergence */
+  SMGPU_ERR_EMPTY = -9,     /* M-scheme dimension is zero */
+  SMGPU_ERR_DEVICE = -10    /* a device-side check failed (bounded wait or bounds guard) */
+};
+
+/* Arithmetic of the H·v and of the Krylov basis storage. */
+enum smgpu_precision {
+  SMGPU_FP64 = 0,   /* plain form: everything FP64 */
+  SMGPU_MIXED = 1   /* H·v and Krylov storage FP32 with compensated sums; recurrences,
+                       re-orthogonalisation, tridiagonal solves and Ritz vectors FP64 */
+};
+
+/* Orbits are given as in an snt file: n, l, 2j, 2tz (tz = -1 proton, +1 neutron). */
+typedef struct {
+  int lp, ln;                /* number of proton / neutron orbits */
+  const int* orbits;         /* (lp+ln) x 4 : n, l, 2j, tz — protons first */
+  const double* spe;         /* lp+ln single-particle energies */
+  int ntbme;                 /* number of TBME entries below */
+  const int* tbme_labels;    /* ntbme x 5 : a, b, c, d (1-based orbit index), J */
+  const double* tbme;        /* ntbme values, massop scaling already applied */
+  int hermitian_partners;    /* 1: add (c,d,a,b) for every {a,b}!={c,d} entry as readsmsnt does */
+  int vp, vn;                /* valence protons / neutrons */
+  int mtot2;                 /* doubled total M */
+} smgpu_problem_desc;
+
+/* Parse an snt file and set the problem up as main_sm does for target_J = []:
+ * readsmsnt (src/ShellModel/shellmodel_main.jl:293-365), mass number and
+ * element from the nucleus name (util_func.jl:1,13-24; shellmodel_main.jl:
+ * 95,116-117,908-916), Mtot = A mod 2 (:110), basis and jump tables
+ * (occ :769-848, prep_Hamil_T1 :580-649, prep_Hamil_pn :658-730,
+ * prep_pn :1139-1199) built on the GPU. */
+int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int precision, smgpu_problem** out);
+
+/* Same, from an in-memory description (the data of the reference's SMobject,
+ * shellmodel_main.jl:38-53). */
+int smgpu_problem_create(const smgpu_problem_desc* desc, int precision, smgpu_problem** out);
+
+/* Free all device and host memory of the handle. */
+int smgpu_problem_destroy(smgpu_problem* h);
+
+/* Message of the last failure (handle-owned string; NULL handle = last create failure). */
+const char* smgpu_last_error(const smgpu_problem* h);
+
+/* M-scheme dimension and block table (the reference's mdim = tdims[end] and
+ * tdims, shellmodel_main.jl:126-128).  tdims_out may be NULL, else holds
+ * nblocks+1 entries. */
+int smgpu_dims(const smgpu_problem* h, long long* mdim, int* nblocks, long long* tdims_out);
+
+/* Per-block data: proton/neutron SD counts and M values (each array nblocks
+ * long, any may be NULL).  Replaces pbits/nbits lengths and Mps/Mns of occ. */
+int smgpu_blocks(const smgpu_problem* h, int* np, int* nn, int* mp2, int* mn2);
+
+/* Copy the proton and neutron Slater determinants (bit strings, blocks
+ * concatenated in order) to host buffers of sum(np) and sum(nn) entries. */
+int smgpu_export_basis(const smgpu_problem* h, unsigned long long* pbits, unsigned long long* nbits);
+
+/* Jump tables in the reference's forward form for parity checks.
+ * which = 0: proton one-body pn jumps, 1: neutron one-body pn jumps,
+ *         2: pp two-body jumps, 3: nn two-body jumps.
+ * count: number of entries.  For which 0/1 each entry is
+ *   (bi, bf, op_a, op_c, i, f, phase) with op bits as the reference's bit2b
+ *   masks, 1-based block and SD indices, phase = 1 for an odd permutation count;
+ * for which 2/3: (block, i, f) and the coefficient in `coef` (f >= i, the
+ * reference's T1info with the 1/2 on the diagonal).
+ * Call with NULL buffers to get the count. */
+int smgpu_export_jumps(const smgpu_problem* h, int which, long long* count, long long* ints, double* coef);
+
+/* w (+)= H v on host buffers in the reference's basis order (unpadded, mdim
+ * doubles each, ncols column vectors stored one after another).
+ * accumulate = 1 reproduces operate_H!'s "twf += H wf" (lanczos_methods.jl:153);
+ * accumulate = 0 overwrites w.  Runs in the handle's precision. */
+int smgpu_matvec(smgpu_problem* h, const double* v, double* w, int ncols, int accumulate);
+
+/* Thick-restart Lanczos for the lowest num_ev eigenvalues: TRL with
+ * diagonalize_T!/ThickRestart (lanczos_methods.jl:1-91,250-307) and Ritz
+ * vectors (shellmodel_main.jl:208-224), entirely on the GPU.
+ *   lm, ls, tol: as main_sm's kwargs (defaults 300, 20, 1e-8);
+ *   max_restarts: stop with SMGPU_ERR_NOCONV after this many restarts;
+ *   v1: optional start vector (mdim doubles, host), NULL = seeded hash draw;
+ *   evals_out: num_ev doubles (min(num_ev, mdim) are written);
+ *   evecs_out: NULL or num_ev x mdim doubles (Ritz vectors, basis order);
+ *   stats_out: NULL or 6 ints: [elit, n_matvec, n_restart, converged, num_ev_written, reserved]. */
+int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int max_restarts,
+                const double* v1, double* evals_out, double* evecs_out, int* stats_out);
+
+/* Seconds spent in the phases of the last smgpu_solve / create call
+ * (the reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos",
+ * "operate H", "ReORTH", "Restart", "Rvecs").  times_out: 8 doubles:
+ * [setup, lanczos, matvec, reorth, restart, ritz, h2d, d2h]. */
+int smgpu_timings(const smgpu_problem* h, double* times_out);
+
+/* Structural statistics of the factorised H: [updates per H·v (multiply-adds),
+ * pn proton pull entries, pn neutron entries, pp entries, nn entries,
+ * table bytes on the device, padded vector length, number of links]. */
+int smgpu_stats(const smgpu_problem* h, long long* stats_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMGPU_H */

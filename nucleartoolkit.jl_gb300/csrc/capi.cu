@@ -1,0 +1,636 @@
+// extern "C" entry points of libsmgpu.so (declared in include/smgpu.h).
+//
+// A handle owns one problem: the host tables from setup.cpp, their device
+// copies, and (during smgpu_solve) the Krylov basis.  The Lanczos iteration
+// of one restart cycle — H·v, α, the eigenvalue test, re-orthogonalisation,
+// β, the next basis vector and the thick restart — is captured once as a CUDA
+// graph and replayed until the device-side convergence flag is set; the host
+// reads that flag once per cycle.  The eigenvalue test of iteration k runs on
+// a second stream concurrently with the re-orthogonalisation of iteration k
+// and the H·v of iteration k+1.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/smgpu.h"
+#include "device.cuh"
+#include "lanczos.cuh"
+#include "setup.h"
+
+using namespace smgpu;
+
+namespace {
+thread_local std::string g_create_error;
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    size_t b = sizeof(T) * (n > 0 ? n : 1);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) throw CudaError{e, "cudaMalloc", __FILE__, __LINE__};
+    ptrs.push_back(p);
+    bytes += b;
+    return (T*)p;
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    T* p = alloc<T>(v.size());
+    if (!v.empty()) SMGPU_CUDA_TRY(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return p;
+  }
+  void free_all() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+    bytes = 0;
+  }
+};
+
+template <class T>
+std::vector<float> to_f32(const std::vector<T>& v) {
+  std::vector<float> r(v.size());
+  for (size_t i = 0; i < v.size(); ++i) r[i] = (float)v[i];
+  return r;
+}
+}  // namespace
+
+struct smgpu_problem {
+  int precision = SMGPU_FP64;
+  Tables T;
+  DeviceArena tables;
+  DevTables dt{};
+  CoefTables<double> c64{};
+  CoefTables<float> c32{};
+  const double* d_ep = nullptr;
+  const double* d_en = nullptr;
+  int nrows = 0;
+  cudaStream_t st = nullptr, st2 = nullptr;
+  std::string err;
+  double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int sms = 152;
+  // solver state of the last solve
+  DeviceArena solver;
+
+  ~smgpu_problem() {
+    solver.free_all();
+    tables.free_all();
+    if (st) cudaStreamDestroy(st);
+    if (st2) cudaStreamDestroy(st2);
+  }
+
+  void upload() {
+    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    int dev = 0;
+    SMGPU_CUDA_TRY(cudaGetDevice(&dev));
+    SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int nb = T.nb;
+    dt.nb = nb;
+    dt.len_pad = T.len_pad;
+    dt.np = tables.upload(T.np);
+    dt.nn = tables.upload(T.nn);
+    dt.stride = tables.upload(T.stride);
+    dt.off_pad = tables.upload(T.off_pad);
+    dt.pstart = tables.upload(T.pstart);
+    dt.nstart = tables.upload(T.nstart);
+    dt.tdims = tables.upload(T.tdims);
+    std::vector<int> prow(T.pstart[nb]);
+    for (int b = 0; b < nb; ++b)
+      for (int g = T.pstart[b]; g < T.pstart[b + 1]; ++g) prow[g] = b;
+    nrows = T.pstart[nb];
+    dt.prow_block = tables.upload(prow);
+    dt.pp_ptr = tables.upload(T.pp_ptr);
+    dt.pp_col = tables.upload(T.pp_col);
+    dt.nn_ptr = tables.upload(T.nn_ptr);
+    dt.nn_col = tables.upload(T.nn_col);
+    std::vector<int4> la(T.links.size());
+    std::vector<int64_t> lv(T.links.size()), ln(T.links.size());
+    for (size_t k = 0; k < T.links.size(); ++k) {
+      la[k] = make_int4(T.links[k].s, T.links[k].nB, T.links[k].dm, 0);
+      lv[k] = T.links[k].vtab_off;
+      ln[k] = T.links[k].nptr_off;
+    }
+    dt.link_a = tables.upload(la);
+    dt.link_v = tables.upload(lv);
+    dt.link_n = tables.upload(ln);
+    dt.ppn_ptr = tables.upload(T.ppn_ptr);
+    dt.ppn_src = tables.upload(T.ppn_src);
+    dt.ppn_meta = tables.upload(T.ppn_meta);
+    dt.npn_ptr = tables.upload(T.npn_ptr);
+    dt.npn_ent = tables.upload(T.npn_ent);
+    d_ep = tables.upload(T.ep);
+    d_en = tables.upload(T.en);
+    if (precision == SMGPU_FP64) {
+      c64.pp_val = tables.upload(T.pp_val);
+      c64.nn_val = tables.upload(T.nn_val);
+      c64.vtab = tables.upload(T.vtab);
+    } else {
+      c32.pp_val = tables.upload(to_f32(T.pp_val));
+      c32.nn_val = tables.upload(to_f32(T.nn_val));
+      c32.vtab = tables.upload(to_f32(T.vtab));
+    }
+  }
+
+  template <class TX>
+  void hv(const TX* v, double* w, const int* done, cudaStream_t s);
+};
+
+template <>
+void smgpu_problem::hv<double>(const double* v, double* w, const int* done, cudaStream_t s) {
+  launch_hv_fp64(dt, d_ep, d_en, c64, v, w, nrows, done, s);
+}
+template <>
+void smgpu_problem::hv<float>(const float* v, double* w, const int* done, cudaStream_t s) {
+  launch_hv_mixed(dt, d_ep, d_en, c32, v, w, nrows, done, s);
+}
+
+namespace {
+
+int fail(smgpu_problem* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+template <class F>
+int guarded(smgpu_problem* h, F&& f) {
+  try {
+    return f();
+  } catch (const SetupError& e) {
+    return fail(h, e.code, e.msg);
+  } catch (const CudaError& e) {
+    return fail(h, SMGPU_ERR_CUDA,
+                std::string("CUDA error ") + cudaGetErrorString(e.err) + " at " + e.what + " (" + e.file + ":" +
+                    std::to_string(e.line) + ")");
+  } catch (const std::bad_alloc&) {
+    return fail(h, SMGPU_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(h, SMGPU_ERR_ARG, e.what());
+  }
+}
+
+int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision, smgpu_problem** out) {
+  if (precision != SMGPU_FP64 && precision != SMGPU_MIXED) throw SetupError{SMGPU_ERR_ARG, "unknown precision"};
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0)
+    throw SetupError{SMGPU_ERR_CUDA, "no CUDA device available: the GPU library has no CPU path"};
+  smgpu_problem* h = new smgpu_problem();
+  try {
+    h->precision = precision;
+    double t0 = now_s();
+    build_tables(I, vp, vn, mtot2, h->T);
+    if (h->T.mdim == 0) throw SetupError{SMGPU_ERR_EMPTY, "M-scheme dimension is zero"};
+    h->upload();
+    SMGPU_CUDA_TRY(cudaDeviceSynchronize());
+    h->times[0] = now_s() - t0;
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  *out = h;
+  return SMGPU_OK;
+}
+
+// ------------------------------------------------------------------ solver
+template <class TX>
+struct Solve {
+  smgpu_problem* P;
+  LanczosDev L{};
+  TX* V = nullptr;
+  TX* U = nullptr;
+  double* w = nullptr;
+  int gate_done = 1, gate_second = 2;  // host copies of the gate codes
+
+  void alloc(int lm, int ls, int num_ev, double tol) {
+    DeviceArena& A = P->solver;
+    A.free_all();
+    L.G = 2 * P->sms;
+    L.lm = lm;
+    L.ls = ls;
+    L.num_ev = num_ev;
+    L.nh = 3;
+    L.len = P->T.len_pad;
+    L.mdim = P->T.mdim;
+    L.tol = tol;
+    const int P_gram = ls * (ls + 1) / 2 + ls;
+    const int npart = std::max(lm + 2, P_gram) + 2;
+    V = A.alloc<TX>((size_t)lm * L.len);
+    U = A.alloc<TX>((size_t)ls * L.len);
+    w = A.alloc<double>(L.len);
+    L.T = A.alloc<double>((size_t)lm * lm);
+    L.en = A.alloc<double>((size_t)L.nh * num_ev);
+    L.partials = A.alloc<double>((size_t)npart * L.G);
+    L.h = A.alloc<double>(lm + 2);
+    L.jacA = A.alloc<double>((size_t)lm * lm);
+    L.jacZ = A.alloc<double>((size_t)lm * lm);
+    L.evals = A.alloc<double>(lm);
+    L.gram = A.alloc<double>(P_gram);
+    L.X = A.alloc<double>((size_t)ls * ls);
+    L.cvec = A.alloc<double>(ls);
+    L.sc = A.alloc<LanczosScalars>(1);
+    L.fl = A.alloc<LanczosFlags>(1);
+    SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(TX) * (size_t)lm * L.len, P->st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * L.len, P->st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(L.T, 0, sizeof(double) * (size_t)lm * lm, P->st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(L.sc, 0, sizeof(LanczosScalars), P->st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(L.fl, 0, sizeof(LanczosFlags), P->st));
+    std::vector<double> en0((size_t)L.nh * num_ev, 1.0e4);
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(L.en, en0.data(), sizeof(double) * en0.size(), cudaMemcpyHostToDevice, P->st));
+  }
+
+  // v1 -> V[0] normalised (start vector in w on entry)
+  void init_start() {
+    launch_multidot<double>(L, w, 1, w, false, nullptr, P->st);
+    launch_reduce(L, 1, RED_INVNORM, L.h, 0, nullptr, P->st);
+    launch_scale_store<TX>(L, w, V, L.h, nullptr, P->st);
+  }
+
+  // One Lanczos iteration, `it` 1-based (lanczos_methods.jl:34-62).
+  void iteration(int it, int lock, cudaEvent_t ev_fork, cudaEvent_t ev_join, bool first_of_cycle) {
+    cudaStream_t s = P->st, s2 = P->st2;
+    const int it0 = it - 1;
+    TX* vk = V + (size_t)it0 * L.len;
+    P->hv<TX>(vk, w, &L.fl->done, s);  // gate read from device memory
+    launch_multidot<TX>(L, vk, 1, w, false, &gate_done, s);
+    launch_reduce(L, 1, RED_ALPHA, nullptr, it0, &gate_done, s);
+    SMGPU_CUDA_TRY(cudaEventRecord(ev_fork, s));
+    SMGPU_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
+    launch_sturm(L, it, lock, s2);
+    (void)first_of_cycle;
+    (void)ev_join;
+    // ReORTH: classical Gram-Schmidt with a second pass when the norm drops
+    // below 1/sqrt(2) of its value (FP64 throughout)
+    launch_multidot<TX>(L, V, it, w, true, &gate_done, s);
+    launch_reduce(L, it, RED_H, L.h, it0, &gate_done, s);
+    launch_multiaxpy<TX>(L, V, it, w, &gate_done, s);
+    launch_reduce(L, 1, RED_NRM_CHECK, nullptr, it0, &gate_done, s);
+    launch_multidot<TX>(L, V, it, w, false, &gate_second, s);
+    launch_reduce(L, it, RED_STORE, L.h, it0, &gate_second, s);
+    launch_multiaxpy<TX>(L, V, it, w, &gate_second, s);
+    launch_reduce(L, 1, RED_NRM, nullptr, it0, &gate_second, s);
+    launch_beta(L, it0, s);
+    launch_scale_store<TX>(L, w, V + (size_t)it * L.len, &L.sc->inv_beta, &gate_done, s);
+  }
+
+  void restart(cudaStream_t s) {
+    // ThickRestart (lanczos_methods.jl:260-307)
+    launch_jacobi(L, L.lm - 1, true, s);
+    launch_restart_small(L, s);
+    launch_restart_rotate<TX>(L, V, U, s);
+    launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, s);
+    const int P_gram = L.ls * (L.ls + 1) / 2 + L.ls;
+    launch_reduce(L, P_gram, RED_STORE, L.gram, 0, &gate_done, s);
+    launch_chol(L, s);
+    launch_restart_apply<TX>(L, U, V, s);
+  }
+
+  cudaGraphExec_t capture_cycle(int kstart, int lock) {
+    cudaStream_t s = P->st, s2 = P->st2;
+    cudaEvent_t e_fork, e_join;
+    SMGPU_CUDA_TRY(cudaEventCreateWithFlags(&e_fork, cudaEventDisableTiming));
+    SMGPU_CUDA_TRY(cudaEventCreateWithFlags(&e_join, cudaEventDisableTiming));
+    cudaGraph_t g;
+    SMGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int it = kstart; it <= L.lm - 1; ++it) iteration(it, lock, e_fork, e_join, it == kstart);
+    SMGPU_CUDA_TRY(cudaEventRecord(e_join, s2));
+    SMGPU_CUDA_TRY(cudaStreamWaitEvent(s, e_join, 0));
+    restart(s);
+    SMGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    cudaGraphExec_t ex;
+    SMGPU_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
+    cudaGraphDestroy(g);
+    cudaEventDestroy(e_fork);
+    cudaEventDestroy(e_join);
+    return ex;
+  }
+
+  int run(int num_ev, int lm, int ls, double tol, int max_restarts, const double* v1, double* evals_out,
+          double* evecs_out, int* stats_out) {
+    const int64_t mdim = P->T.mdim;
+    const int nev = (int)std::min<int64_t>(num_ev, mdim);
+    double t0 = now_s();
+    alloc(lm, ls, num_ev, tol);
+    if (v1) {
+      double* tmp = P->solver.alloc<double>(mdim);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(tmp, v1, sizeof(double) * mdim, cudaMemcpyHostToDevice, P->st));
+      launch_to_padded<double>(P->dt, tmp, w, P->st);
+    } else {
+      launch_start_vector(P->dt, 1234ull, w, P->st);
+    }
+    init_start();
+    cudaGraphExec_t g_first = capture_cycle(1, 0);
+    cudaGraphExec_t g_rest = nullptr;
+    int n_restart = 0, status = SMGPU_OK;
+    LanczosFlags fl{};
+    SMGPU_CUDA_TRY(cudaGraphLaunch(g_first, P->st));
+    while (true) {
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(&fl, L.fl, sizeof(LanczosFlags), cudaMemcpyDeviceToHost, P->st));
+      SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+      if (fl.done) break;
+      if (fl.exhausted) {
+        fl.done = 1;
+        fl.elit = fl.exh_k;
+        break;
+      }
+      ++n_restart;
+      if (n_restart > max_restarts) {
+        status = SMGPU_ERR_NOCONV;
+        fl.elit = lm - 1;
+        break;
+      }
+      if (!g_rest) g_rest = capture_cycle(ls + 1, ls);
+      SMGPU_CUDA_TRY(cudaGraphLaunch(g_rest, P->st));
+    }
+    if (fl.bad) {
+      cudaGraphExecDestroy(g_first);
+      if (g_rest) cudaGraphExecDestroy(g_rest);
+      return fail(P, SMGPU_ERR_DEVICE, "restart Gram matrix was not positive definite");
+    }
+    double t1 = now_s();
+    // eigenvalues: en[1] of the last eigenvalue test (main_sm returns en[1])
+    SMGPU_CUDA_TRY(cudaMemcpy(evals_out, L.en, sizeof(double) * nev, cudaMemcpyDeviceToHost));
+    int elit = fl.elit;
+    if (status == SMGPU_ERR_NOCONV) elit = 0;
+    if (evecs_out && elit > 0) {
+      // Ritz vectors (shellmodel_main.jl:208-224)
+      launch_jacobi(L, elit, false, P->st);
+      double* R = P->solver.alloc<double>((size_t)nev * L.len);
+      double* tmp = P->solver.alloc<double>(mdim);
+      launch_ritz<TX>(L, V, elit, nev, R, P->st);
+      for (int e = 0; e < nev; ++e) {
+        double* r = R + (size_t)e * L.len;
+        launch_multidot<double>(L, r, 1, r, false, nullptr, P->st);
+        launch_reduce(L, 1, RED_INVNORM, L.h + e, 0, nullptr, P->st);
+        launch_scale_store<double>(L, r, r, L.h + e, nullptr, P->st);
+        launch_from_padded(P->dt, r, tmp, P->st);
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(evecs_out + (size_t)e * mdim, tmp, sizeof(double) * mdim,
+                                       cudaMemcpyDeviceToHost, P->st));
+      }
+      SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+    }
+    double t2 = now_s();
+    SMGPU_CUDA_TRY(cudaGetLastError());
+    if (stats_out) {
+      int n_hv = 0;
+      // iterations executed: first cycle 1..lm-1, later cycles ls+1..lm-1
+      if (fl.done) {
+        n_hv = (n_restart == 0) ? elit : (lm - 1) + (n_restart - 1) * (lm - 1 - ls) + (elit - ls);
+      } else {
+        n_hv = (lm - 1) + (n_restart - 1) * (lm - 1 - ls);
+      }
+      stats_out[0] = elit;
+      stats_out[1] = n_hv;
+      stats_out[2] = n_restart;
+      stats_out[3] = fl.done ? 1 : 0;
+      stats_out[4] = nev;
+      stats_out[5] = fl.n_second;
+    }
+    P->times[1] = t1 - t0;
+    P->times[5] = t2 - t1;
+    cudaGraphExecDestroy(g_first);
+    if (g_rest) cudaGraphExecDestroy(g_rest);
+    return status;
+  }
+};
+
+}  // namespace
+
+// =========================================================================
+extern "C" {
+
+int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int precision, smgpu_problem** out) {
+  if (!snt_path || !nucleus || !out) return fail(nullptr, SMGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  return guarded(nullptr, [&]() {
+    int A = 0, Z = 0;
+    parse_nucleus(nucleus, A, Z);
+    Interaction I = read_snt(snt_path, A);
+    int vp = Z - I.cp, vn = (A - Z) - I.cn;
+    if (vp < 0 || vn < 0) throw SetupError{SMGPU_ERR_NUCLEUS, "nucleus lies below the snt core"};
+    int mtot2 = (A % 2 == 0) ? 0 : 1;  // shellmodel_main.jl:110
+    return create_common(I, vp, vn, mtot2, precision, out);
+  });
+}
+
+int smgpu_problem_create(const smgpu_problem_desc* d, int precision, smgpu_problem** out) {
+  if (!d || !out || !d->orbits || !d->spe || (d->ntbme > 0 && (!d->tbme_labels || !d->tbme)))
+    return fail(nullptr, SMGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  return guarded(nullptr, [&]() {
+    Interaction I;
+    I.lp = d->lp;
+    I.ln = d->ln;
+    if (I.lp <= 0 || I.ln <= 0) throw SetupError{SMGPU_ERR_ARG, "bad orbit counts"};
+    for (int k = 0; k < I.lp + I.ln; ++k) {
+      Orbit o{d->orbits[4 * k], d->orbits[4 * k + 1], d->orbits[4 * k + 2], d->orbits[4 * k + 3]};
+      if (k < I.lp) { I.porb.push_back(o); I.spe_p.push_back(d->spe[k]); }
+      else { I.norb.push_back(o); I.spe_n.push_back(d->spe[k]); }
+    }
+    for (int k = 0; k < d->ntbme; ++k) {
+      const int* l = d->tbme_labels + 5 * k;
+      int a = l[0], b = l[1], c = l[2], dd = l[3];
+      int lim = I.lp + I.ln;
+      if (a < 1 || b < 1 || c < 1 || dd < 1 || a > lim || b > lim || c > lim || dd > lim)
+        throw SetupError{SMGPU_ERR_ARG, "TBME orbit index out of range"};
+      int kind;
+      if (a <= I.lp && b <= I.lp) kind = 0;
+      else if (a > I.lp && b > I.lp) kind = 1;
+      else if (a <= I.lp && b > I.lp) kind = 2;
+      else throw SetupError{SMGPU_ERR_ARG, "TBME with the proton index after the neutron index"};
+      if (d->hermitian_partners) {
+        bool same = (a == b) ? (c == dd && c == a) : (c != dd && a == c && b == dd);
+        if (!same) I.tb[kind].push_back({c, dd, a, b, l[4], d->tbme[k]});
+      }
+      I.tb[kind].push_back({a, b, c, dd, l[4], d->tbme[k]});
+    }
+    return create_common(I, d->vp, d->vn, d->mtot2, precision, out);
+  });
+}
+
+int smgpu_problem_destroy(smgpu_problem* h) {
+  delete h;
+  return SMGPU_OK;
+}
+
+const char* smgpu_last_error(const smgpu_problem* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int smgpu_dims(const smgpu_problem* h, long long* mdim, int* nblocks, long long* tdims_out) {
+  if (!h) return SMGPU_ERR_ARG;
+  if (mdim) *mdim = h->T.mdim;
+  if (nblocks) *nblocks = h->T.nb;
+  if (tdims_out)
+    for (int b = 0; b <= h->T.nb; ++b) tdims_out[b] = h->T.tdims[b];
+  return SMGPU_OK;
+}
+
+int smgpu_blocks(const smgpu_problem* h, int* np, int* nn, int* mp2, int* mn2) {
+  if (!h) return SMGPU_ERR_ARG;
+  for (int b = 0; b < h->T.nb; ++b) {
+    if (np) np[b] = h->T.np[b];
+    if (nn) nn[b] = h->T.nn[b];
+    if (mp2) mp2[b] = h->T.mp2[b];
+    if (mn2) mn2[b] = h->T.mn2[b];
+  }
+  return SMGPU_OK;
+}
+
+int smgpu_export_basis(const smgpu_problem* h, unsigned long long* pbits, unsigned long long* nbits) {
+  if (!h) return SMGPU_ERR_ARG;
+  if (pbits) std::memcpy(pbits, h->T.pbits.data(), sizeof(uint64_t) * h->T.pbits.size());
+  if (nbits) std::memcpy(nbits, h->T.nbits.data(), sizeof(uint64_t) * h->T.nbits.size());
+  return SMGPU_OK;
+}
+
+int smgpu_export_jumps(const smgpu_problem* h, int which, long long* count, long long* ints, double* coef) {
+  if (!h || !count) return SMGPU_ERR_ARG;
+  const Tables& T = h->T;
+  long long c = 0;
+  if (which == 0 || which == 1) {
+    // forward links only (source block >= output block) = the reference's lists
+    for (int b = 0; b < T.nb; ++b)
+      for (int li = T.link_begin[b]; li < T.link_begin[b + 1]; ++li) {
+        const auto& L = T.links[li];
+        if (L.s < L.b) continue;
+        if (which == 0) {
+          for (int g = T.pstart[b]; g < T.pstart[b + 1]; ++g)
+            for (int k = T.ppn_ptr[g]; k < T.ppn_ptr[g + 1]; ++k) {
+              uint32_t meta = T.ppn_meta[k];
+              if ((int)(meta >> 16) != li) continue;
+              if (ints) {
+                int ia = (meta >> 1) & 0x7fff;
+                long long* e = ints + 7 * c;
+                e[0] = b + 1; e[1] = L.s + 1;
+                e[2] = (long long)T.Aops_dm[L.dm][2 * ia]; e[3] = (long long)T.Aops_dm[L.dm][2 * ia + 1];
+                e[4] = g - T.pstart[b] + 1; e[5] = (long long)T.ppn_src[k] + 1;
+                e[6] = (meta & 1) ? 0 : 1;  // reference phase flag: true for an even count
+              }
+              ++c;
+            }
+        } else {
+          for (int n = 0; n < T.nn[b]; ++n)
+            for (int64_t j = T.npn_ptr[L.nptr_off + n]; j < T.npn_ptr[L.nptr_off + n + 1]; ++j) {
+              uint32_t e32 = T.npn_ent[j];
+              if (ints) {
+                int ib = (e32 >> 1) & 0x1fff;
+                long long* e = ints + 7 * c;
+                e[0] = b + 1; e[1] = L.s + 1;
+                e[2] = (long long)T.Bops_dm[L.dm][2 * ib]; e[3] = (long long)T.Bops_dm[L.dm][2 * ib + 1];
+                e[4] = n + 1; e[5] = (long long)(e32 >> 14) + 1;
+                e[6] = (e32 & 1) ? 0 : 1;
+              }
+              ++c;
+            }
+        }
+      }
+  } else if (which == 2 || which == 3) {
+    const auto& ptr = which == 2 ? T.pp_ptr : T.nn_ptr;
+    const auto& col = which == 2 ? T.pp_col : T.nn_col;
+    const auto& val = which == 2 ? T.pp_val : T.nn_val;
+    const auto& start = which == 2 ? T.pstart : T.nstart;
+    for (int b = 0; b < T.nb; ++b)
+      for (int g = start[b]; g < start[b + 1]; ++g) {
+        int i = g - start[b];
+        for (int k = ptr[g]; k < ptr[g + 1]; ++k) {
+          if (col[k] < i) continue;
+          if (ints) {
+            long long* e = ints + 3 * c;
+            e[0] = b + 1; e[1] = i + 1; e[2] = col[k] + 1;
+            coef[c] = (col[k] == i) ? 0.5 * val[k] : val[k];
+          }
+          ++c;
+        }
+      }
+  } else {
+    return SMGPU_ERR_ARG;
+  }
+  *count = c;
+  return SMGPU_OK;
+}
+
+int smgpu_matvec(smgpu_problem* h, const double* v, double* w, int ncols, int accumulate) {
+  if (!h || !v || !w || ncols < 1) return fail(h, SMGPU_ERR_ARG, "bad matvec arguments");
+  return guarded(h, [&]() {
+    const int64_t mdim = h->T.mdim, len = h->T.len_pad;
+    DeviceArena tmp;
+    try {
+      double* d_in = tmp.alloc<double>(mdim);
+      double* d_out = tmp.alloc<double>(mdim);
+      double* d_w = tmp.alloc<double>(len);
+      SMGPU_CUDA_TRY(cudaMemsetAsync(d_w, 0, sizeof(double) * len, h->st));
+      std::vector<double> host(mdim);
+      void* d_v = (h->precision == SMGPU_FP64) ? (void*)tmp.alloc<double>(len) : (void*)tmp.alloc<float>(len);
+      double t0 = now_s();
+      for (int c = 0; c < ncols; ++c) {
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(d_in, v + (size_t)c * mdim, sizeof(double) * mdim, cudaMemcpyHostToDevice, h->st));
+        if (h->precision == SMGPU_FP64) {
+          launch_to_padded<double>(h->dt, d_in, (double*)d_v, h->st);
+          h->hv<double>((const double*)d_v, d_w, nullptr, h->st);
+        } else {
+          launch_to_padded<float>(h->dt, d_in, (float*)d_v, h->st);
+          h->hv<float>((const float*)d_v, d_w, nullptr, h->st);
+        }
+        launch_from_padded(h->dt, d_w, d_out, h->st);
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(host.data(), d_out, sizeof(double) * mdim, cudaMemcpyDeviceToHost, h->st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(h->st));
+        double* wc = w + (size_t)c * mdim;
+        if (accumulate)
+          for (int64_t i = 0; i < mdim; ++i) wc[i] += host[i];
+        else
+          std::memcpy(wc, host.data(), sizeof(double) * mdim);
+      }
+      SMGPU_CUDA_TRY(cudaGetLastError());
+      h->times[2] = now_s() - t0;
+    } catch (...) {
+      tmp.free_all();
+      throw;
+    }
+    tmp.free_all();
+    return SMGPU_OK;
+  });
+}
+
+int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int max_restarts, const double* v1,
+                double* evals_out, double* evecs_out, int* stats_out) {
+  if (!h || !evals_out) return fail(h, SMGPU_ERR_ARG, "null argument");
+  if (num_ev < 1 || lm < 3 || ls < 1 || ls > lm - 2 || ls > 60 || lm > 1000 || num_ev > lm - 1 || !(tol > 0.0))
+    return fail(h, SMGPU_ERR_ARG, "need 1 <= num_ev < lm, 1 <= ls <= min(lm-2, 60), lm <= 1000, tol > 0");
+  return guarded(h, [&]() {
+    if (h->precision == SMGPU_FP64) {
+      Solve<double> s{h};
+      return s.run(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
+    }
+    Solve<float> s{h};
+    return s.run(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
+  });
+}
+
+int smgpu_timings(const smgpu_problem* h, double* t) {
+  if (!h || !t) return SMGPU_ERR_ARG;
+  for (int k = 0; k < 8; ++k) t[k] = h->times[k];
+  return SMGPU_OK;
+}
+
+int smgpu_stats(const smgpu_problem* h, long long* s) {
+  if (!h || !s) return SMGPU_ERR_ARG;
+  const Tables& T = h->T;
+  s[0] = T.updates;
+  s[1] = (long long)T.ppn_src.size();
+  s[2] = (long long)T.npn_ent.size();
+  s[3] = (long long)T.pp_col.size();
+  s[4] = (long long)T.nn_col.size();
+  s[5] = (long long)h->tables.bytes;
+  s[6] = (long long)T.len_pad;
+  s[7] = (long long)T.links.size();
+  return SMGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,706 @@
+// Thick-restart Lanczos on the GPU: the device half of TRL
+// (src/ShellModel/lanczos_methods.jl:1-91), diagonalize_T! (:250-258),
+// ThickRestart (:260-307), ReORTH (shellmodel_main.jl:1005-1012) and the Ritz
+// vector assembly (shellmodel_main.jl:208-224).
+//
+// Every kernel reads its gate from device memory (LanczosFlags), so a whole
+// restart cycle can be captured in one CUDA graph: once the convergence test
+// sets `done`, the remaining kernels of the cycle return immediately.
+//
+// FP64 is used for all dot products, the orthogonalisation, the small
+// eigenproblems and the Ritz vectors; Krylov vectors are stored as TX
+// (double in the plain form, float in the mixed form).  Reductions are
+// deterministic: a fixed grid writes per-CTA partial sums that one CTA adds
+// in a fixed order.
+#include <cfloat>
+
+#include "lanczos.cuh"
+
+namespace smgpu {
+
+namespace {
+constexpr int kNT = 256;  // threads of the streaming kernels
+
+enum Gate { GATE_NONE = 0, GATE_DONE = 1, GATE_SECOND = 2 };
+__device__ __forceinline__ bool gated(const LanczosFlags* fl, int gate) {
+  if (gate == GATE_NONE) return false;
+  if (fl->done || fl->exhausted) return true;
+  if (gate == GATE_SECOND && !fl->second) return true;
+  return false;
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+// Deterministic block sum (result valid in thread 0).
+template <int NT>
+__device__ __forceinline__ double block_sum(double x, double* red) {
+  x = warp_sum(x);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = x;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < NT / 32; ++k) s += red[k];
+  return s;
+}
+
+__device__ __forceinline__ void chunk_of(int64_t len, int G, int64_t& b, int64_t& e) {
+  int64_t per = (len + G - 1) / G;
+  per = (per + 31) & ~(int64_t)31;
+  b = (int64_t)blockIdx.x * per;
+  e = b + per;
+  if (e > len) e = len;
+  if (b > len) b = len;
+}
+
+__device__ __forceinline__ int find_block(const int64_t* off, int nb, int64_t i) {
+  int lo = 0, hi = nb - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Seeded start vector (replaces Random.seed!(1234); randn(mdim),
+// shellmodel_main.jl:939-948): v[M] = u0+u1+u2+u3-2 with
+// u_k = (splitmix64(seed + φ·(4M+k+1)) >> 11)·2^-53.  Integer and exactly
+// rounded double operations only, so host and device agree bit for bit.
+__device__ __forceinline__ double start_elem(uint64_t seed, int64_t i) {
+  double u[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(4 * i + k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    u[k] = (double)(z >> 11) * 0x1.0p-53;
+  }
+  return __dsub_rn(__dadd_rn(__dadd_rn(u[0], u[1]), __dadd_rn(u[2], u[3])), 2.0);
+}
+
+__global__ void k_start_vector(DevTables t, uint64_t seed, double* __restrict__ w) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int b = find_block(t.off_pad, t.nb, i);
+    int64_t loc = i - t.off_pad[b];
+    int st = t.stride[b];
+    int p = (int)(loc / st), n = (int)(loc % st);
+    w[i] = (n < t.nn[b]) ? start_elem(seed, t.tdims[b] + (int64_t)p * t.nn[b] + n) : 0.0;
+  }
+}
+
+template <class TX>
+__global__ void k_to_padded(DevTables t, const double* __restrict__ src, TX* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int b = find_block(t.off_pad, t.nb, i);
+    int64_t loc = i - t.off_pad[b];
+    int st = t.stride[b];
+    int p = (int)(loc / st), n = (int)(loc % st);
+    dst[i] = (n < t.nn[b]) ? (TX)src[t.tdims[b] + (int64_t)p * t.nn[b] + n] : (TX)0;
+  }
+}
+__global__ void k_from_padded(DevTables t, const double* __restrict__ src, double* __restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int b = find_block(t.off_pad, t.nb, i);
+    int64_t loc = i - t.off_pad[b];
+    int st = t.stride[b];
+    int p = (int)(loc / st), n = (int)(loc % st);
+    if (n < t.nn[b]) dst[t.tdims[b] + (int64_t)p * t.nn[b] + n] = src[i];
+  }
+}
+
+// partials[j*G + cta] = Σ_{i in chunk} X_j[i]·y[i]  (j < m);  j = m: y·y if self.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int64_t ld, int m,
+                                                  const double* __restrict__ y, int64_t len, int self,
+                                                  double* __restrict__ partials, int G,
+                                                  const LanczosFlags* __restrict__ fl, int gate) {
+  if (gated(fl, gate)) return;
+  __shared__ double red[kNT / 32];
+  int64_t cb, ce;
+  chunk_of(len, G, cb, ce);
+  const int mt = m + (self ? 1 : 0);
+  for (int j0 = 0; j0 < mt; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
+      const double yi = y[i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = j0 + q;
+        if (j < m) acc[q] = fma((double)X[(int64_t)j * ld + i], yi, acc[q]);
+        else if (j == m && self) acc[q] = fma(yi, yi, acc[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q >= mt) break;
+      double s = block_sum<kNT>(acc[q], red);
+      if (threadIdx.x == 0) partials[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+    }
+  }
+}
+
+// y[i] -= Σ_j h[j]·X_j[i];  partials[cta] = Σ_{chunk} y_new[i]².
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_multiaxpy(const TX* __restrict__ X, int64_t ld, int m,
+                                                   const double* __restrict__ h, double* __restrict__ y,
+                                                   int64_t len, double* __restrict__ partials, int G,
+                                                   const LanczosFlags* __restrict__ fl, int gate) {
+  if (gated(fl, gate)) return;
+  extern __shared__ double sh[];  // m coefficients
+  __shared__ double red[kNT / 32];
+  for (int j = threadIdx.x; j < m; j += kNT) sh[j] = h[j];
+  __syncthreads();
+  int64_t cb, ce;
+  chunk_of(len, G, cb, ce);
+  double nrm = 0.0;
+  for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
+    double t = y[i];
+    for (int j = 0; j < m; ++j) t = fma(-sh[j], (double)X[(int64_t)j * ld + i], t);
+    y[i] = t;
+    nrm = fma(t, t, nrm);
+  }
+  double s = block_sum<kNT>(nrm, red);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kNT) k_reduce(const double* __restrict__ partials, int G, int m, int mode,
+                                                double* __restrict__ out, int it, int lm, double* __restrict__ T,
+                                                LanczosScalars* sc, LanczosFlags* fl, int gate) {
+  if (gated(fl, gate)) return;
+  __shared__ double red[kNT / 32];
+  const int mt = (mode == RED_H) ? m + 1 : m;
+  for (int j = 0; j < mt; ++j) {
+    double x = 0.0;
+    for (int g = threadIdx.x; g < G; g += kNT) x += partials[(int64_t)j * G + g];
+    double s = block_sum<kNT>(x, red);
+    if (threadIdx.x == 0) {
+      switch (mode) {
+        case RED_STORE: out[j] = s; break;
+        case RED_ALPHA: T[(int64_t)it * lm + it] = s; break;
+        case RED_H:
+          if (j < m) out[j] = s;
+          else sc->nrm_old = s;
+          break;
+        case RED_NRM_CHECK:
+          sc->nrm = s;
+          fl->second = (s < 0.5 * sc->nrm_old) ? 1 : 0;
+          if (fl->second) fl->n_second += 1;
+          break;
+        case RED_NRM: sc->nrm = s; break;
+        case RED_INVNORM: out[j] = 1.0 / sqrt(s); break;
+      }
+    }
+  }
+}
+
+// β = ||w||, T[it+1,it] = T[it,it+1] = β (it 0-based).  A zero β means the
+// Krylov space is exhausted: stop with the current T (elit = it+1).
+__global__ void k_beta(double* T, int lm, int it, LanczosScalars* sc, LanczosFlags* fl) {
+  if (fl->done || fl->exhausted) return;
+  double beta = sqrt(sc->nrm);
+  sc->beta = beta;
+  if (!(beta > 0.0) || !(beta < INFINITY)) {
+    fl->exh_k = it + 1;
+    fl->exhausted = 1;
+    return;
+  }
+  sc->inv_beta = 1.0 / beta;
+  T[(int64_t)it * lm + it + 1] = beta;
+  T[(int64_t)(it + 1) * lm + it] = beta;
+}
+
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_scale_store(const double* __restrict__ w, TX* __restrict__ out,
+                                                     const double* __restrict__ scale, int64_t len,
+                                                     const LanczosFlags* __restrict__ fl, int gate) {
+  if (gated(fl, gate)) return;
+  const double s = *scale;
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
+    out[i] = (TX)(w[i] * s);
+}
+
+// ---------------------------------------------------------------------------
+// Lowest eigenvalues of the k x k Lanczos matrix by Sturm counts
+// (diagonalize_T!, lanczos_methods.jl:250-258).  After a thick restart T is
+// an arrowhead (rows 0..lock-1 diagonal, coupled to row `lock`) followed by a
+// tridiagonal tail; the LDLᵀ inertia of T - σI is evaluated in O(k) for that
+// shape.  One warp bisects one eigenvalue with 32 trial shifts per step.
+__device__ int sturm_count(const double* a, const double* c2, const double* b2, int lock, int k, double sigma,
+                           double pivmin) {
+  int cnt = 0;
+  double acc = 0.0;
+  for (int i = 0; i < lock; ++i) {
+    double d = a[i] - sigma;
+    if (fabs(d) < pivmin) d = -pivmin;
+    if (d < 0.0) ++cnt;
+    acc += c2[i] / d;
+  }
+  double d = (a[lock] - sigma) - acc;
+  if (fabs(d) < pivmin) d = -pivmin;
+  if (d < 0.0) ++cnt;
+  for (int i = lock + 1; i < k; ++i) {
+    d = (a[i] - sigma) - b2[i - 1] / d;
+    if (fabs(d) < pivmin) d = -pivmin;
+    if (d < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+__global__ void k_sturm(const double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
+                        double tol, int64_t mdim, LanczosFlags* fl) {
+  if (fl->done) return;
+  if (fl->exhausted && k > fl->exh_k) {
+    // the Krylov space ended at exh_k; T_k was never completed
+    if (threadIdx.x == 0) { fl->done = 1; fl->elit = fl->exh_k; }
+    return;
+  }
+  extern __shared__ double sm[];
+  double* a = sm;            // k
+  double* c2 = a + lm;       // lock
+  double* b2 = c2 + lm;      // k-1
+  double* lam = b2 + lm;     // num_ev
+  __shared__ double s_lo, s_hi, s_piv;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < k; i += blockDim.x) {
+    a[i] = T[(int64_t)i * lm + i];
+    if (i < lock) { double x = T[(int64_t)i * lm + lock]; c2[i] = x * x; }
+    if (i >= lock && i + 1 < k) { double x = T[(int64_t)i * lm + i + 1]; b2[i] = x * x; }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // Gershgorin interval and pivot floor
+    double lo = INFINITY, hi = -INFINITY, mx = 1.0;
+    for (int i = 0; i < k; ++i) {
+      double r = 0.0;
+      if (i < lock) r = sqrt(c2[i]);
+      else {
+        if (i == lock) for (int j = 0; j < lock; ++j) r += sqrt(c2[j]);
+        if (i > lock) r += sqrt(b2[i - 1]);
+        if (i + 1 < k) r += sqrt(b2[i]);
+      }
+      lo = fmin(lo, a[i] - r);
+      hi = fmax(hi, a[i] + r);
+    }
+    for (int i = 0; i < lock; ++i) mx = fmax(mx, c2[i]);
+    for (int i = lock; i + 1 < k; ++i) mx = fmax(mx, b2[i]);
+    double w = hi - lo;
+    s_lo = lo - 1e-3 * w - 1e-300;
+    s_hi = hi + 1e-3 * w + 1e-300;
+    s_piv = DBL_MIN * mx;
+  }
+  __syncthreads();
+  const int n = min(num_ev, k);
+  const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  for (int e = wid; e < n; e += nw) {
+    double lo = s_lo, hi = s_hi;
+    for (int step = 0; step < 100; ++step) {
+      double sigma = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 33.0);
+      int cnt = sturm_count(a, c2, b2, lock, k, sigma, s_piv);
+      unsigned le = __ballot_sync(0xffffffffu, cnt <= e);
+      unsigned ge = __ballot_sync(0xffffffffu, cnt >= e + 1);
+      double nlo = lo, nhi = hi;
+      if (le) nlo = __shfl_sync(0xffffffffu, sigma, 31 - __clz(le));
+      if (ge) nhi = __shfl_sync(0xffffffffu, sigma, __ffs(ge) - 1);
+      lo = nlo;
+      hi = nhi;
+      if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 1e-300) break;
+    }
+    if (lane == 0) lam[e] = 0.5 * (lo + hi);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int hh = nh - 1; hh >= 1; --hh)
+      for (int j = 0; j < num_ev; ++j) en[hh * num_ev + j] = en[(hh - 1) * num_ev + j];
+    for (int j = 0; j < n; ++j) en[j] = lam[j];
+    bool conv = true;
+    for (int j = 0; j < num_ev; ++j)
+      if (!(en[num_ev + j] - en[j] < tol)) conv = false;
+    if (conv || (int64_t)k == mdim || (fl->exhausted && k == fl->exh_k)) {
+      fl->done = 1;
+      fl->elit = k;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric eigen-decomposition of T[0:n,0:n] by parallel cyclic Jacobi
+// (round-robin pairing, n/2 disjoint rotations per round) in one CTA.
+// Output: evals ascending, A = eigenvectors (column-major, ld n).
+template <int NT>
+__global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int ldt, int n, double* A, double* Z,
+                                               double* evals, const LanczosFlags* fl, int gate) {
+  if (gate && (fl->done || fl->exhausted)) return;
+  __shared__ double red[NT / 32];
+  __shared__ int s_stop;
+  extern __shared__ double shj[];
+  const int N = n + (n & 1);
+  const int npair = N / 2;
+  double* cc = shj;
+  double* ss = cc + npair;
+  double* dg = ss + npair;
+  int* pp = (int*)(dg + N);
+  int* qq = pp + npair;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < n * n; idx += NT) {
+    int i = idx % n, j = idx / n;
+    A[idx] = T[(int64_t)j * ldt + i];
+    Z[idx] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  double fro = 0.0;
+  for (int idx = tid; idx < n * n; idx += NT) fro += A[idx] * A[idx];
+  fro = block_sum<NT>(fro, red);
+  if (tid == 0) red[0] = fro;
+  __syncthreads();
+  fro = red[0];
+  __syncthreads();
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double off = 0.0;
+    for (int idx = tid; idx < n * n; idx += NT) {
+      int i = idx % n, j = idx / n;
+      if (i < j) off += A[idx] * A[idx];
+    }
+    off = block_sum<NT>(off, red);
+    if (tid == 0) s_stop = (off <= 1e-34 * fro || off == 0.0) ? 1 : 0;
+    __syncthreads();
+    if (s_stop) break;
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = tid; k < npair; k += NT) {
+        int p, q;
+        if (k == 0) { p = N - 1; q = r; }
+        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
+        if (p > q) { int x = p; p = q; q = x; }
+        double c = 1.0, s = 0.0;
+        if (q < n) {
+          double apq = A[(int64_t)q * n + p];
+          if (apq != 0.0) {
+            double app = A[(int64_t)p * n + p], aqq = A[(int64_t)q * n + q];
+            double theta = (aqq - app) / (2.0 * apq);
+            double t = (fabs(theta) > 1e150) ? 0.5 / theta
+                                              : (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
+            c = 1.0 / sqrt(1.0 + t * t);
+            s = t * c;
+          }
+        }
+        pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = s;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        int k = idx / n, i = idx % n;
+        if (ss[k] == 0.0) continue;
+        int p = pp[k], q = qq[k];
+        double c = cc[k], s = ss[k];
+        double aip = A[(int64_t)p * n + i], aiq = A[(int64_t)q * n + i];
+        A[(int64_t)p * n + i] = c * aip - s * aiq;
+        A[(int64_t)q * n + i] = s * aip + c * aiq;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        int k = idx / n, j = idx % n;
+        if (ss[k] == 0.0) continue;
+        int p = pp[k], q = qq[k];
+        double c = cc[k], s = ss[k];
+        double apj = A[(int64_t)j * n + p], aqj = A[(int64_t)j * n + q];
+        A[(int64_t)j * n + p] = c * apj - s * aqj;
+        A[(int64_t)j * n + q] = s * apj + c * aqj;
+      }
+      __syncthreads();
+      for (int k = tid; k < npair; k += NT)
+        if (ss[k] != 0.0) {
+          A[(int64_t)qq[k] * n + pp[k]] = 0.0;
+          A[(int64_t)pp[k] * n + qq[k]] = 0.0;
+        }
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        int k = idx / n, i = idx % n;
+        if (ss[k] == 0.0) continue;
+        int p = pp[k], q = qq[k];
+        double c = cc[k], s = ss[k];
+        double zip = Z[(int64_t)p * n + i], ziq = Z[(int64_t)q * n + i];
+        Z[(int64_t)p * n + i] = c * zip - s * ziq;
+        Z[(int64_t)q * n + i] = s * zip + c * ziq;
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = tid; i < n; i += NT) dg[i] = A[(int64_t)i * n + i];
+  __syncthreads();
+  for (int i = tid; i < n; i += NT) {
+    double d = dg[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j)
+      if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
+    evals[rank] = d;
+    for (int r = 0; r < n; ++r) A[(int64_t)rank * n + r] = Z[(int64_t)i * n + r];
+  }
+}
+
+// ThickRestart's small part (lanczos_methods.jl:261-271): new arrowhead T.
+__global__ void k_restart_small(double* T, int lm, int ls, const double* evals, const double* vecs,
+                                const LanczosFlags* fl) {
+  if (fl->done || fl->exhausted) return;
+  const int m = lm - 1;
+  __shared__ double beta;
+  if (threadIdx.x == 0) beta = T[(int64_t)(lm - 1) * lm + (lm - 2)];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < lm * lm; idx += blockDim.x) T[idx] = 0.0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < ls; k += blockDim.x) {
+    T[(int64_t)k * lm + k] = evals[k];
+    double tmp = beta * vecs[(int64_t)k * m + (m - 1)];
+    T[(int64_t)k * lm + ls] = tmp;
+    T[(int64_t)ls * lm + k] = tmp;
+  }
+}
+
+// U_k = Σ_{j<m} Y[j,k] V_j  (k < ls), FP64 accumulation.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V, TX* __restrict__ U,
+                                                        const double* __restrict__ Y, int m, int ls, int64_t len,
+                                                        const LanczosFlags* __restrict__ fl) {
+  if (fl->done || fl->exhausted) return;
+  extern __shared__ double yS[];  // m x ls
+  for (int idx = threadIdx.x; idx < m * ls; idx += kNT) yS[idx] = Y[(int64_t)(idx / m) * m + (idx % m)];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    for (int k0 = 0; k0 < ls; k0 += 8) {
+      double acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+      for (int j = 0; j < m; ++j) {
+        const double x = (double)V[(int64_t)j * len + i];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (k0 + q < ls) acc[q] = fma(yS[(k0 + q) * m + j], x, acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q];
+    }
+  }
+}
+
+// Gram matrix of U (upper triangle, packed row by row) and U_k·v_last.
+// Entry order: pairs (k,l) with k <= l in row-major order, then g_k.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX* __restrict__ vl, int ls,
+                                              int64_t len, double* __restrict__ partials, int G,
+                                              const LanczosFlags* __restrict__ fl) {
+  if (fl->done || fl->exhausted) return;
+  constexpr int TILE = 64;
+  extern __shared__ double tile[];  // (ls+1) x TILE
+  const int P = ls * (ls + 1) / 2 + ls;
+  int64_t cb, ce;
+  chunk_of(len, G, cb, ce);
+  double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int64_t t0 = cb; t0 < ce; t0 += TILE) {
+    const int cnt = (int)min((int64_t)TILE, ce - t0);
+    for (int idx = threadIdx.x; idx < (ls + 1) * TILE; idx += kNT) {
+      int j = idx / TILE, x = idx % TILE;
+      double val = 0.0;
+      if (x < cnt) val = (j < ls) ? (double)U[(int64_t)j * len + t0 + x] : (double)vl[t0 + x];
+      tile[idx] = val;
+    }
+    __syncthreads();
+    for (int q = 0; q < 8; ++q) {
+      int pr = threadIdx.x + q * kNT;
+      if (pr >= P) break;
+      int k, l;
+      if (pr < ls * (ls + 1) / 2) {
+        k = 0;
+        int rem = pr;
+        while (rem >= ls - k) { rem -= ls - k; ++k; }
+        l = k + rem;
+      } else {
+        k = pr - ls * (ls + 1) / 2;
+        l = ls;  // v_last
+      }
+      double s = acc[q];
+      for (int x = 0; x < cnt; ++x) s = fma(tile[k * TILE + x], tile[l * TILE + x], s);
+      acc[q] = s;
+    }
+    __syncthreads();
+  }
+  for (int q = 0; q < 8; ++q) {
+    int pr = threadIdx.x + q * kNT;
+    if (pr < P) partials[(int64_t)pr * G + blockIdx.x] = acc[q];
+  }
+}
+
+// Cholesky G = RᵀR, X = R⁻¹ (upper), c = Xᵀ g.  Single thread (ls is small).
+__global__ void k_chol(const double* __restrict__ gram, int ls, double* X, double* cvec, LanczosFlags* fl) {
+  if (fl->done || fl->exhausted || threadIdx.x != 0) return;
+  extern __shared__ double R[];  // ls x ls, column-major
+  auto G = [&](int k, int l) {  // k <= l
+    int off = 0;
+    for (int r = 0; r < k; ++r) off += ls - r;
+    return gram[off + (l - k)];
+  };
+  for (int j = 0; j < ls; ++j) {
+    for (int i = 0; i <= j; ++i) {
+      double s = G(i, j);
+      for (int k = 0; k < i; ++k) s -= R[j * ls + k] * R[i * ls + k];
+      if (i == j) {
+        if (!(s > 0.0)) { fl->bad = 1; s = 1e-300; }
+        R[j * ls + j] = sqrt(s);
+      } else {
+        R[j * ls + i] = s / R[i * ls + i];
+      }
+    }
+  }
+  for (int j = 0; j < ls; ++j) {
+    for (int i = ls - 1; i >= 0; --i) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int k = i + 1; k <= j; ++k) s -= R[k * ls + i] * X[j * ls + k];
+      X[j * ls + i] = (i <= j) ? s / R[i * ls + i] : 0.0;
+    }
+  }
+  const int gofs = ls * (ls + 1) / 2;
+  for (int k = 0; k < ls; ++k) {
+    double s = 0.0;
+    for (int j = 0; j <= k; ++j) s += X[k * ls + j] * gram[gofs + j];
+    cvec[k] = s;
+  }
+}
+
+// V_k = Σ_{j<=k} X[j,k] U_j (k < ls);  V_ls = V_{lm-1} - Σ_k c_k V_k.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U, TX* __restrict__ V,
+                                                       const double* __restrict__ X, const double* __restrict__ cvec,
+                                                       int ls, int lm, int64_t len,
+                                                       const LanczosFlags* __restrict__ fl) {
+  if (fl->done || fl->exhausted) return;
+  extern __shared__ double xs[];  // ls*ls + ls
+  for (int idx = threadIdx.x; idx < ls * ls; idx += kNT) xs[idx] = X[idx];
+  for (int idx = threadIdx.x; idx < ls; idx += kNT) xs[ls * ls + idx] = cvec[idx];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    double last = (double)V[(int64_t)(lm - 1) * len + i];
+    for (int k = 0; k < ls; ++k) {
+      double q = 0.0;
+      for (int j = 0; j <= k; ++j) q = fma(xs[k * ls + j], (double)U[(int64_t)j * len + i], q);
+      V[(int64_t)k * len + i] = (TX)q;
+      last = fma(-xs[ls * ls + k], q, last);
+    }
+    V[(int64_t)ls * len + i] = (TX)last;
+  }
+}
+
+// R_e = Σ_{k<elit} Y[k,e] V_k  (shellmodel_main.jl:210-214), FP64.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_ritz(const TX* __restrict__ V, const double* __restrict__ Y, int elit,
+                                              int nev, double* __restrict__ R, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    for (int e = 0; e < nev; ++e) {
+      double s = 0.0;
+      for (int k = 0; k < elit; ++k) s = fma(Y[(int64_t)e * elit + k], (double)V[(int64_t)k * len + i], s);
+      R[(int64_t)e * len + i] = s;
+    }
+  }
+}
+
+inline int grid_for(int64_t len) {
+  int64_t g = (len + kNT - 1) / kNT;
+  if (g > 152 * 8) g = 152 * 8;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st) {
+  k_start_vector<<<grid_for(t.len_pad), kNT, 0, st>>>(t, seed, w);
+}
+template <class TX>
+void launch_to_padded(const DevTables& t, const double* src, TX* dst, cudaStream_t st) {
+  k_to_padded<TX><<<grid_for(t.len_pad), kNT, 0, st>>>(t, src, dst);
+}
+void launch_from_padded(const DevTables& t, const double* src, double* dst, cudaStream_t st) {
+  k_from_padded<<<grid_for(t.len_pad), kNT, 0, st>>>(t, src, dst);
+}
+template <class TX>
+void launch_multidot(const LanczosDev& L, const TX* X, int m, const double* y, bool self, const int* gate,
+                     cudaStream_t st) {
+  int g = gate ? *gate : GATE_NONE;
+  k_multidot<TX><<<L.G, kNT, 0, st>>>(X, L.len, m, y, L.len, self ? 1 : 0, L.partials, L.G, L.fl, g);
+}
+void launch_reduce(const LanczosDev& L, int m, ReduceMode mode, double* out, int it, const int* gate,
+                   cudaStream_t st) {
+  int g = gate ? *gate : GATE_NONE;
+  k_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, m, (int)mode, out, it, L.lm, L.T, L.sc, L.fl, g);
+}
+template <class TX>
+void launch_multiaxpy(const LanczosDev& L, const TX* X, int m, double* y, const int* gate, cudaStream_t st) {
+  int g = gate ? *gate : GATE_NONE;
+  k_multiaxpy<TX><<<L.G, kNT, sizeof(double) * (m > 0 ? m : 1), st>>>(X, L.len, m, L.h, y, L.len, L.partials, L.G,
+                                                                        L.fl, g);
+}
+void launch_beta(const LanczosDev& L, int it, cudaStream_t st) { k_beta<<<1, 1, 0, st>>>(L.T, L.lm, it, L.sc, L.fl); }
+template <class TX>
+void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const double* scale, const int* gate,
+                        cudaStream_t st) {
+  int g = gate ? *gate : GATE_NONE;
+  k_scale_store<TX><<<grid_for(L.len), kNT, 0, st>>>(w, out, scale, L.len, L.fl, g);
+}
+void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
+  int warps = L.num_ev < 32 ? L.num_ev : 32;
+  if (warps < 1) warps = 1;
+  size_t shm = sizeof(double) * (3 * (size_t)L.lm + L.num_ev);
+  k_sturm<<<1, 32 * warps, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.fl);
+}
+void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st) {
+  int N = n + (n & 1);
+  size_t shm = sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+  k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
+}
+void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
+  k_restart_small<<<1, 256, 0, st>>>(L.T, L.lm, L.ls, L.evals, L.jacA, L.fl);
+}
+template <class TX>
+void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st) {
+  int m = L.lm - 1;
+  k_restart_rotate<TX><<<grid_for(L.len), kNT, sizeof(double) * m * L.ls, st>>>(V, U, L.jacA, m, L.ls, L.len, L.fl);
+}
+template <class TX>
+void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
+  k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 64, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
+}
+void launch_chol(const LanczosDev& L, cudaStream_t st) {
+  k_chol<<<1, 32, sizeof(double) * L.ls * L.ls, st>>>(L.gram, L.ls, L.X, L.cvec, L.fl);
+}
+template <class TX>
+void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st) {
+  k_restart_apply<TX><<<grid_for(L.len), kNT, sizeof(double) * (L.ls * L.ls + L.ls), st>>>(U, V, L.X, L.cvec, L.ls,
+                                                                                             L.lm, L.len, L.fl);
+}
+template <class TX>
+void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R, cudaStream_t st) {
+  k_ritz<TX><<<grid_for(L.len), kNT, 0, st>>>(V, L.jacA, elit, nev, R, L.len);
+}
+
+#define SMGPU_INST(TX)                                                                                       \
+  template void launch_to_padded<TX>(const DevTables&, const double*, TX*, cudaStream_t);                    \
+  template void launch_multidot<TX>(const LanczosDev&, const TX*, int, const double*, bool, const int*,      \
+                                    cudaStream_t);                                                           \
+  template void launch_multiaxpy<TX>(const LanczosDev&, const TX*, int, double*, const int*, cudaStream_t);  \
+  template void launch_scale_store<TX>(const LanczosDev&, const double*, TX*, const double*, const int*,     \
+                                       cudaStream_t);                                                        \
+  template void launch_restart_rotate<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                  \
+  template void launch_gram<TX>(const LanczosDev&, const TX*, const TX*, cudaStream_t);                      \
+  template void launch_restart_apply<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                   \
+  template void launch_ritz<TX>(const LanczosDev&, const TX*, int, int, double*, cudaStream_t);
+SMGPU_INST(double)
+SMGPU_INST(float)
+#undef SMGPU_INST
+
+}  // namespace smgpu

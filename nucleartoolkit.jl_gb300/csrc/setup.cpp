@@ -1,0 +1,697 @@
+// Host-side set-up of a shell-model problem for the GPU kernels.
+//
+// Restates, for the GPU table layout, what NuclearToolkit.jl does before its
+// Lanczos loop (paths relative to the NuclearToolkit.jl source tree):
+//   readsmsnt          src/ShellModel/shellmodel_main.jl:293-365
+//   construct_msps     :373-384      occ (basis, blocks)  :769-848
+//   prep_Hamil_T1      :580-649      prep_2bjumps         :1115-1137
+//   prep_Hamil_pn      :658-730      prep_pn/calc_1b_jumps! :1139-1199
+// The m-scheme matrix elements are accumulated in the reference's loop and
+// insertion order, so every operator value is bit-identical to the
+// reference's.  The jump tables are re-organised for the GPU: instead of the
+// reference's per-(block pair, V entry) lists they are "pull" tables in which
+// every output row of H·v lists the source rows it reads (see hv.cu).
+#include "setup.h"
+
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <unordered_map>
+
+#include "../../include/smgpu.h"
+
+namespace smgpu {
+
+// ---------------------------------------------------------------- parsing
+namespace {
+std::string trim(const std::string& s) {
+  size_t b = s.find_first_not_of(" \t\r\n");
+  if (b == std::string::npos) return std::string();
+  size_t e = s.find_last_not_of(" \t\r\n");
+  return s.substr(b, e - b + 1);
+}
+// Fields separated by single spaces (empty fields dropped), as
+// rm_nan(split(line," ")) in util_func.jl:40-46.
+std::vector<std::string> tokens(const std::string& line) {
+  std::vector<std::string> out;
+  size_t i = 0;
+  while (i < line.size()) {
+    while (i < line.size() && line[i] == ' ') ++i;
+    size_t j = i;
+    while (j < line.size() && line[j] != ' ') ++j;
+    if (j > i) out.push_back(line.substr(i, j - i));
+    i = j;
+  }
+  return out;
+}
+int to_int(const std::string& s) {
+  char* end = nullptr;
+  long v = std::strtol(s.c_str(), &end, 10);
+  if (end == s.c_str() || *end != '\0') throw SetupError{SMGPU_ERR_PARSE, "not an integer: '" + s + "'"};
+  return (int)v;
+}
+double to_dbl(const std::string& s) {
+  char* end = nullptr;
+  double v = std::strtod(s.c_str(), &end);
+  if (end == s.c_str() || *end != '\0') throw SetupError{SMGPU_ERR_PARSE, "not a number: '" + s + "'"};
+  return v;
+}
+}  // namespace
+
+Interaction read_snt(const std::string& path, int Anum) {
+  std::ifstream f(path);
+  if (!f) throw SetupError{SMGPU_ERR_IO, "cannot open interaction file " + path};
+  // util_func.jl:26-38 rm_comment: lines starting with '!' or '#' go, blank lines stay.
+  std::vector<std::string> lines;
+  std::string raw;
+  while (std::getline(f, raw)) {
+    std::string t = trim(raw);
+    if (!t.empty() && (t[0] == '!' || t[0] == '#')) continue;
+    lines.push_back(t);
+  }
+  size_t cur = 0;
+  auto next = [&](size_t need) {
+    if (cur >= lines.size()) throw SetupError{SMGPU_ERR_PARSE, "interaction file ends early"};
+    auto t = tokens(lines[cur++]);
+    if (t.size() < need) throw SetupError{SMGPU_ERR_PARSE, "too few fields on an snt line"};
+    return t;
+  };
+  Interaction I;
+  auto h = next(4);
+  I.lp = to_int(h[0]); I.ln = to_int(h[1]); I.cp = to_int(h[2]); I.cn = to_int(h[3]);
+  if (I.lp <= 0 || I.ln <= 0 || I.lp > 64 || I.ln > 64) throw SetupError{SMGPU_ERR_PARSE, "bad orbit counts"};
+  I.porb.assign(I.lp, Orbit{-1, -1, -1, 0});
+  I.norb.assign(I.ln, Orbit{-1, -1, -1, 0});
+  for (int k = 0; k < I.lp + I.ln; ++k) {
+    auto t = next(5);
+    int idx = to_int(t[0]);
+    Orbit o{to_int(t[1]), to_int(t[2]), to_int(t[3]), to_int(t[4])};
+    if (idx >= 1 && idx <= I.lp) I.porb[idx - 1] = o;
+    else if (idx > I.lp && idx <= I.lp + I.ln) I.norb[idx - I.lp - 1] = o;
+    else throw SetupError{SMGPU_ERR_PARSE, "orbit index out of range"};
+  }
+  for (auto& o : I.porb) if (o.j2 < 0) throw SetupError{SMGPU_ERR_PARSE, "missing proton orbit"};
+  for (auto& o : I.norb) if (o.j2 < 0) throw SetupError{SMGPU_ERR_PARSE, "missing neutron orbit"};
+  // SPE block: only the first column selects the orbit, the third is the value.
+  auto hs = next(2);
+  int nsp = to_int(hs[0]);
+  I.spe_p.assign(I.lp, 0.0);
+  I.spe_n.assign(I.ln, 0.0);
+  for (int k = 0; k < nsp; ++k) {
+    auto t = next(3);
+    int j = to_int(t[0]);
+    if (j >= 1 && j <= I.lp) I.spe_p[j - 1] = to_dbl(t[2]);
+    else if (j > I.lp && j <= I.lp + I.ln) I.spe_n[j - I.lp - 1] = to_dbl(t[2]);
+    else throw SetupError{SMGPU_ERR_PARSE, "SPE index out of range"};
+  }
+  auto ht = next(3);
+  int ntbme = to_int(ht[0]);
+  int massop = to_int(ht[1]);
+  double Aref = to_dbl(ht[2]);
+  double pw = ht.size() > 3 ? to_dbl(ht[3]) : 0.0;
+  for (int k = 0; k < ntbme; ++k) {
+    auto t = next(6);
+    int a = to_int(t[0]), b = to_int(t[1]), c = to_int(t[2]), d = to_int(t[3]), J = to_int(t[4]);
+    double v = to_dbl(t[5]);
+    int kind;
+    if (a <= I.lp && b <= I.lp) kind = 0;
+    else if (a > I.lp && b > I.lp) kind = 1;
+    else if (a <= I.lp && b > I.lp) kind = 2;
+    else throw SetupError{SMGPU_ERR_PARSE, "TBME with the proton index after the neutron index"};
+    int lim = I.lp + I.ln;
+    if (a < 1 || b < 1 || c < 1 || d < 1 || a > lim || b > lim || c > lim || d > lim)
+      throw SetupError{SMGPU_ERR_PARSE, "TBME orbit index out of range"};
+    if (massop == 1) v *= std::pow((double)Anum / Aref, pw);
+    // readsmsnt adds (c,d,a,b) first when unique([a,b]) != unique([c,d]) (:354-357)
+    bool same = (a == b) ? (c == d && c == a) : (c != d && a == c && b == d);
+    if (!same) I.tb[kind].push_back({c, d, a, b, J, v});
+    I.tb[kind].push_back({a, b, c, d, J, v});
+  }
+  return I;
+}
+
+void parse_nucleus(const std::string& nuc, int& A, int& Z) {
+  static const char* el[] = {
+      "n",  "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",  "S",
+      "Cl", "Ar", "K",  "Ca", "Sc", "Ti", "V",  "Cr", "Mn", "Fe", "Co", "Ni", "Cu", "Zn", "Ga", "Ge", "As",
+      "Se", "Br", "Kr", "Rb", "Sr", "Y",  "Zr", "Nb", "Mo", "Tc", "Ru", "Rh", "Pd", "Ag", "Cd", "In", "Sn",
+      "Sb", "Te", "I",  "Xe", "Cs", "Ba", "La", "Ce", "Pr", "Nd", "Pm", "Sm", "Eu", "Gd", "Tb", "Dy", "Ho",
+      "Er", "Tm", "Yb", "Lu", "Hf", "Ta", "W",  "Re", "Os", "Ir", "Pt", "Au", "Hg", "Tl", "Pb", "Bi", "Po",
+      "At", "Rn", "Fr", "Ra", "Ac", "Th", "Pa", "U",  "Np", "Pu", "Am", "Cm", "Bk", "Cf", "Es", "Fm", "Md",
+      "No", "Lr", "Rf", "Db", "Sg", "Bh", "Hs", "Mt", "Ds", "Rg", "Cn", "Nh", "Fl", "Mc", "Lv", "Ts", "Og"};
+  size_t d0 = nuc.find_first_of("0123456789");
+  if (d0 == std::string::npos) throw SetupError{SMGPU_ERR_NUCLEUS, "no mass number in '" + nuc + "'"};
+  size_t d1 = nuc.find_first_not_of("0123456789", d0);
+  std::string digits = nuc.substr(d0, d1 == std::string::npos ? std::string::npos : d1 - d0);
+  A = to_int(digits);
+  if (A <= 0) throw SetupError{SMGPU_ERR_NUCLEUS, "invalid mass number in '" + nuc + "'"};
+  // replace(target_nuc, string(Anum) => ""): remove every occurrence
+  std::string s = nuc, a = std::to_string(A);
+  for (size_t p; (p = s.find(a)) != std::string::npos;) s.erase(p, a.size());
+  Z = -1;
+  for (int z = 1; z < (int)(sizeof(el) / sizeof(el[0])); ++z)
+    if (s == el[z]) { Z = z; break; }
+  if (Z < 0) throw SetupError{SMGPU_ERR_NUCLEUS, "unknown element in '" + nuc + "'"};
+}
+
+// ------------------------------------------------------ Clebsch–Gordan
+// ⟨j1 m1 j2 m2|J M⟩ = sign(S)·sqrt(S²·C(2j1,n1)C(2j2,n1)(2J+1) /
+//   [(j1+j2+J+1)·C(j1+j2+J,n1)·C(2j1,j1-m1)·C(2j2,j2-m2)·C(2J,J-M)])
+// with n1 = j1+j2-J, n2 = j1-j2+J, n3 = j2-j1+J and the integer
+// S = Σ_k (-1)^k C(n1,k) C(n2,j1-m1-k) C(n3,j2+m2-k) — Racah's sum
+// rewritten in binomials.  The square is reduced exactly before the final
+// sqrt, so the result is the rounded square root of the rounded quotient.
+namespace {
+typedef __int128 i128;
+i128 binom(int n, int k) {
+  if (k < 0 || k > n) return 0;
+  if (k > n - k) k = n - k;
+  i128 r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+i128 gcd_(i128 a, i128 b) {
+  if (a < 0) a = -a;
+  if (b < 0) b = -b;
+  while (b != 0) { i128 t = a % b; a = b; b = t; }
+  return a;
+}
+}  // namespace
+
+double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
+  if (tm1 + tm2 != tM) return 0.0;
+  if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return 0.0;
+  if (((tj1 + tm1) | (tj2 + tm2) | (tJ + tM)) & 1) return 0.0;
+  if (tJ > tj1 + tj2 || tJ < std::abs(tj1 - tj2) || ((tj1 + tj2 + tJ) & 1)) return 0.0;
+  int n1 = (tj1 + tj2 - tJ) / 2, n2 = (tj1 - tj2 + tJ) / 2, n3 = (tj2 - tj1 + tJ) / 2;
+  int j1mm1 = (tj1 - tm1) / 2, j2pm2 = (tj2 + tm2) / 2;
+  i128 S = 0;
+  for (int k = 0; k <= n1; ++k) {
+    i128 t = binom(n1, k) * binom(n2, j1mm1 - k) * binom(n3, j2pm2 - k);
+    S += (k & 1) ? -t : t;
+  }
+  if (S == 0) return 0.0;
+  int s3 = (tj1 + tj2 + tJ) / 2;
+  i128 num = S * S, den = 1;
+  auto mul_num = [&](i128 x) { i128 g = gcd_(x, den); num *= x / g; den /= g; g = gcd_(num, den); num /= g; den /= g; };
+  auto mul_den = [&](i128 x) { i128 g = gcd_(x, num); den *= x / g; num /= g; g = gcd_(num, den); num /= g; den /= g; };
+  mul_num(binom(tj1, n1));
+  mul_num(binom(tj2, n1));
+  mul_num(tJ + 1);
+  mul_den(s3 + 1);
+  mul_den(binom(s3, n1));
+  mul_den(binom(tj1, j1mm1));
+  mul_den(binom(tj2, (tj2 - tm2) / 2));
+  mul_den(binom(tJ, (tJ - tM) / 2));
+  double v = std::sqrt((double)num / (double)den);
+  return S < 0 ? -v : v;
+}
+
+// ------------------------------------------------------------- helpers
+namespace {
+inline int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+// ⟨f|a†c|i⟩ for one-hot masks a (create) and c (annihilate).  Returns false
+// when not connectable.  `odd` = parity of the fermion sign count: occupied
+// states at or above c in i, then at or above a after removing c
+// (calc_phase_1!, shellmodel_main.jl:887-897, without its constant offset,
+// which cancels between the proton and neutron factors).
+inline bool apply1(uint64_t i, uint64_t a, uint64_t c, uint64_t& f, int& odd) {
+  if ((i & c) == 0) return false;
+  uint64_t r = i & ~c;
+  if (r & a) return false;
+  int cnt = popc(i & ~(c - 1)) + popc(r & ~(a - 1));
+  f = r | a;
+  odd = cnt & 1;
+  return true;
+}
+// ⟨f|a†b†dc|i⟩ (TF_connectable + calc_phase!, shellmodel_main.jl:850-885).
+inline bool apply2(uint64_t i, const Op2& o, uint64_t& f, int& odd) {
+  if ((i & o.c) != o.c || (i & o.d) != o.d) return false;
+  uint64_t r = i & ~o.c & ~o.d;
+  if ((r & o.a) || (r & o.b)) return false;
+  int cnt = popc(i & ~(o.c - 1));
+  uint64_t x = i & ~o.c;
+  cnt += popc(x & ~(o.d - 1));
+  x &= ~o.d;
+  cnt += popc(x & ~(o.b - 1));
+  x |= o.b;
+  cnt += popc(x & ~(o.a - 1));
+  f = x | o.a;
+  odd = cnt & 1;
+  return true;
+}
+// Index of `x` in a descending list, or -1 (bisearch!, :1068-1083).
+inline int find_desc(const uint64_t* v, int n, uint64_t x) {
+  int lo = 0, hi = n - 1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    if (v[mid] > x) lo = mid + 1;
+    else if (v[mid] < x) hi = mid - 1;
+    else return mid;
+  }
+  return -1;
+}
+
+struct Key4 {
+  uint64_t a, b, c, d;
+  bool operator==(const Key4& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
+};
+struct Key4H {
+  size_t operator()(const Key4& k) const {
+    uint64_t h = k.a * 0x9E3779B97F4A7C15ull ^ (k.b + 0x632BE59BD9B4E019ull);
+    h = (h ^ (h >> 29)) * 0xBF58476D1CE4E5B9ull ^ (k.c * 0x94D049BB133111EBull);
+    h = (h ^ (h >> 31)) * 0x9E3779B97F4A7C15ull ^ (k.d + 0x2545F4914F6CDD1Dull);
+    return (size_t)(h ^ (h >> 32));
+  }
+};
+// Operator list with first-insertion order and in-place accumulation: same
+// order and sums as the reference's `tl in blist` linear search.
+struct OpList {
+  std::vector<Op2> ops;
+  std::unordered_map<Key4, size_t, Key4H> where;
+  void add(uint64_t a, uint64_t b, uint64_t c, uint64_t d, double v) {
+    Key4 k{a, b, c, d};
+    auto it = where.find(k);
+    if (it == where.end()) {
+      where.emplace(k, ops.size());
+      ops.push_back(Op2{a, b, c, d, v});
+    } else {
+      ops[it->second].v += v;
+    }
+  }
+};
+
+std::vector<MState> msps(const std::vector<Orbit>& orb) {
+  std::vector<MState> m;
+  for (size_t o = 0; o < orb.size(); ++o)
+    for (int m2 = -orb[o].j2; m2 <= orb[o].j2; m2 += 2) m.push_back(MState{(int)o, orb[o].j2, m2});
+  return m;
+}
+inline uint64_t bit_of(int L, int k0) { return 1ull << (L - 1 - k0); }
+// m-state indices of orbit o (possible_mz, :552-565)
+std::vector<int> mstates_of(const std::vector<MState>& ms, int o) {
+  std::vector<int> r;
+  for (size_t k = 0; k < ms.size(); ++k)
+    if (ms[k].orbit == o) r.push_back((int)k);
+  return r;
+}
+
+// Lexicographic k-combinations of L m-states as bit strings (descending ints).
+void combos(int L, int k, std::vector<uint64_t>& bits, std::vector<int>& M, const std::vector<MState>& ms) {
+  bits.clear();
+  M.clear();
+  if (k > L) return;
+  std::vector<int> c(k);
+  for (int i = 0; i < k; ++i) c[i] = i;
+  while (true) {
+    uint64_t b = 0;
+    int m = 0;
+    for (int i = 0; i < k; ++i) { b |= bit_of(L, c[i]); m += ms[c[i]].m2; }
+    bits.push_back(b);
+    M.push_back(m);
+    int i = k - 1;
+    while (i >= 0 && c[i] == L - k + i) --i;
+    if (i < 0) break;
+    ++c[i];
+    for (int j = i + 1; j < k; ++j) c[j] = c[j - 1] + 1;
+  }
+}
+
+// prep_Hamil_T1 (:580-649) for one species.
+std::vector<Op2> two_body_ops(const std::vector<Interaction::TB>& tbs, const std::vector<Orbit>& orb,
+                              const std::vector<MState>& ms, int loff) {
+  int L = (int)ms.size();
+  OpList list;
+  for (const auto& t : tbs) {
+    int oa = t.a - 1 - loff, ob = t.b - 1 - loff, oc = t.c - 1 - loff, od = t.d - 1 - loff;
+    auto ia = mstates_of(ms, oa), ib = mstates_of(ms, ob), ic = mstates_of(ms, oc), id = mstates_of(ms, od);
+    int J2 = 2 * t.J;
+    double nfac = std::sqrt((1.0 + (t.a == t.b ? 1.0 : 0.0)) * (1.0 + (t.c == t.d ? 1.0 : 0.0)));
+    for (int kc : ic)
+      for (int kd : id) {
+        int mc = ms[kc].m2, md = ms[kd].m2;
+        if (t.c == t.d && mc >= md) continue;
+        if (std::abs(mc + md) > J2) continue;
+        int Mani = mc + md;
+        for (int ka : ia)
+          for (int kb : ib) {
+            int ma = ms[ka].m2, mb = ms[kb].m2;
+            if (t.a == t.b && ma >= mb) continue;
+            if (ma + mb != Mani) continue;
+            double cg1 = clebsch_gordan(orb[oa].j2, ma, orb[ob].j2, mb, J2, Mani);
+            double cg2 = clebsch_gordan(orb[oc].j2, mc, orb[od].j2, md, J2, Mani);
+            list.add(bit_of(L, ka), bit_of(L, kb), bit_of(L, kc), bit_of(L, kd), t.v * nfac * cg1 * cg2);
+          }
+      }
+  }
+  return list.ops;
+}
+}  // namespace
+
+// ------------------------------------------------------------ build_tables
+void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
+  T = Tables();
+  T.msp = msps(I.porb);
+  T.msn = msps(I.norb);
+  T.Lp = (int)T.msp.size();
+  T.Ln = (int)T.msn.size();
+  if (T.Lp > 63 || T.Ln > 63) throw SetupError{SMGPU_ERR_LIMIT, "more than 63 m-states per species"};
+  if (vp < 0 || vn < 0 || vp > T.Lp || vn > T.Ln) throw SetupError{SMGPU_ERR_NUCLEUS, "invalid valence particle numbers"};
+
+  // ---- basis (occ, :769-848)
+  std::vector<uint64_t> pall, nall;
+  std::vector<int> Mpall, Mnall;
+  combos(T.Lp, vp, pall, Mpall, T.msp);
+  combos(T.Ln, vn, nall, Mnall, T.msn);
+  std::vector<int> Mps = Mpall, Mns = Mnall;
+  std::sort(Mps.begin(), Mps.end());
+  Mps.erase(std::unique(Mps.begin(), Mps.end()), Mps.end());
+  std::sort(Mns.begin(), Mns.end());
+  Mns.erase(std::unique(Mns.begin(), Mns.end()), Mns.end());
+  std::reverse(Mns.begin(), Mns.end());
+  T.tdims.push_back(0);
+  T.off_pad.push_back(0);
+  T.pstart.push_back(0);
+  T.nstart.push_back(0);
+  for (int Mp : Mps)
+    for (int Mn : Mns) {
+      if (Mp + Mn != mtot2) continue;
+      int np = 0, nn = 0;
+      for (size_t i = 0; i < pall.size(); ++i)
+        if (Mpall[i] == Mp) { T.pbits.push_back(pall[i]); ++np; }
+      for (size_t j = 0; j < nall.size(); ++j)
+        if (Mnall[j] == Mn) { T.nbits.push_back(nall[j]); ++nn; }
+      int stride = (nn + 3) & ~3;
+      T.np.push_back(np);
+      T.nn.push_back(nn);
+      T.stride.push_back(stride);
+      T.mp2.push_back(Mp);
+      T.mn2.push_back(Mn);
+      T.tdims.push_back(T.tdims.back() + (int64_t)np * nn);
+      T.off_pad.push_back(T.off_pad.back() + (int64_t)np * stride);
+      T.pstart.push_back(T.pstart.back() + np);
+      T.nstart.push_back(T.nstart.back() + nn);
+    }
+  T.nb = (int)T.np.size();
+  T.mdim = T.tdims.back();
+  T.len_pad = T.off_pad.back();
+  if (T.mdim == 0) return;
+  const int nb = T.nb;
+  const int64_t NP = T.pstart[nb], NN = T.nstart[nb];
+
+  // one-body diagonal: dot(SPEs, jocc) per SD
+  T.ep.assign(NP, 0.0);
+  T.en.assign(NN, 0.0);
+  for (int64_t g = 0; g < NP; ++g) {
+    std::vector<double> occ(I.lp, 0.0);
+    for (int k = 0; k < T.Lp; ++k)
+      if (T.pbits[g] & bit_of(T.Lp, k)) occ[T.msp[k].orbit] += 1.0;
+    double s = 0.0;
+    for (int o = 0; o < I.lp; ++o) s += I.spe_p[o] * occ[o];
+    T.ep[g] = s;
+  }
+  for (int64_t g = 0; g < NN; ++g) {
+    std::vector<double> occ(I.ln, 0.0);
+    for (int k = 0; k < T.Ln; ++k)
+      if (T.nbits[g] & bit_of(T.Ln, k)) occ[T.msn[k].orbit] += 1.0;
+    double s = 0.0;
+    for (int o = 0; o < I.ln; ++o) s += I.spe_n[o] * occ[o];
+    T.en[g] = s;
+  }
+
+  // ---- pp / nn operators and their pull CSR (prep_Hamil_T1 + prep_2bjumps)
+  T.vpp = two_body_ops(I.tb[0], I.porb, T.msp, 0);
+  T.vnn = two_body_ops(I.tb[1], I.norb, T.msn, I.lp);
+  auto build_2b = [&](const std::vector<Op2>& ops, const std::vector<uint64_t>& bits, const std::vector<int>& start,
+                      std::vector<int>& ptr, std::vector<int>& col, std::vector<double>& val) {
+    // index of the hermitian conjugate (c,d,a,b) of each operator
+    std::unordered_map<Key4, size_t, Key4H> where;
+    for (size_t k = 0; k < ops.size(); ++k) where.emplace(Key4{ops[k].a, ops[k].b, ops[k].c, ops[k].d}, k);
+    std::vector<long> conj(ops.size());
+    for (size_t k = 0; k < ops.size(); ++k) {
+      auto it = where.find(Key4{ops[k].c, ops[k].d, ops[k].a, ops[k].b});
+      conj[k] = it == where.end() ? -1 : (long)it->second;
+    }
+    int64_t nrow = start[nb];
+    std::vector<std::vector<std::pair<int, double>>> rows(nrow);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t g = 0; g < nrow; ++g) {
+      int b = (int)(std::upper_bound(start.begin(), start.end(), (int)g) - start.begin()) - 1;
+      const uint64_t* blk = bits.data() + start[b];
+      int n = start[b + 1] - start[b];
+      int i = (int)(g - start[b]);
+      auto& row = rows[g];
+      for (size_t k = 0; k < ops.size(); ++k) {
+        if (ops[k].v == 0.0) continue;
+        uint64_t f;
+        int odd;
+        if (!apply2(bits[g], ops[k], f, odd)) continue;
+        int j = find_desc(blk, n, f);
+        if (j < 0) continue;
+        double v = ops[k].v;
+        if (j < i && conj[k] >= 0) {
+          // the reference stores this pair on row j with the conjugate operator
+          uint64_t f2;
+          int odd2;
+          if (apply2(f, ops[conj[k]], f2, odd2) && f2 == bits[g] && ops[conj[k]].v != 0.0) {
+            v = ops[conj[k]].v;
+            odd = odd2;
+          }
+        }
+        row.push_back({j, odd ? -v : v});
+      }
+      // merge equal columns, keeping the list order inside each column
+      std::stable_sort(row.begin(), row.end(), [](const std::pair<int, double>& x, const std::pair<int, double>& y) {
+        return x.first < y.first;
+      });
+      std::vector<std::pair<int, double>> merged;
+      for (auto& e : row) {
+        if (!merged.empty() && merged.back().first == e.first) merged.back().second += e.second;
+        else merged.push_back(e);
+      }
+      row.swap(merged);
+    }
+    ptr.assign(nrow + 1, 0);
+    for (int64_t g = 0; g < nrow; ++g) ptr[g + 1] = ptr[g] + (int)rows[g].size();
+    col.resize(ptr[nrow]);
+    val.resize(ptr[nrow]);
+    for (int64_t g = 0; g < nrow; ++g)
+      for (size_t k = 0; k < rows[g].size(); ++k) {
+        col[ptr[g] + k] = rows[g][k].first;
+        val[ptr[g] + k] = rows[g][k].second;
+      }
+  };
+  build_2b(T.vpp, T.pbits, T.pstart, T.pp_ptr, T.pp_col, T.pp_val);
+  build_2b(T.vnn, T.nbits, T.nstart, T.nn_ptr, T.nn_col, T.nn_val);
+
+  // ---- pn operators (prep_Hamil_pn, :658-730)
+  {
+    std::vector<int> Mzs;
+    for (int j = 0; j < T.Lp; ++j)
+      for (int i = 0; i < T.Lp; ++i) Mzs.push_back(T.msp[i].m2 - T.msp[j].m2);
+    std::sort(Mzs.begin(), Mzs.end());
+    Mzs.erase(std::unique(Mzs.begin(), Mzs.end()), Mzs.end());
+    std::reverse(Mzs.begin(), Mzs.end());
+    T.delMs = Mzs;
+    std::vector<OpList> lists(Mzs.size());
+    for (const auto& t : I.tb[2]) {
+      int oa = t.a - 1, oc = t.c - 1, ob = t.b - 1 - I.lp, od = t.d - 1 - I.lp;
+      auto ia = mstates_of(T.msp, oa), ic = mstates_of(T.msp, oc);
+      auto ib = mstates_of(T.msn, ob), id = mstates_of(T.msn, od);
+      int J2 = 2 * t.J;
+      for (int kc : ic) {
+        int mc = T.msp[kc].m2;
+        for (int ka : ia) {
+          int ma = T.msp[ka].m2;
+          int Mp = ma - mc;
+          int idx = (int)(std::find(Mzs.begin(), Mzs.end(), Mp) - Mzs.begin());
+          for (int kd : id) {
+            int md = T.msn[kd].m2;
+            if (std::abs(mc + md) > J2) continue;
+            double tfac = t.v * clebsch_gordan(I.porb[oc].j2, mc, I.norb[od].j2, md, J2, mc + md);
+            for (int kb : ib) {
+              int mb = T.msn[kb].m2;
+              if (mb - md + Mp != 0) continue;
+              double fac = tfac * clebsch_gordan(I.porb[oa].j2, ma, I.norb[ob].j2, mb, J2, ma + mb);
+              lists[idx].add(bit_of(T.Lp, ka), bit_of(T.Ln, kb), bit_of(T.Lp, kc), bit_of(T.Ln, kd), fac);
+            }
+          }
+        }
+      }
+    }
+    T.vpn.resize(Mzs.size());
+    for (size_t k = 0; k < Mzs.size(); ++k) T.vpn[k] = lists[k].ops;
+  }
+
+  // V tables: per ΔM, distinct proton operators (a,c) and neutron operators
+  // (b,d) among the non-zero entries, in first-appearance order.
+  const size_t ndm = T.delMs.size();
+  T.vtab_off_dm.assign(ndm + 1, 0);
+  T.nA_dm.assign(ndm, 0);
+  T.nB_dm.assign(ndm, 0);
+  std::vector<std::vector<std::pair<uint64_t, uint64_t>>> Aops(ndm), Bops(ndm);
+  for (size_t k = 0; k < ndm; ++k) {
+    std::unordered_map<uint64_t, int> ai, bi;
+    std::vector<std::pair<int, int>> cells;
+    for (const Op2& o : T.vpn[k]) {
+      if (o.v == 0.0) { cells.push_back({-1, -1}); continue; }
+      uint64_t ka = o.a * 131ull + o.c * 7919ull + (o.a ^ (o.c << 1));
+      uint64_t kb = o.b * 131ull + o.d * 7919ull + (o.b ^ (o.d << 1));
+      // exact keys: one-hot masks identify m-states uniquely
+      ka = (uint64_t)(63 - __builtin_clzll(o.a)) * 64 + (uint64_t)(63 - __builtin_clzll(o.c));
+      kb = (uint64_t)(63 - __builtin_clzll(o.b)) * 64 + (uint64_t)(63 - __builtin_clzll(o.d));
+      auto pa = ai.find(ka);
+      if (pa == ai.end()) { pa = ai.emplace(ka, (int)Aops[k].size()).first; Aops[k].push_back({o.a, o.c}); }
+      auto pb = bi.find(kb);
+      if (pb == bi.end()) { pb = bi.emplace(kb, (int)Bops[k].size()).first; Bops[k].push_back({o.b, o.d}); }
+      cells.push_back({pa->second, pb->second});
+    }
+    T.nA_dm[k] = (int)Aops[k].size();
+    T.nB_dm[k] = (int)Bops[k].size();
+    T.vtab_off_dm[k + 1] = T.vtab_off_dm[k] + (int64_t)T.nA_dm[k] * T.nB_dm[k];
+    if (T.nA_dm[k] >= (1 << 15) || T.nB_dm[k] >= (1 << 13))
+      throw SetupError{SMGPU_ERR_LIMIT, "too many distinct one-body operators for one ΔM"};
+    T.vtab.resize(T.vtab_off_dm[k + 1], 0.0);
+    for (size_t e = 0; e < T.vpn[k].size(); ++e) {
+      if (cells[e].first < 0) continue;
+      T.vtab[T.vtab_off_dm[k] + (int64_t)cells[e].first * T.nB_dm[k] + cells[e].second] = T.vpn[k][e].v;
+    }
+  }
+
+  // ---- links (prep_pn's bfs/bis, :1139-1151).  The reference indexes its
+  // list of all proton M values by block number; that is reproduced here.
+  std::vector<std::vector<Tables::Link>> per_b(nb);
+  for (int bi = 0; bi < nb; ++bi)
+    for (int bf = bi; bf < nb; ++bf) {
+      if (bf >= (int)Mps.size()) break;
+      int dm = Mps[bf] - Mps[bi];
+      auto it = std::find(T.delMs.begin(), T.delMs.end(), dm);
+      if (it == T.delMs.end()) continue;
+      int k = (int)(it - T.delMs.begin());
+      if (T.nA_dm[k] == 0) continue;
+      per_b[bi].push_back(Tables::Link{bi, bf, k, T.nA_dm[k], T.nB_dm[k], T.vtab_off_dm[k], 0});
+      if (bf != bi) per_b[bf].push_back(Tables::Link{bf, bi, k, T.nA_dm[k], T.nB_dm[k], T.vtab_off_dm[k], 0});
+    }
+  T.link_begin.assign(nb + 1, 0);
+  for (int b = 0; b < nb; ++b) {
+    std::sort(per_b[b].begin(), per_b[b].end(), [](const Tables::Link& x, const Tables::Link& y) { return x.s < y.s; });
+    for (auto& L : per_b[b]) T.links.push_back(L);
+    T.link_begin[b + 1] = (int)T.links.size();
+  }
+  if (T.links.size() >= (1u << 16)) throw SetupError{SMGPU_ERR_LIMIT, "too many block links"};
+
+  // ---- neutron pull CSR per link
+  int64_t nptr_total = 0;
+  for (auto& L : T.links) { L.nptr_off = nptr_total; nptr_total += T.nn[L.b] + 1; }
+  T.npn_ptr.assign(nptr_total, 0);
+  {
+    std::vector<std::vector<uint32_t>> per_link(T.links.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long li = 0; li < (long)T.links.size(); ++li) {
+      const auto& L = T.links[li];
+      bool fwd = L.s >= L.b;
+      const uint64_t* src = T.nbits.data() + T.nstart[L.s];
+      int nsrc = T.nn[L.s];
+      auto& out = per_link[li];
+      int64_t* ptr = T.npn_ptr.data() + L.nptr_off;
+      ptr[0] = 0;
+      for (int n = 0; n < T.nn[L.b]; ++n) {
+        uint64_t sd = T.nbits[T.nstart[L.b] + n];
+        for (int ib = 0; ib < L.nB; ++ib) {
+          uint64_t opb = Bops[L.dm][ib].first, opd = Bops[L.dm][ib].second;
+          uint64_t f;
+          int odd;
+          if (fwd) {
+            if (!apply1(sd, opb, opd, f, odd)) continue;
+          } else {
+            uint64_t back;
+            int dummy;
+            if (!apply1(sd, opd, opb, f, dummy)) continue;  // d†b maps output n to source n'
+            if (!apply1(f, opb, opd, back, odd) || back != sd) continue;
+          }
+          int j = find_desc(src, nsrc, f);
+          if (j < 0) continue;
+          if (j >= (1 << 18)) throw SetupError{SMGPU_ERR_LIMIT, "neutron block too large"};
+          out.push_back(((uint32_t)j << 14) | ((uint32_t)ib << 1) | (uint32_t)odd);
+        }
+        ptr[n + 1] = (int64_t)out.size();
+      }
+    }
+    int64_t base = 0;
+    for (size_t li = 0; li < T.links.size(); ++li) {
+      int64_t* ptr = T.npn_ptr.data() + T.links[li].nptr_off;
+      for (int n = 0; n <= T.nn[T.links[li].b]; ++n) ptr[n] += base;
+      T.npn_ent.insert(T.npn_ent.end(), per_link[li].begin(), per_link[li].end());
+      base += (int64_t)per_link[li].size();
+    }
+  }
+
+  // ---- proton pull entries per output proton row
+  {
+    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> rows(NP);
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t g = 0; g < NP; ++g) {
+      int b = (int)(std::upper_bound(T.pstart.begin(), T.pstart.end(), (int)g) - T.pstart.begin()) - 1;
+      uint64_t sd = T.pbits[g];
+      for (int li = T.link_begin[b]; li < T.link_begin[b + 1]; ++li) {
+        const auto& L = T.links[li];
+        bool fwd = L.s >= L.b;
+        const uint64_t* src = T.pbits.data() + T.pstart[L.s];
+        int nsrc = T.np[L.s];
+        for (int ia = 0; ia < L.nA; ++ia) {
+          uint64_t opa = Aops[L.dm][ia].first, opc = Aops[L.dm][ia].second;
+          uint64_t f;
+          int odd;
+          if (fwd) {
+            if (!apply1(sd, opa, opc, f, odd)) continue;
+          } else {
+            uint64_t back;
+            int dummy;
+            if (!apply1(sd, opc, opa, f, dummy)) continue;
+            if (!apply1(f, opa, opc, back, odd) || back != sd) continue;
+          }
+          int j = find_desc(src, nsrc, f);
+          if (j < 0) continue;
+          rows[g].push_back({(uint32_t)j, ((uint32_t)li << 16) | ((uint32_t)ia << 1) | (uint32_t)odd});
+        }
+      }
+    }
+    T.ppn_ptr.assign(NP + 1, 0);
+    for (int64_t g = 0; g < NP; ++g) T.ppn_ptr[g + 1] = T.ppn_ptr[g] + (int)rows[g].size();
+    T.ppn_src.resize(T.ppn_ptr[NP]);
+    T.ppn_meta.resize(T.ppn_ptr[NP]);
+    for (int64_t g = 0; g < NP; ++g)
+      for (size_t k = 0; k < rows[g].size(); ++k) {
+        T.ppn_src[T.ppn_ptr[g] + k] = rows[g][k].first;
+        T.ppn_meta[T.ppn_ptr[g] + k] = rows[g][k].second;
+      }
+  }
+
+  T.Aops_dm.assign(ndm, {});
+  T.Bops_dm.assign(ndm, {});
+  for (size_t k = 0; k < ndm; ++k) {
+    for (auto& pr : Aops[k]) { T.Aops_dm[k].push_back(pr.first); T.Aops_dm[k].push_back(pr.second); }
+    for (auto& pr : Bops[k]) { T.Bops_dm[k].push_back(pr.first); T.Bops_dm[k].push_back(pr.second); }
+  }
+
+  // ---- multiply-adds per H·v
+  int64_t upd = 0;
+  for (int b = 0; b < nb; ++b) {
+    upd += (int64_t)T.np[b] * T.nn[b];  // diagonal
+    upd += (int64_t)(T.pp_ptr[T.pstart[b + 1]] - T.pp_ptr[T.pstart[b]]) * T.nn[b];
+    upd += (int64_t)(T.nn_ptr[T.nstart[b + 1]] - T.nn_ptr[T.nstart[b]]) * T.np[b];
+  }
+  std::vector<int64_t> link_pcount(T.links.size(), 0);
+  for (int64_t k = 0; k < (int64_t)T.ppn_meta.size(); ++k) link_pcount[T.ppn_meta[k] >> 16]++;
+  for (size_t li = 0; li < T.links.size(); ++li) {
+    const auto& L = T.links[li];
+    int64_t nent = T.npn_ptr[L.nptr_off + T.nn[L.b]] - T.npn_ptr[L.nptr_off];
+    // each proton entry of the link pairs with every neutron entry of the link
+    // (averaged: exact count is sum over rows; rows of one link share the CSR)
+    upd += link_pcount[li] * nent;
+  }
+  T.updates = upd;
+}
+
+}  // namespace smgpu

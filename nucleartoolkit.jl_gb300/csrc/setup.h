@@ -1,0 +1,100 @@
+// Host-side problem set-up for libsmgpu: interaction parsing, m-scheme
+// matrix elements and the factorised ("pull") tables the GPU kernels read.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace smgpu {
+
+struct Orbit {
+  int n, l, j2, tz;
+};
+
+// The data of the reference's SMobject (shellmodel_main.jl:38-53) that the
+// eigensolver needs.  `tb[k]` holds pp (k=0), nn (1) and pn (2) entries with
+// the hermitian partners already added in readsmsnt's order.
+struct Interaction {
+  int lp = 0, ln = 0, cp = 0, cn = 0;
+  std::vector<Orbit> porb, norb;
+  std::vector<double> spe_p, spe_n;
+  struct TB {
+    int a, b, c, d, J;
+    double v;
+  };
+  std::vector<TB> tb[3];
+};
+
+struct SetupError {
+  int code;
+  std::string msg;
+};
+
+// snt text -> Interaction (readsmsnt semantics, shellmodel_main.jl:293-365)
+Interaction read_snt(const std::string& path, int Anum);
+// "Cr48" / "48Cr" -> A and Z (util_func.jl:1,13-24; shellmodel_main.jl:908-916)
+void parse_nucleus(const std::string& nuc, int& A, int& Z);
+
+// Clebsch–Gordan coefficient with doubled arguments (exact, binomial form).
+double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
+
+// One m-state of a species, in construct_msps order (shellmodel_main.jl:373-384).
+struct MState {
+  int orbit;  // 0-based orbit index within the species
+  int j2, m2;
+};
+
+// m-scheme two-body operator a†b† d c, keyed by one-hot SD bit masks.
+struct Op2 {
+  uint64_t a, b, c, d;
+  double v;
+};
+
+// Everything the GPU needs, in flat arrays.
+struct Tables {
+  // species
+  int Lp = 0, Ln = 0;  // number of m-states
+  std::vector<MState> msp, msn;
+  // blocks (ordered by ascending proton M)
+  int nb = 0;
+  std::vector<int> np, nn, stride, mp2, mn2;
+  std::vector<int64_t> tdims;    // nb+1, unpadded offsets (reference order)
+  std::vector<int64_t> off_pad;  // nb+1, padded offsets (rows padded to `stride`)
+  int64_t mdim = 0, len_pad = 0;
+  std::vector<uint64_t> pbits, nbits;  // per block, descending
+  std::vector<int> pstart, nstart;     // nb+1
+  std::vector<double> ep, en;          // one-body diagonal per SD
+  // m-scheme operators (reference prep_Hamil_T1 / prep_Hamil_pn lists)
+  std::vector<Op2> vpp, vnn;
+  std::vector<int> delMs;                   // descending, as the reference's Mzs
+  std::vector<std::vector<Op2>> vpn;        // per delMs entry (fields a,b,c,d = bit_a,bit_b,bit_c,bit_d)
+  // pp / nn pull CSR (rows = SDs of a block, cols local, merged duplicates)
+  std::vector<int> pp_ptr, pp_col, nn_ptr, nn_col;
+  std::vector<double> pp_val, nn_val;
+  // pn: links (output block b <- source block s)
+  struct Link {
+    int b, s, dm;   // dm = index of the V table
+    int nA, nB;
+    int64_t vtab_off;   // into vtab
+    int64_t nptr_off;   // into npn_ptr: nn[b]+1 row pointers
+  };
+  std::vector<Link> links;
+  std::vector<int> link_begin;  // nb+1
+  // proton pull entries per global proton row: src row (local in s), meta = link<<16 | ia<<1 | sign
+  std::vector<int> ppn_ptr;
+  std::vector<uint32_t> ppn_src, ppn_meta;
+  // neutron pull CSR per link: entries n'<<14 | ib<<1 | sign
+  std::vector<int64_t> npn_ptr;
+  std::vector<uint32_t> npn_ent;
+  std::vector<double> vtab;  // V tables [nA x nB] per delMs index (only ΔM >= 0 used)
+  std::vector<int64_t> vtab_off_dm;
+  std::vector<int> nA_dm, nB_dm;
+  std::vector<std::vector<uint64_t>> Aops_dm, Bops_dm;  // per dm: (bit_a<<32|bit_c) style pairs, see setup.cpp
+  // statistics
+  int64_t updates = 0;
+};
+
+// Full host set-up of one problem.  vp, vn valence numbers, mtot2 doubled M.
+void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T);
+
+}  // namespace smgpu

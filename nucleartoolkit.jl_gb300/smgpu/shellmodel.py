@@ -1,0 +1,145 @@
+"""Host-side mirror of NuclearToolkit.jl's ShellModel entry point over libsmgpu.
+
+``main_sm`` keeps the reference's signature and return value
+(src/ShellModel/shellmodel_main.jl:89-281): it reads the snt file, sets the
+problem up for the target nucleus and returns the lowest ``num_ev``
+eigenvalues (MeV) — all compute on the GPU through the C ABI.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import FP64, MIXED, check, load
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class ShellModelProblem:
+    """One M-scheme problem resident on the GPU (an ``smgpu_problem`` handle)."""
+
+    def __init__(self, sntf: str, target_nuc: str, precision: int = FP64):
+        L = load()
+        h = C.c_void_p()
+        rc = L.smgpu_problem_create_from_snt(os.fsencode(sntf), target_nuc.encode(), int(precision), C.byref(h))
+        check(rc, None)
+        self._h = h
+        self.precision = precision
+        md = C.c_longlong()
+        nb = C.c_int()
+        check(L.smgpu_dims(h, C.byref(md), C.byref(nb), None), h)
+        self.mdim = int(md.value)
+        self.nblocks = int(nb.value)
+        self.tdims = np.zeros(self.nblocks + 1, dtype=np.int64)
+        check(L.smgpu_dims(h, None, None, _p(self.tdims)), h)
+        self.np_ = np.zeros(self.nblocks, dtype=np.int32)
+        self.nn_ = np.zeros(self.nblocks, dtype=np.int32)
+        self.Mp = np.zeros(self.nblocks, dtype=np.int32)
+        self.Mn = np.zeros(self.nblocks, dtype=np.int32)
+        check(L.smgpu_blocks(h, _p(self.np_), _p(self.nn_), _p(self.Mp), _p(self.Mn)), h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().smgpu_problem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- exports for parity checks
+    def basis(self):
+        p = np.zeros(int(self.np_.sum()), dtype=np.uint64)
+        n = np.zeros(int(self.nn_.sum()), dtype=np.uint64)
+        check(load().smgpu_export_basis(self._h, _p(p), _p(n)), self._h)
+        return p, n
+
+    def jumps(self, which: int):
+        L = load()
+        cnt = C.c_longlong()
+        check(L.smgpu_export_jumps(self._h, which, C.byref(cnt), None, None), self._h)
+        width = 7 if which in (0, 1) else 3
+        ints = np.zeros((cnt.value, width), dtype=np.int64)
+        coef = np.zeros(cnt.value)
+        check(L.smgpu_export_jumps(self._h, which, C.byref(cnt), _p(ints), _p(coef)), self._h)
+        return (ints, coef) if which in (2, 3) else ints
+
+    def stats(self):
+        s = np.zeros(8, dtype=np.int64)
+        check(load().smgpu_stats(self._h, _p(s)), self._h)
+        keys = ["updates", "pn_proton_entries", "pn_neutron_entries", "pp_entries", "nn_entries", "table_bytes",
+                "len_pad", "links"]
+        return dict(zip(keys, map(int, s)))
+
+    def timings(self):
+        t = np.zeros(8)
+        check(load().smgpu_timings(self._h, _p(t)), self._h)
+        keys = ["setup", "lanczos", "matvec", "reorth", "restart", "ritz", "h2d", "d2h"]
+        return dict(zip(keys, map(float, t)))
+
+    # --- compute
+    def matvec(self, v, accumulate: bool = False, out=None):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        ncols = 1 if v.ndim == 1 else v.shape[0]
+        w = np.zeros_like(v) if out is None else out
+        check(load().smgpu_matvec(self._h, _p(v), _p(w), ncols, 1 if accumulate else 0), self._h)
+        return w
+
+    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False):
+        nev = min(num_ev, self.mdim)
+        ev = np.zeros(nev)
+        vecs = np.zeros((nev, self.mdim)) if want_vecs else None
+        stats = np.zeros(6, dtype=np.int32)
+        v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
+        rc = load().smgpu_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts), _p(v1a),
+                                _p(ev), _p(vecs), _p(stats))
+        if rc not in (_lib.OK, _lib.ERR_NOCONV):
+            check(rc, self._h)
+        return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_matvec=int(stats[1]), n_restart=int(stats[2]),
+                    converged=bool(stats[3]) and rc == _lib.OK, n_second_pass=int(stats[5]), status=rc)
+
+
+def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=False, is_show=False,
+            num_history=3, lm=300, ls=20, tol=1.0e-8, in_wf="", mdimmode=False, print_evec=False,
+            calc_moment=False, calc_entropy=False, visualize_occ=False, gfactors=(1.0, 0.0, 5.586, -3.826),
+            effcharge=(1.5, 0.5), truncation_scheme="", truncated_jocc=None, debugmode="", precision=FP64,
+            max_restarts=10000, verbose=True):
+    """Lowest ``num_ev`` eigenvalues of the valence-space Hamiltonian.
+
+    Same positional arguments and keyword names as the reference's ``main_sm``
+    (src/ShellModel/shellmodel_main.jl:89-92).  ``precision`` selects the
+    plain FP64 form or the FP32-mixed form.  Features of the reference outside
+    the eigensolver path raise ``NotImplementedError``.
+    """
+    if target_J is not None and len(target_J) > 0:
+        raise NotImplementedError("J-projected Lanczos (target_J non-empty) is not in this library")
+    unsupported = dict(save_wav=save_wav, is_block=is_block, in_wf=bool(in_wf), calc_moment=calc_moment,
+                       calc_entropy=calc_entropy, visualize_occ=visualize_occ, print_evec=print_evec,
+                       truncation=bool(truncation_scheme), debugmode=bool(debugmode))
+    bad = [k for k, v in unsupported.items() if v]
+    if bad:
+        raise NotImplementedError("not supported by the GPU eigensolver: " + ", ".join(bad))
+    if num_history != 3:
+        raise NotImplementedError("num_history other than 3")
+    P = ShellModelProblem(sntf, target_nuc, precision)
+    if verbose:
+        print(f"{target_nuc:>6s}  mdim: {P.mdim:12d} ({np.log10(max(P.mdim, 1)):5.2f}) ")
+    if mdimmode:
+        P.close()
+        return None
+    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts)
+    en = list(map(float, r["evals"]))
+    if verbose:
+        print("En. " + " ".join(f"{x:10.4f}" for x in en))
+        print("Ex. " + " ".join(f"{x - en[0]:10.4f}" for x in en))
+        if is_show:
+            print(P.timings())
+    P.close()
+    if r["status"] == _lib.ERR_NOCONV:
+        raise RuntimeError(f"Lanczos did not converge within {max_restarts} restarts")
+    return en
