@@ -1,0 +1,341 @@
+"""Benchmark: 48Cr pf-shell M=0 (dim 1,963,461), time to the 5 lowest eigenvalues.
+
+One step = one thick-restart Lanczos eigensolve (lm=30, ls=15, tol=1e-8) of
+the seeded synthetic pf interaction, FP32-mixed form, problem resident on the
+GPU.  The line also carries the plain FP64 GPU form, the per-eigenvalue error
+of both forms against the FP64 oracle, the H·v roofline and the CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's path (the
+oracle: operate_H! + TRL with OpenMP over blocks) on all host cores instead;
+each step is a bounded sample (two Lanczos iterations) projected to the
+oracle's full iteration count.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "nucleartoolkit.jl_gb300"))
+
+METRIC = "pf M=0 time-to-5-eigvals & H·v HBM GB/s: FP32-mixed vs FP64 GPU, ΔE≤1e-4 MeV"
+WORKLOAD = "pf4p4n"
+NEV, LM, LS, TOL = 5, 30, 15, 1e-8
+HBM_FALLBACK = 6800.0
+
+
+def load_json(path):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def golden_run():
+    g = load_json(os.path.join(ROOT, "tests", "golden", "oracle_runs.json")) or {}
+    return g.get(WORKLOAD)
+
+
+def config_dict(extra=None):
+    c = {"workload": "48Cr pf-shell 4p4n M=0, dim 1963461, 21 (Mp,Mn) blocks, 5 lowest eigenvalues, "
+                     "thick-restart Lanczos lm=30 ls=15 tol=1e-8",
+         "interaction": "synthetic seeded snt: TBMEs N(0,1.0^2) MeV seed 4848, SPE -8.6/-6.0/-2.0/-4.0",
+         "mdim": 1963461, "num_ev": NEV, "lm": LM, "ls": LS, "tol": TOL,
+         "l2": "flushed (256 MB write) between timed steps; Krylov basis 236 MB > L2"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = tempfile.mktemp(suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 10:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        load = [r for r in rows if (num(r[4]) or 0) >= 20] or rows
+        sm = [num(r[1]) for r in load if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[6 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(rows[0][2]),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(load)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ CPU arm
+def oracle_sample(snt, nuc, iters=2, setup_only=False):
+    """Time the oracle on the full problem: set-up and `iters` Lanczos
+    iterations (operate_H! + α + full MGS re-orthogonalisation + β)."""
+    from oracle.oracle import OracleProblem, get_threads
+    t0 = time.perf_counter()
+    O = OracleProblem(snt, nuc)
+    t_setup = time.perf_counter() - t0
+    if setup_only:
+        return O, t_setup, None
+    r = O.trl(NEV, lm=iters + 1, ls=1, tol=TOL, max_restart=0)
+    return O, t_setup, dict(t_iter=r["t_total"] / max(r["n_hv"], 1), n=r["n_hv"], t_hv=r["t_hv"] / max(r["n_hv"], 1),
+                            threads=get_threads())
+
+
+def project(t_setup, t_iter, g):
+    n = g["n_hv"] if g else None
+    return (t_setup + n * t_iter) if n else None
+
+
+def run_reference(args, dist, rank):
+    if rank != 0:
+        return
+    from smgpu import synth
+    d = tempfile.mkdtemp()
+    snt, nuc = synth.config_snt(d, WORKLOAD)
+    g = golden_run()
+    if not g:
+        print(json.dumps({"impl": "reference", "unavailable": "oracle iteration count for the projection is missing "
+                                                              "(tests/golden/oracle_runs.json)"}))
+        return
+    O, t_setup, _ = oracle_sample(snt, nuc, setup_only=True)
+    for _ in range(args.warmup):
+        O.trl(NEV, lm=3, ls=1, tol=TOL, max_restart=0)
+    vals = []
+    threads = None
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = O.trl(NEV, lm=3, ls=1, tol=TOL, max_restart=0)
+        t_iter = r["t_total"] / max(r["n_hv"], 1)
+        vals.append(project(t_setup, t_iter, g))
+        from oracle.oracle import get_threads
+        threads = get_threads()
+    wall = time.perf_counter() - t_wall0
+    v = statistics.mean(vals)
+    sample = (f"oracle set-up on the full 48Cr problem ({t_setup:.2f} s, once) + per step 2 Lanczos iterations "
+              f"(operate_H! + MGS re-orthogonalisation), projected to the oracle's full TRL iteration count "
+              f"n_hv={g['n_hv']}")
+    line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict({"impl": "CPU restatement (oracle) of operate_H!/TRL, OpenMP over blocks"}),
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+def run_gpu(args, dist, rank, local):
+    import numpy as np
+    import torch
+    import smgpu
+    from smgpu import synth
+
+    torch.cuda.set_device(0)
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def flush():
+        flush_buf.fill_(1)
+        torch.cuda.synchronize()
+
+    d = tempfile.mkdtemp()
+    snt, nuc = synth.config_snt(d, WORKLOAD)
+    g = golden_run()
+
+    # ---- device-resident solves (value)
+    M = smgpu.ShellModelProblem(snt, nuc, smgpu.MIXED)
+    st = M.stats()
+    for _ in range(args.warmup):
+        M.solve(NEV, lm=LM, ls=LS, tol=TOL)
+    times, launches, res = [], 0, None
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush()
+            res = M.solve(NEV, lm=LM, ls=LS, tol=TOL)
+            times.append(M.timings()["lanczos"])
+            launches += res["kernel_launches"]
+    barrier(dist)
+    t_mixed = max_over_ranks(dist, statistics.mean(times))
+    clocks = clk.summary()
+    ev_mixed = res["evals"]
+
+    # ---- H·v kernel timing (CUDA events on the library stream)
+    hv_ms_mixed = M.time_matvec(reps=20, flush_l2=True)
+    M.close()
+
+    # ---- plain FP64 form
+    F = smgpu.ShellModelProblem(snt, nuc, smgpu.FP64)
+    F.solve(NEV, lm=LM, ls=LS, tol=TOL)
+    t64 = []
+    for _ in range(max(1, min(args.steps, 2))):
+        flush()
+        rf = F.solve(NEV, lm=LM, ls=LS, tol=TOL)
+        t64.append(F.timings()["lanczos"])
+    t_fp64 = statistics.mean(t64)
+    ev_fp64 = rf["evals"]
+    hv_ms_fp64 = F.time_matvec(reps=10, flush_l2=True)
+    F.close()
+
+    # ---- end to end through the C ABI: snt file -> set-up -> solve -> eigenvalues
+    e2e_times = []
+    h2d = d2h = 0
+    for _ in range(max(1, min(args.steps, 3))):
+        flush()
+        t0 = time.perf_counter()
+        E = smgpu.ShellModelProblem(snt, nuc, smgpu.MIXED)
+        re = E.solve(NEV, lm=LM, ls=LS, tol=TOL)
+        e2e_times.append(time.perf_counter() - t0)
+        h2d = E.stats()["table_bytes"]
+        d2h = 8 * NEV + 32 * (re["n_restart"] + 1)
+        E.close()
+    t_e2e = max_over_ranks(dist, statistics.mean(e2e_times))
+
+    # ---- roofline of the H·v kernel (FP32-mixed): CSR-equivalent algorithmic bytes
+    mdim = 1963461
+    nnz = g["nnz"] if g else None
+    peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
+    peak = (peaks or {}).get("hbm_gbs") or HBM_FALLBACK
+    peak_src = "measured" if peaks and peaks.get("hbm_gbs") else "fallback"
+    prof = load_json(os.path.join(ROOT, "profiles", "hv_pull_pf4p4n_traffic.json")) or {}
+    roof = None
+    if nnz:
+        b_alg = nnz * (4 + 4) + 4 * (mdim + 1) + 2 * 1 * mdim * 4
+        achieved = b_alg / (hv_ms_mixed * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": prof.get("mixed_bytes_per_launch"), "kernel": "hv_pull_kernel<float> (FP32-mixed H·v)",
+                "peak_source": peak_src, "algorithmic_bytes": b_alg,
+                "hv_ms": hv_ms_mixed, "hv_fp64_ms": hv_ms_fp64,
+                "hv_fp64_achieved": (nnz * (8 + 4) + 4 * (mdim + 1) + 2 * mdim * 8) / (hv_ms_fp64 * 1e-3) / 1e9}
+
+    # ---- CPU baseline (rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and args.gpus == 1 and not args.no_cpu:
+        O, t_setup, s = oracle_sample(snt, nuc, iters=2)
+        v = project(t_setup, s["t_iter"], g)
+        cpu = {"value": v, "unit": "s", "cores": s["threads"], "kind": "port",
+               "sample": f"oracle set-up ({t_setup:.2f} s) + 2 Lanczos iterations on the full 48Cr problem "
+                         f"({s['t_iter']:.3f} s/iteration, H·v {s['t_hv']:.3f} s), projected to the oracle's "
+                         f"n_hv={g['n_hv'] if g else None}"}
+        del O
+
+    dE = None
+    if g:
+        ref = np.array(g["evals"])
+        dE = {"mixed_vs_oracle_MeV": [float(x) for x in (ev_mixed - ref)],
+              "fp64_vs_oracle_MeV": [float(x) for x in (ev_fp64 - ref)],
+              "max_abs_mixed_MeV": float(np.abs(ev_mixed - ref).max()),
+              "max_rel_fp64": float(np.abs((ev_fp64 - ref) / ref).max())}
+    if rank == 0:
+        line = {"metric": METRIC, "value": t_mixed, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_mixed * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "fp32-mixed (f32 H·v, f64 Lanczos)", "data": "synthetic",
+                "config": config_dict({"parallelism": f"replicas x{args.gpus}"}),
+                "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                        "path": "smgpu_problem_create_from_snt + smgpu_solve (snt file to eigenvalues)"},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches),
+                "fp64_plain": {"value": t_fp64, "unit": "s", "evals": [float(x) for x in ev_fp64]},
+                "speedup_mixed_vs_fp64": t_fp64 / t_mixed,
+                "evals_mixed": [float(x) for x in ev_mixed], "dE": dE,
+                "lanczos": {"n_matvec": res["n_matvec"], "n_restart": res["n_restart"],
+                            "second_pass": res["n_second_pass"]},
+                "matvecs_per_s": res["n_matvec"] / t_mixed, "hv_updates": st["updates"]}
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = init_dist(world)
+    if args.impl == "reference":
+        run_reference(args, dist, rank)
+    else:
+        run_gpu(args, dist, rank, local)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -117,15 +117,26 @@ int smgpu_matvec(smgpu_problem* h, const double* v, double* w, int ncols, int ac
  *   v1: optional start vector (mdim doubles, host), NULL = seeded hash draw;
  *   evals_out: num_ev doubles (min(num_ev, mdim) are written);
  *   evecs_out: NULL or num_ev x mdim doubles (Ritz vectors, basis order);
- *   stats_out: NULL or 6 ints: [elit, n_matvec, n_restart, converged, num_ev_written, reserved]. */
+ *   stats_out: NULL or 8 ints: [elit, n_matvec, n_restart, converged, num_ev_written,
+ *              second re-orthogonalisation passes, kernel launches, reserved]. */
 int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int max_restarts,
                 const double* v1, double* evals_out, double* evecs_out, int* stats_out);
 
-/* Seconds spent in the phases of the last smgpu_solve / create call
- * (the reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos",
- * "operate H", "ReORTH", "Restart", "Rvecs").  times_out: 8 doubles:
- * [setup, lanczos, matvec, reorth, restart, ritz, h2d, d2h]. */
+/* Seconds spent in the phases of the last create / solve / matvec call (the
+ * reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos", "Rvecs",
+ * shellmodel_main.jl:137,159,208).  times_out: 8 doubles:
+ * [setup (host wall), lanczos (CUDA events on the handle's stream, start
+ *  vector to converged eigenvalues), last matvec call (host wall), graph
+ *  capture + instantiation (host wall), ritz vectors (events), solve call
+ *  (host wall), reserved, reserved]. */
 int smgpu_timings(const smgpu_problem* h, double* times_out);
+
+/* Time `reps` back-to-back H·v launches on the handle's stream with CUDA
+ * events (the reference's "operate H" section, lanczos_methods.jl:36), on a
+ * device-resident seeded vector in the handle's precision.  flush_l2 != 0
+ * writes a 256 MB buffer between launches and excludes that from the time.
+ * ms_out: mean milliseconds per launch. */
+int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
 /* Structural statistics of the factorised H: [updates per H·v (multiply-adds),
  * pn proton pull entries, pn neutron entries, pp entries, nn entries,

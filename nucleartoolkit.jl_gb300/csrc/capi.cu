@@ -293,7 +293,7 @@ struct Solve {
     launch_restart_apply<TX>(L, U, V, s);
   }
 
-  cudaGraphExec_t capture_cycle(int kstart, int lock) {
+  cudaGraphExec_t capture_cycle(int kstart, int lock, long long* nkernels) {
     cudaStream_t s = P->st, s2 = P->st2;
     cudaEvent_t e_fork, e_join;
     SMGPU_CUDA_TRY(cudaEventCreateWithFlags(&e_fork, cudaEventDisableTiming));
@@ -305,6 +305,17 @@ struct Solve {
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s, e_join, 0));
     restart(s);
     SMGPU_CUDA_TRY(cudaStreamEndCapture(s, &g));
+    size_t nn = 0;
+    SMGPU_CUDA_TRY(cudaGraphGetNodes(g, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    SMGPU_CUDA_TRY(cudaGraphGetNodes(g, nodes.data(), &nn));
+    long long nk = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType ty;
+      SMGPU_CUDA_TRY(cudaGraphNodeGetType(nd, &ty));
+      if (ty == cudaGraphNodeTypeKernel) ++nk;
+    }
+    *nkernels = nk;
     cudaGraphExec_t ex;
     SMGPU_CUDA_TRY(cudaGraphInstantiate(&ex, g, 0));
     cudaGraphDestroy(g);
@@ -317,21 +328,30 @@ struct Solve {
           double* evecs_out, int* stats_out) {
     const int64_t mdim = P->T.mdim;
     const int nev = (int)std::min<int64_t>(num_ev, mdim);
-    double t0 = now_s();
+    double tw0 = now_s();
     alloc(lm, ls, num_ev, tol);
+    double* v1dev = nullptr;
     if (v1) {
-      double* tmp = P->solver.alloc<double>(mdim);
-      SMGPU_CUDA_TRY(cudaMemcpyAsync(tmp, v1, sizeof(double) * mdim, cudaMemcpyHostToDevice, P->st));
-      launch_to_padded<double>(P->dt, tmp, w, P->st);
-    } else {
-      launch_start_vector(P->dt, 1234ull, w, P->st);
+      v1dev = P->solver.alloc<double>(mdim);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(v1dev, v1, sizeof(double) * mdim, cudaMemcpyHostToDevice, P->st));
     }
+    double tc0 = now_s();
+    cudaGraphExec_t g_first = capture_cycle(1, 0, &launches_first);
+    cudaGraphExec_t g_rest = capture_cycle(ls + 1, ls, &launches_rest);
+    P->times[3] = now_s() - tc0;
+    cudaEvent_t e0, e1, e2;
+    SMGPU_CUDA_TRY(cudaEventCreate(&e0));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e1));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e2));
+    SMGPU_CUDA_TRY(cudaEventRecord(e0, P->st));
+    if (v1dev) launch_to_padded<double>(P->dt, v1dev, w, P->st);
+    else launch_start_vector(P->dt, 1234ull, w, P->st);
     init_start();
-    cudaGraphExec_t g_first = capture_cycle(1, 0);
-    cudaGraphExec_t g_rest = nullptr;
+    long long launches = 4;
     int n_restart = 0, status = SMGPU_OK;
     LanczosFlags fl{};
     SMGPU_CUDA_TRY(cudaGraphLaunch(g_first, P->st));
+    launches += launches_first;
     while (true) {
       SMGPU_CUDA_TRY(cudaMemcpyAsync(&fl, L.fl, sizeof(LanczosFlags), cudaMemcpyDeviceToHost, P->st));
       SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
@@ -347,38 +367,45 @@ struct Solve {
         fl.elit = lm - 1;
         break;
       }
-      if (!g_rest) g_rest = capture_cycle(ls + 1, ls);
       SMGPU_CUDA_TRY(cudaGraphLaunch(g_rest, P->st));
+      launches += launches_rest;
     }
-    if (fl.bad) {
-      cudaGraphExecDestroy(g_first);
-      if (g_rest) cudaGraphExecDestroy(g_rest);
-      return fail(P, SMGPU_ERR_DEVICE, "restart Gram matrix was not positive definite");
-    }
-    double t1 = now_s();
     // eigenvalues: en[1] of the last eigenvalue test (main_sm returns en[1])
-    SMGPU_CUDA_TRY(cudaMemcpy(evals_out, L.en, sizeof(double) * nev, cudaMemcpyDeviceToHost));
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(evals_out, L.en, sizeof(double) * nev, cudaMemcpyDeviceToHost, P->st));
+    SMGPU_CUDA_TRY(cudaEventRecord(e1, P->st));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+    cudaGraphExecDestroy(g_first);
+    cudaGraphExecDestroy(g_rest);
+    if (fl.bad) return fail(P, SMGPU_ERR_DEVICE, "restart Gram matrix was not positive definite");
     int elit = fl.elit;
     if (status == SMGPU_ERR_NOCONV) elit = 0;
     if (evecs_out && elit > 0) {
       // Ritz vectors (shellmodel_main.jl:208-224)
-      launch_jacobi(L, elit, false, P->st);
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
+      launch_jacobi(L, elit, false, P->st);
       launch_ritz<TX>(L, V, elit, nev, R, P->st);
+      launches += 2;
       for (int e = 0; e < nev; ++e) {
         double* r = R + (size_t)e * L.len;
         launch_multidot<double>(L, r, 1, r, false, nullptr, P->st);
         launch_reduce(L, 1, RED_INVNORM, L.h + e, 0, nullptr, P->st);
         launch_scale_store<double>(L, r, r, L.h + e, nullptr, P->st);
         launch_from_padded(P->dt, r, tmp, P->st);
+        launches += 4;
         SMGPU_CUDA_TRY(cudaMemcpyAsync(evecs_out + (size_t)e * mdim, tmp, sizeof(double) * mdim,
                                        cudaMemcpyDeviceToHost, P->st));
       }
-      SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
     }
-    double t2 = now_s();
+    SMGPU_CUDA_TRY(cudaEventRecord(e2, P->st));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
     SMGPU_CUDA_TRY(cudaGetLastError());
+    float ms1 = 0.f, ms2 = 0.f;
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms1, e0, e1));
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms2, e1, e2));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
     if (stats_out) {
       int n_hv = 0;
       // iterations executed: first cycle 1..lm-1, later cycles ls+1..lm-1
@@ -393,13 +420,15 @@ struct Solve {
       stats_out[3] = fl.done ? 1 : 0;
       stats_out[4] = nev;
       stats_out[5] = fl.n_second;
+      stats_out[6] = (int)launches;
+      stats_out[7] = 0;
     }
-    P->times[1] = t1 - t0;
-    P->times[5] = t2 - t1;
-    cudaGraphExecDestroy(g_first);
-    if (g_rest) cudaGraphExecDestroy(g_rest);
+    P->times[1] = ms1 * 1e-3;
+    P->times[4] = ms2 * 1e-3;
+    P->times[5] = now_s() - tw0;
     return status;
   }
+  long long launches_first = 0, launches_rest = 0;
 };
 
 }  // namespace
@@ -610,6 +639,51 @@ int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int ma
     }
     Solve<float> s{h};
     return s.run(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
+  });
+}
+
+int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out) {
+  if (!h || !ms_out || reps < 1) return fail(h, SMGPU_ERR_ARG, "bad time_matvec arguments");
+  return guarded(h, [&]() {
+    DeviceArena tmp;
+    cudaEvent_t a = nullptr, b = nullptr;
+    try {
+      const int64_t len = h->T.len_pad;
+      double* d_start = tmp.alloc<double>(len);
+      double* d_w = tmp.alloc<double>(len);
+      void* d_v = (h->precision == SMGPU_FP64) ? (void*)tmp.alloc<double>(len) : (void*)tmp.alloc<float>(len);
+      char* flush = flush_l2 ? tmp.alloc<char>(256u << 20) : nullptr;
+      launch_start_vector(h->dt, 1234ull, d_start, h->st);
+      if (h->precision == SMGPU_FP64)
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(d_v, d_start, sizeof(double) * len, cudaMemcpyDeviceToDevice, h->st));
+      else
+        launch_scale_store_plain(d_start, (float*)d_v, len, h->st);
+      SMGPU_CUDA_TRY(cudaEventCreate(&a));
+      SMGPU_CUDA_TRY(cudaEventCreate(&b));
+      double total = 0.0;
+      for (int r = 0; r < reps; ++r) {
+        if (flush) SMGPU_CUDA_TRY(cudaMemsetAsync(flush, r & 0xff, 256u << 20, h->st));
+        SMGPU_CUDA_TRY(cudaEventRecord(a, h->st));
+        if (h->precision == SMGPU_FP64) h->hv<double>((const double*)d_v, d_w, nullptr, h->st);
+        else h->hv<float>((const float*)d_v, d_w, nullptr, h->st);
+        SMGPU_CUDA_TRY(cudaEventRecord(b, h->st));
+        SMGPU_CUDA_TRY(cudaEventSynchronize(b));
+        float ms = 0.f;
+        SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+        total += ms;
+      }
+      SMGPU_CUDA_TRY(cudaGetLastError());
+      *ms_out = total / reps;
+    } catch (...) {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      tmp.free_all();
+      throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    tmp.free_all();
+    return SMGPU_OK;
   });
 }
 

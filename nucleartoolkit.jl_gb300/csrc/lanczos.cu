@@ -618,6 +618,13 @@ inline int grid_for(int64_t len) {
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
+__global__ void k_convert(const double* __restrict__ a, float* __restrict__ b, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+void launch_scale_store_plain(const double* a, float* b, int64_t len, cudaStream_t st) {
+  k_convert<<<grid_for(len), kNT, 0, st>>>(a, b, len);
+}
 void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st) {
   k_start_vector<<<grid_for(t.len_pad), kNT, 0, st>>>(t, seed, w);
 }

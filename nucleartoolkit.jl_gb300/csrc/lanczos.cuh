@@ -57,6 +57,7 @@ struct LanczosDev {
 };
 
 void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st);
+void launch_scale_store_plain(const double* a, float* b, int64_t len, cudaStream_t st);
 template <class TX>
 void launch_multidot(const LanczosDev& L, const TX* X, int m, const double* y, bool self, const int* gate,
                      cudaStream_t st);

@@ -39,6 +39,7 @@ SIGNATURES = {
     "smgpu_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),
+    "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _lib = None

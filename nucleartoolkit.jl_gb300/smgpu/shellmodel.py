@@ -79,8 +79,14 @@ class ShellModelProblem:
     def timings(self):
         t = np.zeros(8)
         check(load().smgpu_timings(self._h, _p(t)), self._h)
-        keys = ["setup", "lanczos", "matvec", "reorth", "restart", "ritz", "h2d", "d2h"]
+        keys = ["setup", "lanczos", "matvec", "capture", "ritz", "solve_wall", "r6", "r7"]
         return dict(zip(keys, map(float, t)))
+
+    def time_matvec(self, reps=20, flush_l2=True):
+        """Mean ms per H·v launch, CUDA events on the library's stream."""
+        ms = C.c_double()
+        check(load().smgpu_time_matvec(self._h, int(reps), 1 if flush_l2 else 0, C.byref(ms)), self._h)
+        return float(ms.value)
 
     # --- compute
     def matvec(self, v, accumulate: bool = False, out=None):
@@ -94,14 +100,15 @@ class ShellModelProblem:
         nev = min(num_ev, self.mdim)
         ev = np.zeros(nev)
         vecs = np.zeros((nev, self.mdim)) if want_vecs else None
-        stats = np.zeros(6, dtype=np.int32)
+        stats = np.zeros(8, dtype=np.int32)
         v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
         rc = load().smgpu_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts), _p(v1a),
                                 _p(ev), _p(vecs), _p(stats))
         if rc not in (_lib.OK, _lib.ERR_NOCONV):
             check(rc, self._h)
         return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_matvec=int(stats[1]), n_restart=int(stats[2]),
-                    converged=bool(stats[3]) and rc == _lib.OK, n_second_pass=int(stats[5]), status=rc)
+                    converged=bool(stats[3]) and rc == _lib.OK, n_second_pass=int(stats[5]),
+                    kernel_launches=int(stats[6]), status=rc)
 
 
 def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=False, is_show=False,

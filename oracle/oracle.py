@@ -46,6 +46,8 @@ def lib():
         L.orc_v1_export.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_spe_diag.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.orc_operate_H.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.orc_nnz.restype = C.c_longlong
+        L.orc_nnz.argtypes = [vp]
         L.orc_start_vector.argtypes = [C.c_longlong, C.c_ulonglong, C.c_void_p]
         L.orc_trl.restype = C.c_int
         L.orc_trl.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
@@ -171,6 +173,10 @@ class OracleProblem:
         twf = np.zeros_like(wf)
         lib().orc_operate_H(self._h, _p(wf), _p(twf))
         return twf
+
+    def nnz(self) -> int:
+        """Structural non-zeros of H (distinct (row, col) pairs, diagonal included)."""
+        return int(lib().orc_nnz(self._h))
 
     def dense_H(self):
         n = self.mdim

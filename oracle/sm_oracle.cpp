@@ -826,6 +826,62 @@ void operate_H(const Problem& P, const double* wf, double* twf) {
   }
 }
 
+// Number of distinct (row, col) pairs that operate_H! touches: the structural
+// non-zeros of H (diagonal included).  Each block's owner emits the pairs of
+// its rows in the same loops as operate_H!, then sorts and de-duplicates them.
+long long count_nnz(const Problem& P) {
+  const auto& B = P.B;
+  int nb = (int)B.pbits.size();
+  long long total = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : total)
+  for (int bi = 1; bi <= nb; ++bi) {
+    std::vector<u64> pr;
+    auto push = [&](i64 row, i64 col) { pr.push_back(((u64)(row - 1) << 32) | (u64)(col - 1)); };
+    i64 idim = B.tdims[bi - 1];
+    i64 l_Np = (i64)B.pbits[bi - 1].size(), l_Nn = (i64)B.nbits[bi - 1].size();
+    i64 offset = idim - l_Nn;
+    for (size_t bfidx = 0; bfidx < P.bfs[bi - 1].size(); ++bfidx) {
+      int bf = P.bfs[bi - 1][bfidx];
+      i64 l_Nn_f = (i64)B.nbits[bf - 1].size(), off_f = B.tdims[bf - 1] - l_Nn_f;
+      const auto& pN = P.pNiNfs[bi - 1][bfidx];
+      const auto& nN = P.nNiNfs[bi - 1][bfidx];
+      for (size_t nth = 0; nth < pN.size(); ++nth)
+        for (const Ifph& pj : pN[nth])
+          for (const Ifph& nj : nN[nth]) push(offset + pj.i * l_Nn + nj.i, off_f + pj.f * l_Nn_f + nj.f);
+    }
+    for (size_t j = 0; j + 1 < P.bis[bi - 1].size(); ++j) {
+      int tbi = P.bis[bi - 1][j];
+      const auto& bft = P.bfs[tbi - 1];
+      int r2 = (int)(std::lower_bound(bft.begin(), bft.end(), bi) - bft.begin());
+      i64 l_Nn_i = (i64)B.nbits[tbi - 1].size(), off_f = B.tdims[tbi - 1] - l_Nn_i;
+      const auto& pN = P.pNiNfs[tbi - 1][r2];
+      const auto& nN = P.nNiNfs[tbi - 1][r2];
+      for (size_t nth = 0; nth < pN.size(); ++nth)
+        for (const Ifph& pj : pN[nth])
+          for (const Ifph& nj : nN[nth]) push(offset + pj.f * l_Nn + nj.f, off_f + pj.i * l_Nn_i + nj.i);
+    }
+    for (i64 Npi = 1; Npi <= l_Np; ++Npi)
+      for (const T1info& t1 : P.pp[bi - 1][Npi - 1])
+        for (i64 n = 1; n <= l_Nn; ++n) {
+          i64 Mi = offset + Npi * l_Nn + n, Mf = offset + t1.f * l_Nn + n;
+          push(Mf, Mi);
+          push(Mi, Mf);
+        }
+    for (i64 Nni = 1; Nni <= l_Nn; ++Nni)
+      for (const T1info& t1 : P.nn[bi - 1][Nni - 1])
+        for (i64 p = 1; p <= l_Np; ++p) {
+          i64 Mi = offset + p * l_Nn + Nni, Mf = offset + p * l_Nn + t1.f;
+          push(Mf, Mi);
+          push(Mi, Mf);
+        }
+    for (i64 p = 1; p <= l_Np; ++p)
+      for (i64 n = 1; n <= l_Nn; ++n) push(offset + p * l_Nn + n, offset + p * l_Nn + n);
+    std::sort(pr.begin(), pr.end());
+    total += (long long)(std::unique(pr.begin(), pr.end()) - pr.begin());
+  }
+  return total;
+}
+
 // ---------------------------------------------------------------------------
 // Dense symmetric eigen-decomposition by cyclic Jacobi rotations (stands in
 // for LAPACK eigen/eigvals at lanczos_methods.jl:255,261 and
@@ -1216,6 +1272,8 @@ void orc_spe_diag(void* h, double* ep, double* en) {
 
 // twf += H wf   (lanczos_methods.jl:153 operate_H! semantics)
 void orc_operate_H(void* h, const double* wf, double* twf) { operate_H(*(Problem*)h, wf, twf); }
+
+long long orc_nnz(void* h) { return count_nnz(*(Problem*)h); }
 
 void orc_start_vector(long long mdim, unsigned long long seed, double* v) {
   for (i64 i = 0; i < mdim; ++i) v[i] = start_elem(seed, i);

@@ -1,0 +1,218 @@
+"""GPU library vs the CPU oracle through the C ABI (needs a GB300)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CKPOT = os.path.join(GOLDEN, "ckpot.snt")
+USDB = os.path.join(GOLDEN, "usdb.snt")
+
+# Tolerances (stated here, used below)
+MATVEC_FP64_RTOL = 1e-12   # FP64 H·v vs oracle operate_H!, relative to max|w|
+MATVEC_MIXED_RTOL = 2e-6   # FP32-mixed H·v vs oracle, relative to max|w|
+EIG_FP64_RTOL = 1e-8       # FP64 eigenvalues vs oracle TRL, relative
+EIG_MIXED_ATOL = 1e-4      # FP32-mixed eigenvalues vs oracle, MeV
+
+
+def _cases(snt_dir):
+    return {
+        "ckpot_Be8": (CKPOT, "Be8"),
+        "usdb_Na21": (USDB, "Na21"),   # odd A, uneven vp/vn
+        "usdb_O19": (USDB, "O19"),     # zero valence protons
+        "sd2p2n": snt_dir["sd2p2n"],
+        "sd4p4n": snt_dir["sd4p4n"],
+    }
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from smgpu import _lib
+    from smgpu import build as b
+    b.build()
+    return _lib.load()
+
+
+def _oracle(snt, nuc):
+    from oracle.oracle import OracleProblem
+    return OracleProblem(snt, nuc)
+
+
+def _gpu(snt, nuc, prec=0):
+    from smgpu import ShellModelProblem
+    return ShellModelProblem(snt, nuc, prec)
+
+
+@pytest.mark.parametrize("case", ["ckpot_Be8", "usdb_Na21", "usdb_O19", "sd2p2n", "sd4p4n", "pf4p4n"])
+def test_basis_bit_exact(lib, snt_dir, case):
+    snt, nuc = snt_dir["pf4p4n"] if case == "pf4p4n" else _cases(snt_dir)[case]
+    O, G = _oracle(snt, nuc), _gpu(snt, nuc)
+    assert G.mdim == O.mdim and G.nblocks == O.nblocks
+    assert np.array_equal(G.tdims, O.tdims)
+    assert np.array_equal(G.np_, O.np_) and np.array_equal(G.nn_, O.nn_)
+    assert np.array_equal(G.Mp, O.Mp) and np.array_equal(G.Mn, O.Mn)
+    gp, gn = G.basis()
+    op, on = O.sds()
+    assert np.array_equal(gp.astype(np.int64), op) and np.array_equal(gn.astype(np.int64), on)
+
+
+def _oracle_pn_set(O, which):
+    """Distinct (bi, bf, op1, op2, i, f, phase) of the reference's per-V-entry lists."""
+    bi, bf, nth, i, f, ph = O.jumps_pn(which)
+    delMs, idx, abcd, V = O.vpn()
+    # map (bi, bf, nth) -> operator bits: nth indexes Vpn[ΔM] for ΔM = Mps[bf]-Mps[bi]
+    starts = np.concatenate([[0], np.cumsum(np.bincount(idx, minlength=len(delMs)))])
+    Mps = O.Mp  # block M values; differences equal the reference's Mps differences
+    out = set()
+    for k in range(len(bi)):
+        dm = int(Mps[bf[k] - 1] - Mps[bi[k] - 1])
+        di = int(np.where(delMs == dm)[0][0])
+        row = abcd[starts[di] + nth[k] - 1]
+        ops = (int(row[0]), int(row[2])) if which == 0 else (int(row[1]), int(row[3]))
+        out.add((int(bi[k]), int(bf[k])) + ops + (int(i[k]), int(f[k]), int(ph[k])))
+    return out
+
+
+@pytest.mark.parametrize("case", ["ckpot_Be8", "usdb_Na21", "sd2p2n", "sd4p4n"])
+def test_jump_tables_match_reference(lib, snt_dir, case):
+    snt, nuc = _cases(snt_dir)[case]
+    O, G = _oracle(snt, nuc), _gpu(snt, nuc)
+    for which in (0, 1):
+        g = {tuple(map(int, r)) for r in G.jumps(which)}
+        assert g == _oracle_pn_set(O, which), f"pn table {which}"
+    for which, ow in ((2, 0), (3, 1)):
+        ints, coef = G.jumps(which)
+        blk, i, f, c = O.jumps_2b(ow)
+        ref = {}
+        for k in range(len(blk)):
+            key = (int(blk[k]), int(i[k]), int(f[k]))
+            ref[key] = ref.get(key, 0.0) + c[k]
+        got = {tuple(map(int, r)): v for r, v in zip(ints, coef)}
+        ref = {k: v for k, v in ref.items() if v != 0.0}
+        got = {k: v for k, v in got.items() if v != 0.0}
+        assert set(got) == set(ref)
+        scale = max(abs(v) for v in ref.values())
+        assert max(abs(got[k] - ref[k]) for k in ref) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("case", ["ckpot_Be8", "usdb_Na21", "usdb_O19", "sd2p2n", "sd4p4n"])
+def test_matvec_fp64_and_mixed(lib, snt_dir, case):
+    snt, nuc = _cases(snt_dir)[case]
+    O = _oracle(snt, nuc)
+    v = np.random.default_rng(3).standard_normal(O.mdim)
+    ref = O.operate_H(v)
+    scale = np.abs(ref).max()
+    G = _gpu(snt, nuc, 0)
+    assert np.abs(G.matvec(v) - ref).max() <= MATVEC_FP64_RTOL * scale
+    # accumulate = operate_H!'s "twf += H wf"
+    w0 = np.full(O.mdim, 0.25)
+    assert np.abs(G.matvec(v, accumulate=True, out=w0.copy()) - (ref + 0.25)).max() <= MATVEC_FP64_RTOL * scale
+    M = _gpu(snt, nuc, 1)
+    assert np.abs(M.matvec(v) - ref).max() <= MATVEC_MIXED_RTOL * scale
+
+
+def test_matvec_pf_full_size(lib, snt_dir):
+    """48Cr pf (dim 1,963,461): FP64 H·v vs the oracle, mixed vs FP64, and
+    the size-independent symmetry <u,Hv> = <Hu,v>."""
+    snt, nuc = snt_dir["pf4p4n"]
+    O = _oracle(snt, nuc)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(O.mdim)
+    u = rng.standard_normal(O.mdim)
+    ref = O.operate_H(v)
+    G = _gpu(snt, nuc, 0)
+    w = G.matvec(v)
+    scale = np.abs(ref).max()
+    assert np.abs(w - ref).max() <= MATVEC_FP64_RTOL * scale
+    hu = G.matvec(u)
+    assert abs(u @ w - hu @ v) <= 1e-12 * np.linalg.norm(u) * np.linalg.norm(w)
+    M = _gpu(snt, nuc, 1)
+    assert np.abs(M.matvec(v) - ref).max() <= MATVEC_MIXED_RTOL * scale
+
+
+def test_ckpot_known_answer_on_gpu(lib, golden):
+    g = golden["ckpot_Be8"]
+    for prec in (0, 1):
+        G = _gpu(CKPOT, "Be8", prec)
+        r = G.solve(10, lm=300, ls=20, tol=1e-8)
+        assert r["converged"]
+        for e, ref in zip(r["evals"], g["energies"]):
+            assert (e - ref) ** 2 < g["tolerance_sq"]
+
+
+@pytest.mark.parametrize("case,nev,lm,ls", [("sd2p2n", 5, 300, 20), ("sd4p4n", 10, 30, 15), ("usdb_Na21", 5, 40, 15),
+                                            ("sd4p4n", 5, 100, 20)])
+def test_eigenvalues_vs_oracle(lib, snt_dir, case, nev, lm, ls):
+    snt, nuc = _cases(snt_dir)[case]
+    O = _oracle(snt, nuc)
+    ro = O.trl(nev, lm=lm, ls=ls, tol=1e-8)
+    assert ro["converged"]
+    G = _gpu(snt, nuc, 0)
+    rg = G.solve(nev, lm=lm, ls=ls, tol=1e-8)
+    assert rg["converged"]
+    assert np.allclose(rg["evals"], ro["evals"], rtol=EIG_FP64_RTOL, atol=0)
+    M = _gpu(snt, nuc, 1)
+    rm = M.solve(nev, lm=lm, ls=ls, tol=1e-8)
+    assert np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL
+
+
+def test_ritz_vectors(lib, snt_dir):
+    snt, nuc = snt_dir["sd4p4n"]
+    G = _gpu(snt, nuc, 0)
+    r = G.solve(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    X = r["evecs"]
+    for k in range(3):
+        x = X[k]
+        assert abs(np.linalg.norm(x) - 1) < 1e-12
+        res = G.matvec(x) - r["evals"][k] * x
+        assert np.linalg.norm(res) < 1e-3
+    O = _oracle(snt, nuc)
+    ro = O.trl(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    for k in range(3):
+        assert abs(abs(X[k] @ ro["evecs"][k]) - 1.0) < 1e-6
+
+
+def test_user_start_vector_and_noconv(lib, snt_dir):
+    from smgpu import _lib as L
+    snt, nuc = snt_dir["sd2p2n"]
+    G = _gpu(snt, nuc, 0)
+    v1 = np.ones(G.mdim)
+    r = G.solve(3, lm=30, ls=10, tol=1e-8, v1=v1)
+    O = _oracle(snt, nuc)
+    ro = O.trl(3, lm=30, ls=10, tol=1e-8, v1=v1)
+    assert np.allclose(r["evals"], ro["evals"], rtol=EIG_FP64_RTOL)
+    r2 = G.solve(5, lm=8, ls=3, tol=1e-14, max_restarts=1)
+    assert r2["status"] == L.ERR_NOCONV and not r2["converged"]
+
+
+def test_error_paths(lib, tmp_path):
+    from smgpu import SmgpuError, ShellModelProblem
+    from smgpu import _lib as L
+    with pytest.raises(SmgpuError) as e:
+        ShellModelProblem(str(tmp_path / "missing.snt"), "Be8")
+    assert e.value.code == L.ERR_IO
+    with pytest.raises(SmgpuError) as e:
+        ShellModelProblem(CKPOT, "Xx8")
+    assert e.value.code == L.ERR_NUCLEUS
+    bad = tmp_path / "bad.snt"
+    bad.write_text("2 2 2 2\n1 0 1 1 -1\n")
+    with pytest.raises(SmgpuError) as e:
+        ShellModelProblem(str(bad), "Be8")
+    assert e.value.code == L.ERR_PARSE
+    with pytest.raises(SmgpuError) as e:
+        ShellModelProblem(CKPOT, "He3")  # below the snt core
+    assert e.value.code == L.ERR_NUCLEUS
+    G = ShellModelProblem(CKPOT, "Be8")
+    with pytest.raises(SmgpuError) as e:
+        G.solve(0)
+    assert e.value.code == L.ERR_ARG
+
+
+def test_main_sm_mirror(lib, golden):
+    from smgpu import main_sm
+    en = main_sm(CKPOT, "Be8", 10, [], verbose=False)
+    for e, ref in zip(en, golden["ckpot_Be8"]["energies"]):
+        assert (e - ref) ** 2 < 1e-6
