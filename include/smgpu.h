@@ -138,9 +138,10 @@ int smgpu_timings(const smgpu_problem* h, double* times_out);
  * ms_out: mean milliseconds per launch. */
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
-/* Structural statistics of the factorised H: [updates per H·v (multiply-adds),
- * pn proton pull entries, pn neutron entries, pp entries, nn entries,
- * table bytes on the device, padded vector length, number of links]. */
+/* Structural statistics of the factorised H (10 entries): [updates per H·v
+ * (multiply-adds), pn proton pull entries, pn neutron entries, pp entries,
+ * nn entries, table bytes on the device, padded vector length, number of
+ * links, H·v threads per CTA, H·v rows per CTA (the autotuned shape)]. */
 int smgpu_stats(const smgpu_problem* h, long long* stats_out);
 
 #ifdef __cplusplus

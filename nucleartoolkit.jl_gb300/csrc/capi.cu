@@ -2,16 +2,29 @@
 //
 // A handle owns one problem: the host tables from setup.cpp, their device
 // copies, and (during smgpu_solve) the Krylov basis.  The Lanczos iteration
-// of one restart cycle — H·v, α, the eigenvalue test, re-orthogonalisation,
-// β, the next basis vector and the thick restart — is captured once as a CUDA
-// graph and replayed until the device-side convergence flag is set; the host
-// reads that flag once per cycle.  The eigenvalue test of iteration k runs on
-// a second stream concurrently with the re-orthogonalisation of iteration k
-// and the H·v of iteration k+1.
+// of one restart cycle — H·v with its α/three-term epilogue, the eigenvalue
+// test, the re-orthogonalisation passes, β, the next basis vector and the
+// thick restart — is captured once as a CUDA graph and replayed until the
+// device-side convergence flag is set; the host reads that flag once per
+// cycle.  The eigenvalue test of iteration k runs on a second stream,
+// concurrently with the re-orthogonalisation of iteration k and the H·v of
+// iteration k+1.
+//
+// H·v launch shape (threads per CTA, rows per CTA) is chosen per problem by a
+// small autotuner that times the candidate shapes on the device; results are
+// cached per shape class (precision, m-states and valence particles of both
+// species, total M) for the life of the process, and in the file named by
+// SMGPU_TUNE_CACHE when that variable is set.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/smgpu.h"
@@ -60,30 +73,91 @@ std::vector<float> to_f32(const std::vector<T>& v) {
   for (size_t i = 0; i < v.size(); ++i) r[i] = (float)v[i];
   return r;
 }
+
+// ---- autotuner cache: shape class -> (threads, rows)
+typedef std::tuple<int, int, int, int, int, int> ShapeKey;  // precision, Lp, Ln, vp, vn, mtot2
+std::mutex g_tune_mu;
+std::map<ShapeKey, std::pair<int, int>> g_tune;
+bool g_tune_file_loaded = false;
+
+void tune_file_load() {
+  if (g_tune_file_loaded) return;
+  g_tune_file_loaded = true;
+  const char* path = std::getenv("SMGPU_TUNE_CACHE");
+  if (!path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  int a[8];
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7]) == 8)
+    g_tune[ShapeKey{a[0], a[1], a[2], a[3], a[4], a[5]}] = {a[6], a[7]};
+  std::fclose(f);
+}
+void tune_file_store() {
+  const char* path = std::getenv("SMGPU_TUNE_CACHE");
+  if (!path) return;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return;
+  for (auto& kv : g_tune)
+    std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
+                 std::get<3>(kv.first), std::get<4>(kv.first), std::get<5>(kv.first), kv.second.first,
+                 kv.second.second);
+  std::fclose(f);
+}
 }  // namespace
 
 struct smgpu_problem {
   int precision = SMGPU_FP64;
+  int vp = 0, vn = 0, mtot2 = 0;
   Tables T;
   DeviceArena tables;
   DevTables dt{};
+  TileTables tt{};
   CoefTables<double> c64{};
   CoefTables<float> c32{};
   const double* d_ep = nullptr;
   const double* d_en = nullptr;
-  int nrows = 0;
+  HvConfig cfg{128, 4, 0};
+  std::map<int, std::pair<const int*, const int*>> task_arrays;  // rows -> (task_b, task_p0)
+  std::map<int, int> task_count;
   cudaStream_t st = nullptr, st2 = nullptr;
   std::string err;
   double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_ms[16] = {0};
   int sms = 152;
-  // solver state of the last solve
-  DeviceArena solver;
+  DeviceArena solver;  // Krylov basis and scratch of the last solve
 
   ~smgpu_problem() {
     solver.free_all();
     tables.free_all();
     if (st) cudaStreamDestroy(st);
     if (st2) cudaStreamDestroy(st2);
+  }
+
+  // Row tasks of R rows each, largest blocks first.
+  void ensure_tasks(int R) {
+    if (task_arrays.count(R)) return;
+    std::vector<int> order(T.nb);
+    for (int b = 0; b < T.nb; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return (int64_t)T.nn[x] * (T.ppn_ptr[T.pstart[x + 1]] - T.ppn_ptr[T.pstart[x]] + 1) >
+             (int64_t)T.nn[y] * (T.ppn_ptr[T.pstart[y + 1]] - T.ppn_ptr[T.pstart[y]] + 1);
+    });
+    std::vector<int> tb, tp;
+    for (int b : order)
+      for (int p0 = 0; p0 < T.np[b]; p0 += R) {
+        tb.push_back(b);
+        tp.push_back(p0);
+      }
+    task_arrays[R] = {tables.upload(tb), tables.upload(tp)};
+    task_count[R] = (int)tb.size();
+  }
+  void set_config(int nt, int R) {
+    ensure_tasks(R);
+    cfg.nt = nt;
+    cfg.rows = R;
+    cfg.ntasks = task_count[R];
+    tt.task_b = task_arrays[R].first;
+    tt.task_p0 = task_arrays[R].second;
   }
 
   void upload() {
@@ -102,11 +176,6 @@ struct smgpu_problem {
     dt.pstart = tables.upload(T.pstart);
     dt.nstart = tables.upload(T.nstart);
     dt.tdims = tables.upload(T.tdims);
-    std::vector<int> prow(T.pstart[nb]);
-    for (int b = 0; b < nb; ++b)
-      for (int g = T.pstart[b]; g < T.pstart[b + 1]; ++g) prow[g] = b;
-    nrows = T.pstart[nb];
-    dt.prow_block = tables.upload(prow);
     dt.pp_ptr = tables.upload(T.pp_ptr);
     dt.pp_col = tables.upload(T.pp_col);
     dt.nn_ptr = tables.upload(T.nn_ptr);
@@ -115,42 +184,142 @@ struct smgpu_problem {
     std::vector<int64_t> lv(T.links.size()), ln(T.links.size());
     for (size_t k = 0; k < T.links.size(); ++k) {
       la[k] = make_int4(T.links[k].s, T.links[k].nB, T.links[k].dm, 0);
-      lv[k] = T.links[k].vtab_off;
+      lv[k] = 2 * T.links[k].vtab_off;  // signed (V, -V) table
       ln[k] = T.links[k].nptr_off;
     }
     dt.link_a = tables.upload(la);
     dt.link_v = tables.upload(lv);
     dt.link_n = tables.upload(ln);
-    dt.ppn_ptr = tables.upload(T.ppn_ptr);
     dt.ppn_src = tables.upload(T.ppn_src);
     dt.ppn_meta = tables.upload(T.ppn_meta);
-    dt.npn_ptr = tables.upload(T.npn_ptr);
-    dt.npn_ent = tables.upload(T.npn_ent);
     d_ep = tables.upload(T.ep);
     d_en = tables.upload(T.en);
+    // row-tile tables: per (row, link slot) first proton entry
+    std::vector<int64_t> rl_base(nb);
+    std::vector<int> rl;
+    for (int b = 0; b < nb; ++b) {
+      rl_base[b] = (int64_t)rl.size();
+      const int lb = T.link_begin[b], nl = T.link_begin[b + 1] - lb;
+      for (int g = T.pstart[b]; g < T.pstart[b + 1]; ++g) {
+        int e = T.ppn_ptr[g];
+        for (int j = 0; j <= nl; ++j) {
+          while (e < T.ppn_ptr[g + 1] && (int)(T.ppn_meta[e] >> 16) < lb + j) ++e;
+          rl.push_back(e);
+        }
+      }
+    }
+    tt.link_begin = tables.upload(T.link_begin);
+    tt.rl_base = tables.upload(rl_base);
+    tt.rl = tables.upload(rl);
+    tt.npn_ptr = tables.upload(T.npn_ptr);
+    // neutron entries with the sign folded into the (V, -V) table index
+    std::vector<uint32_t> ent(T.npn_ent.size());
+    for (size_t li = 0; li < T.links.size(); ++li) {
+      const auto& L = T.links[li];
+      const uint32_t nab = (uint32_t)(L.nA * L.nB);
+      for (int64_t j = T.npn_ptr[L.nptr_off]; j < T.npn_ptr[L.nptr_off + T.nn[L.b]]; ++j) {
+        uint32_t e = T.npn_ent[j];
+        uint32_t col = ((e >> 1) & 0x1fffu) + ((e & 1u) ? nab : 0u);
+        if (col >= (1u << 14)) throw SetupError{SMGPU_ERR_LIMIT, "pn coefficient table too large for the packing"};
+        ent[j] = (e & ~0x3fffu) | col;
+      }
+    }
+    tt.npn_ent = tables.upload(ent);
+    // signed coefficient tables
+    std::vector<double> vt2(2 * T.vtab.size());
+    for (size_t k = 0; k + 1 < T.vtab_off_dm.size(); ++k) {
+      const int64_t o = T.vtab_off_dm[k], n = T.vtab_off_dm[k + 1] - o;
+      for (int64_t x = 0; x < n; ++x) {
+        vt2[2 * o + x] = T.vtab[o + x];
+        vt2[2 * o + n + x] = -T.vtab[o + x];
+      }
+    }
     if (precision == SMGPU_FP64) {
       c64.pp_val = tables.upload(T.pp_val);
       c64.nn_val = tables.upload(T.nn_val);
-      c64.vtab = tables.upload(T.vtab);
+      c64.vtab = tables.upload(vt2);
     } else {
       c32.pp_val = tables.upload(to_f32(T.pp_val));
       c32.nn_val = tables.upload(to_f32(T.nn_val));
-      c32.vtab = tables.upload(to_f32(T.vtab));
+      c32.vtab = tables.upload(to_f32(vt2));
     }
+    set_config(128, 4);
   }
 
-  template <class TX>
-  void hv(const TX* v, double* w, const int* done, cudaStream_t s);
+  void hv(const double* v, double* w, const HvEpilogue<double>& epi, cudaStream_t s) {
+    launch_hv_fp64(dt, tt, cfg, d_ep, d_en, c64, v, w, epi, s);
+  }
+  void hv(const float* v, double* w, const HvEpilogue<float>& epi, cudaStream_t s) {
+    launch_hv_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
+  }
+
+  // Time every candidate launch shape on a device vector and keep the fastest.
+  void autotune() {
+    ShapeKey key{precision, T.Lp, T.Ln, vp, vn, mtot2};
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      tune_file_load();
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        set_config(it->second.first, it->second.second);
+        return;
+      }
+    }
+    const char* off = std::getenv("SMGPU_AUTOTUNE");
+    if (off && std::string(off) == "0") return;
+    DeviceArena tmp;
+    cudaEvent_t a = nullptr, b = nullptr;
+    try {
+      double* d_start = tmp.alloc<double>(T.len_pad);
+      double* d_w = tmp.alloc<double>(T.len_pad);
+      void* d_v = (precision == SMGPU_FP64) ? (void*)tmp.alloc<double>(T.len_pad) : (void*)tmp.alloc<float>(T.len_pad);
+      launch_start_vector(dt, 1234ull, d_start, st);
+      if (precision == SMGPU_FP64)
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(d_v, d_start, sizeof(double) * T.len_pad, cudaMemcpyDeviceToDevice, st));
+      else
+        launch_convert(d_start, (float*)d_v, T.len_pad, st);
+      SMGPU_CUDA_TRY(cudaEventCreate(&a));
+      SMGPU_CUDA_TRY(cudaEventCreate(&b));
+      int nc = 0;
+      const HvConfig* cand = hv_candidates(&nc);
+      int best = -1;
+      float best_ms = 1e30f;
+      for (int c = 0; c < nc; ++c) {
+        set_config(cand[c].nt, cand[c].rows);
+        float total = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {
+          SMGPU_CUDA_TRY(cudaEventRecord(a, st));
+          if (precision == SMGPU_FP64) hv((const double*)d_v, d_w, HvEpilogue<double>{}, st);
+          else hv((const float*)d_v, d_w, HvEpilogue<float>{}, st);
+          SMGPU_CUDA_TRY(cudaEventRecord(b, st));
+          SMGPU_CUDA_TRY(cudaEventSynchronize(b));
+          float ms = 0.f;
+          SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+          if (rep > 0) total += ms;  // first launch is the warm-up
+        }
+        SMGPU_CUDA_TRY(cudaGetLastError());
+        if (c < 16) tune_ms[c] = total / 2;
+        if (total < best_ms) {
+          best_ms = total;
+          best = c;
+        }
+      }
+      set_config(cand[best].nt, cand[best].rows);
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = {cfg.nt, cfg.rows};
+      tune_file_store();
+    } catch (...) {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      tmp.free_all();
+      throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    tmp.free_all();
+  }
 };
 
-template <>
-void smgpu_problem::hv<double>(const double* v, double* w, const int* done, cudaStream_t s) {
-  launch_hv_fp64(dt, d_ep, d_en, c64, v, w, nrows, done, s);
-}
-template <>
-void smgpu_problem::hv<float>(const float* v, double* w, const int* done, cudaStream_t s) {
-  launch_hv_mixed(dt, d_ep, d_en, c32, v, w, nrows, done, s);
-}
 
 namespace {
 
@@ -186,11 +355,15 @@ int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision
   smgpu_problem* h = new smgpu_problem();
   try {
     h->precision = precision;
+    h->vp = vp;
+    h->vn = vn;
+    h->mtot2 = mtot2;
     double t0 = now_s();
     build_tables(I, vp, vn, mtot2, h->T);
     if (h->T.mdim == 0) throw SetupError{SMGPU_ERR_EMPTY, "M-scheme dimension is zero"};
     h->upload();
-    SMGPU_CUDA_TRY(cudaDeviceSynchronize());
+    h->autotune();
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(h->st));
     h->times[0] = now_s() - t0;
   } catch (...) {
     delete h;
@@ -208,7 +381,7 @@ struct Solve {
   TX* V = nullptr;
   TX* U = nullptr;
   double* w = nullptr;
-  int gate_done = 1, gate_second = 2;  // host copies of the gate codes
+  long long launches_first = 0, launches_rest = 0;
 
   void alloc(int lm, int ls, int num_ev, double tol) {
     DeviceArena& A = P->solver;
@@ -221,6 +394,7 @@ struct Solve {
     L.len = P->T.len_pad;
     L.mdim = P->T.mdim;
     L.tol = tol;
+    L.nalpha = P->cfg.ntasks;
     const int P_gram = ls * (ls + 1) / 2 + ls;
     const int npart = std::max(lm + 2, P_gram) + 2;
     V = A.alloc<TX>((size_t)lm * L.len);
@@ -228,6 +402,11 @@ struct Solve {
     w = A.alloc<double>(L.len);
     L.T = A.alloc<double>((size_t)lm * lm);
     L.en = A.alloc<double>((size_t)L.nh * num_ev);
+    L.alpha_part = A.alloc<double>((size_t)lm * L.nalpha);
+    L.pdot = A.alloc<double>((size_t)(lm + 2) * L.G);
+    L.pn1 = A.alloc<double>(L.G);
+    L.pdot2 = A.alloc<double>((size_t)(lm + 2) * L.G);
+    L.pn2 = A.alloc<double>(L.G);
     L.partials = A.alloc<double>((size_t)npart * L.G);
     L.h = A.alloc<double>(lm + 2);
     L.jacA = A.alloc<double>((size_t)lm * lm);
@@ -249,36 +428,30 @@ struct Solve {
 
   // v1 -> V[0] normalised (start vector in w on entry)
   void init_start() {
-    launch_multidot<double>(L, w, 1, w, false, nullptr, P->st);
-    launch_reduce(L, 1, RED_INVNORM, L.h, 0, nullptr, P->st);
-    launch_scale_store<TX>(L, w, V, L.h, nullptr, P->st);
+    launch_multidot<double>(L, w, 1, w, false, P->st);
+    launch_reduce(L, 1, RED_INVNORM, L.h, P->st);
+    launch_scale_store<TX>(L, w, V, L.h, P->st);
   }
 
   // One Lanczos iteration, `it` 1-based (lanczos_methods.jl:34-62).
-  void iteration(int it, int lock, cudaEvent_t ev_fork, cudaEvent_t ev_join, bool first_of_cycle) {
+  void iteration(int it, int lock, cudaEvent_t ev_fork) {
     cudaStream_t s = P->st, s2 = P->st2;
     const int it0 = it - 1;
     TX* vk = V + (size_t)it0 * L.len;
-    P->hv<TX>(vk, w, &L.fl->done, s);  // gate read from device memory
-    launch_multidot<TX>(L, vk, 1, w, false, &gate_done, s);
-    launch_reduce(L, 1, RED_ALPHA, nullptr, it0, &gate_done, s);
+    HvEpilogue<TX> epi{};
+    epi.fl = L.fl;
+    epi.alpha_part = L.alpha_part + (size_t)it0 * L.nalpha;
+    if (it0 > lock) {
+      // three-term correction; the first iteration after a restart couples to
+      // every kept Ritz vector and is left to the Gram-Schmidt passes
+      epi.vprev = V + (size_t)(it0 - 1) * L.len;
+      epi.beta = L.T + (size_t)(it0 - 1) * L.lm + it0;
+    }
+    P->hv(vk, w, epi, s);
     SMGPU_CUDA_TRY(cudaEventRecord(ev_fork, s));
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
     launch_sturm(L, it, lock, s2);
-    (void)first_of_cycle;
-    (void)ev_join;
-    // ReORTH: classical Gram-Schmidt with a second pass when the norm drops
-    // below 1/sqrt(2) of its value (FP64 throughout)
-    launch_multidot<TX>(L, V, it, w, true, &gate_done, s);
-    launch_reduce(L, it, RED_H, L.h, it0, &gate_done, s);
-    launch_multiaxpy<TX>(L, V, it, w, &gate_done, s);
-    launch_reduce(L, 1, RED_NRM_CHECK, nullptr, it0, &gate_done, s);
-    launch_multidot<TX>(L, V, it, w, false, &gate_second, s);
-    launch_reduce(L, it, RED_STORE, L.h, it0, &gate_second, s);
-    launch_multiaxpy<TX>(L, V, it, w, &gate_second, s);
-    launch_reduce(L, 1, RED_NRM, nullptr, it0, &gate_second, s);
-    launch_beta(L, it0, s);
-    launch_scale_store<TX>(L, w, V + (size_t)it * L.len, &L.sc->inv_beta, &gate_done, s);
+    launch_orth_iteration<TX>(L, V, w, it0, s);
   }
 
   void restart(cudaStream_t s) {
@@ -287,8 +460,7 @@ struct Solve {
     launch_restart_small(L, s);
     launch_restart_rotate<TX>(L, V, U, s);
     launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, s);
-    const int P_gram = L.ls * (L.ls + 1) / 2 + L.ls;
-    launch_reduce(L, P_gram, RED_STORE, L.gram, 0, &gate_done, s);
+    launch_gram_reduce(L, s);
     launch_chol(L, s);
     launch_restart_apply<TX>(L, U, V, s);
   }
@@ -300,7 +472,7 @@ struct Solve {
     SMGPU_CUDA_TRY(cudaEventCreateWithFlags(&e_join, cudaEventDisableTiming));
     cudaGraph_t g;
     SMGPU_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    for (int it = kstart; it <= L.lm - 1; ++it) iteration(it, lock, e_fork, e_join, it == kstart);
+    for (int it = kstart; it <= L.lm - 1; ++it) iteration(it, lock, e_fork);
     SMGPU_CUDA_TRY(cudaEventRecord(e_join, s2));
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s, e_join, 0));
     restart(s);
@@ -388,9 +560,9 @@ struct Solve {
       launches += 2;
       for (int e = 0; e < nev; ++e) {
         double* r = R + (size_t)e * L.len;
-        launch_multidot<double>(L, r, 1, r, false, nullptr, P->st);
-        launch_reduce(L, 1, RED_INVNORM, L.h + e, 0, nullptr, P->st);
-        launch_scale_store<double>(L, r, r, L.h + e, nullptr, P->st);
+        launch_multidot<double>(L, r, 1, r, false, P->st);
+        launch_reduce(L, 1, RED_INVNORM, L.h + e, P->st);
+        launch_scale_store<double>(L, r, r, L.h + e, P->st);
         launch_from_padded(P->dt, r, tmp, P->st);
         launches += 4;
         SMGPU_CUDA_TRY(cudaMemcpyAsync(evecs_out + (size_t)e * mdim, tmp, sizeof(double) * mdim,
@@ -428,7 +600,6 @@ struct Solve {
     P->times[5] = now_s() - tw0;
     return status;
   }
-  long long launches_first = 0, launches_rest = 0;
 };
 
 }  // namespace
@@ -602,10 +773,10 @@ int smgpu_matvec(smgpu_problem* h, const double* v, double* w, int ncols, int ac
         SMGPU_CUDA_TRY(cudaMemcpyAsync(d_in, v + (size_t)c * mdim, sizeof(double) * mdim, cudaMemcpyHostToDevice, h->st));
         if (h->precision == SMGPU_FP64) {
           launch_to_padded<double>(h->dt, d_in, (double*)d_v, h->st);
-          h->hv<double>((const double*)d_v, d_w, nullptr, h->st);
+          h->hv((const double*)d_v, d_w, HvEpilogue<double>{}, h->st);
         } else {
           launch_to_padded<float>(h->dt, d_in, (float*)d_v, h->st);
-          h->hv<float>((const float*)d_v, d_w, nullptr, h->st);
+          h->hv((const float*)d_v, d_w, HvEpilogue<float>{}, h->st);
         }
         launch_from_padded(h->dt, d_w, d_out, h->st);
         SMGPU_CUDA_TRY(cudaMemcpyAsync(host.data(), d_out, sizeof(double) * mdim, cudaMemcpyDeviceToHost, h->st));
@@ -657,15 +828,15 @@ int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out) 
       if (h->precision == SMGPU_FP64)
         SMGPU_CUDA_TRY(cudaMemcpyAsync(d_v, d_start, sizeof(double) * len, cudaMemcpyDeviceToDevice, h->st));
       else
-        launch_scale_store_plain(d_start, (float*)d_v, len, h->st);
+        launch_convert(d_start, (float*)d_v, len, h->st);
       SMGPU_CUDA_TRY(cudaEventCreate(&a));
       SMGPU_CUDA_TRY(cudaEventCreate(&b));
       double total = 0.0;
       for (int r = 0; r < reps; ++r) {
         if (flush) SMGPU_CUDA_TRY(cudaMemsetAsync(flush, r & 0xff, 256u << 20, h->st));
         SMGPU_CUDA_TRY(cudaEventRecord(a, h->st));
-        if (h->precision == SMGPU_FP64) h->hv<double>((const double*)d_v, d_w, nullptr, h->st);
-        else h->hv<float>((const float*)d_v, d_w, nullptr, h->st);
+        if (h->precision == SMGPU_FP64) h->hv((const double*)d_v, d_w, HvEpilogue<double>{}, h->st);
+        else h->hv((const float*)d_v, d_w, HvEpilogue<float>{}, h->st);
         SMGPU_CUDA_TRY(cudaEventRecord(b, h->st));
         SMGPU_CUDA_TRY(cudaEventSynchronize(b));
         float ms = 0.f;
@@ -704,6 +875,8 @@ int smgpu_stats(const smgpu_problem* h, long long* s) {
   s[5] = (long long)h->tables.bytes;
   s[6] = (long long)T.len_pad;
   s[7] = (long long)T.links.size();
+  s[8] = h->cfg.nt;
+  s[9] = h->cfg.rows;
   return SMGPU_OK;
 }
 

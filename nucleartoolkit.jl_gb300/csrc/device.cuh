@@ -1,4 +1,5 @@
-// Device-side view of one shell-model problem (all pointers are device memory).
+// Device-side view of one shell-model problem (all pointers are device memory)
+// and the small structs shared by the kernels.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -6,6 +7,7 @@
 namespace smgpu {
 
 // Coefficient tables exist in FP64 (plain form) and FP32 (mixed form).
+// vtab holds, per ΔM, the table [2][nA][nB] = (V, −V).
 template <class TC>
 struct CoefTables {
   const TC* pp_val;
@@ -20,26 +22,65 @@ struct DevTables {
   const int* np;
   const int* nn;
   const int* stride;
-  const int64_t* off_pad;
-  const int* pstart;
-  const int* nstart;
-  const int64_t* tdims;
-  // per global proton row: owning block
-  const int* prow_block;
+  const int64_t* off_pad;  // nb+1
+  const int* pstart;       // nb+1
+  const int* nstart;       // nb+1
+  const int64_t* tdims;    // nb+1
   // pp / nn pull CSR
   const int* pp_ptr;
   const int* pp_col;
   const int* nn_ptr;
   const int* nn_col;
-  // pn links
-  const int4* link_a;      // x = source block, y = nB, z = unused, w = unused
-  const int64_t* link_v;   // V table offset
-  const int64_t* link_n;   // offset of the link's neutron row pointers
-  const int* ppn_ptr;
-  const uint32_t* ppn_src;
+  // pn links (output block b <- source block s)
+  const int4* link_a;     // x = source block, y = nB
+  const int64_t* link_v;  // offset of the link's signed V table
+  const int64_t* link_n;  // offset of the link's neutron row pointers
+  const uint32_t* ppn_src;   // proton pull entries: source row
   const uint32_t* ppn_meta;  // link<<16 | ia<<1 | sign
-  const int64_t* npn_ptr;
-  const uint32_t* npn_ent;   // n'<<14 | ib<<1 | sign
+};
+
+// Row-tile schedule of the H·v kernel.
+struct TileTables {
+  const int* task_b;       // block of each CTA
+  const int* task_p0;      // first row of each CTA
+  const int* link_begin;   // nb+1
+  const int64_t* rl_base;  // per block: offset into rl
+  const int* rl;           // per (row, link slot): first proton entry; slot nl = end
+  const int64_t* npn_ptr;  // neutron pull CSR row pointers (per link, nn[b]+1 each)
+  const uint32_t* npn_ent; // n'<<14 | (sign*nA*nB + ib)
+};
+
+struct HvConfig {
+  int nt;      // threads per CTA
+  int rows;    // rows per CTA
+  int ntasks;  // CTAs
+};
+
+// Scalars and flags of the Lanczos driver (device memory, one per solve).
+struct LanczosScalars {
+  double nrm_old;
+  double nrm;
+  double beta;
+  double inv_beta;
+  double pad[4];
+};
+struct LanczosFlags {
+  int done;       // converged (set by the eigenvalue test)
+  int elit;       // iteration (1-based) at which it stopped
+  int second;     // second CGS pass taken in the last iteration
+  int n_second;   // number of second passes taken (diagnostic)
+  int bad;        // a device-side guard fired
+  int exhausted;  // beta == 0: the Krylov space is exhausted
+  int exh_k;      // size of T when that happened
+  int pad;
+};
+
+template <class TV>
+struct HvEpilogue {
+  const LanczosFlags* fl;  // gate: skip when done/exhausted (null: always run)
+  const TV* vprev;         // w -= beta * vprev (null: no correction)
+  const double* beta;
+  double* alpha_part;      // per-CTA partial sums of v·Hv (null: none)
 };
 
 #define SMGPU_CUDA_TRY(expr)                                                      \
@@ -55,10 +96,12 @@ struct CudaError {
   int line;
 };
 
-// Launch helpers implemented in hv.cu / lanczos.cu
-void launch_hv_fp64(const DevTables& t, const double* ep, const double* en, const CoefTables<double>& c,
-                    const double* v, double* w, int nrows, const int* done, cudaStream_t st);
-void launch_hv_mixed(const DevTables& t, const double* ep, const double* en, const CoefTables<float>& c,
-                     const float* v, double* w, int nrows, const int* done, cudaStream_t st);
+const HvConfig* hv_candidates(int* count);
+void launch_hv_fp64(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
+                    const double* en, const CoefTables<double>& c, const double* v, double* w,
+                    const HvEpilogue<double>& epi, cudaStream_t st);
+void launch_hv_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
+                     const double* en, const CoefTables<float>& c, const float* v, double* w,
+                     const HvEpilogue<float>& epi, cudaStream_t st);
 
 }  // namespace smgpu

@@ -7,11 +7,23 @@
 // restart cycle can be captured in one CUDA graph: once the convergence test
 // sets `done`, the remaining kernels of the cycle return immediately.
 //
+// One iteration after the H·v (whose epilogue already produced per-CTA
+// partials of α and w = Hv − β v_prev):
+//   orth_dot   : α (summed by every CTA from the partials), w' = w − α v_k,
+//                partials of h_j = v_j·w' and of ||w'||²
+//   orth_axpy  : h (summed per CTA), w'' = w' − Σ h_j v_j, partials of ||w''||²
+//   orth_dot2 / orth_axpy2 : second classical Gram-Schmidt pass, taken only
+//                when ||w''||² < ||w'||²/2 (Daniel-Gragg-Kaufman-Stewart test)
+//   orth_scale : β = ||w||, T entries, v_{k+1} = w/β
+// Reductions are deterministic: a fixed grid writes per-CTA partial sums and
+// every consumer adds them in the same fixed order, so all CTAs agree bit for
+// bit on α, h, β and the second-pass decision.
+//
 // FP64 is used for all dot products, the orthogonalisation, the small
-// eigenproblems and the Ritz vectors; Krylov vectors are stored as TX
-// (double in the plain form, float in the mixed form).  Reductions are
-// deterministic: a fixed grid writes per-CTA partial sums that one CTA adds
-// in a fixed order.
+// eigenproblems and the Ritz vectors.  Krylov vectors are stored as TX
+// (double in the plain form, float in the mixed form); in the mixed form the
+// restart's basis rotation runs in FP32 with Kahan-compensated sums (its
+// result is stored in FP32) and is re-orthonormalised in FP64 (Cholesky QR).
 #include <cfloat>
 
 #include "lanczos.cuh"
@@ -21,31 +33,47 @@ namespace smgpu {
 namespace {
 constexpr int kNT = 256;  // threads of the streaming kernels
 
-enum Gate { GATE_NONE = 0, GATE_DONE = 1, GATE_SECOND = 2 };
-__device__ __forceinline__ bool gated(const LanczosFlags* fl, int gate) {
-  if (gate == GATE_NONE) return false;
-  if (fl->done || fl->exhausted) return true;
-  if (gate == GATE_SECOND && !fl->second) return true;
-  return false;
-}
+__device__ __forceinline__ bool stopped(const LanczosFlags* fl) { return fl->done || fl->exhausted; }
 
 __device__ __forceinline__ double warp_sum(double x) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
   return x;
 }
-// Deterministic block sum (result valid in thread 0).
+
+// Deterministic block sum, result returned to every thread.
 template <int NT>
-__device__ __forceinline__ double block_sum(double x, double* red) {
+__device__ __forceinline__ double block_sum_all(double x, double* red) {
   x = warp_sum(x);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[wid] = x;
   __syncthreads();
   double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int k = 0; k < NT / 32; ++k) s += red[k];
+#pragma unroll
+  for (int k = 0; k < NT / 32; ++k) s += red[k];
   return s;
+}
+
+// Sum of n partials in a fixed order (every thread gets the same value).
+template <int NT>
+__device__ __forceinline__ double sum_partials(const double* __restrict__ p, int n, double* red) {
+  double x = 0.0;
+  for (int i = threadIdx.x; i < n; i += NT) x += p[i];
+  return block_sum_all<NT>(x, red);
+}
+
+// m sums of G partials each, one warp per sum; results into smem out[0..m).
+template <int NT>
+__device__ __forceinline__ void sum_partials_many(const double* __restrict__ p, int G, int m, double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < m; j += NT / 32) {
+    double x = 0.0;
+    for (int g = lane; g < G; g += 32) x += p[(int64_t)j * G + g];
+    x = warp_sum(x);
+    if (lane == 0) out[j] = x;
+  }
+  __syncthreads();
 }
 
 __device__ __forceinline__ void chunk_of(int64_t len, int G, int64_t& b, int64_t& e) {
@@ -66,6 +94,19 @@ __device__ __forceinline__ int find_block(const int64_t* off, int nb, int64_t i)
   }
   return lo;
 }
+
+// Kahan-compensated FP32 sum.
+struct KahanF {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float y = __fsub_rn(x, c);
+    float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ float get() const { return __fsub_rn(s, c); }
+};
 
 // Seeded start vector (replaces Random.seed!(1234); randn(mdim),
 // shellmodel_main.jl:939-948): v[M] = u0+u1+u2+u3-2 with
@@ -95,6 +136,11 @@ __global__ void k_start_vector(DevTables t, uint64_t seed, double* __restrict__ 
   }
 }
 
+__global__ void k_convert(const double* __restrict__ a, float* __restrict__ b, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
 template <class TX>
 __global__ void k_to_padded(DevTables t, const double* __restrict__ src, TX* __restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
@@ -121,9 +167,7 @@ __global__ void k_from_padded(DevTables t, const double* __restrict__ src, doubl
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int64_t ld, int m,
                                                   const double* __restrict__ y, int64_t len, int self,
-                                                  double* __restrict__ partials, int G,
-                                                  const LanczosFlags* __restrict__ fl, int gate) {
-  if (gated(fl, gate)) return;
+                                                  double* __restrict__ partials, int G) {
   __shared__ double red[kNT / 32];
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
@@ -144,90 +188,184 @@ __global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int6
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       if (j0 + q >= mt) break;
-      double s = block_sum<kNT>(acc[q], red);
+      double s = block_sum_all<kNT>(acc[q], red);
       if (threadIdx.x == 0) partials[(int64_t)(j0 + q) * G + blockIdx.x] = s;
     }
   }
 }
 
-// y[i] -= Σ_j h[j]·X_j[i];  partials[cta] = Σ_{chunk} y_new[i]².
-template <class TX>
-__global__ void __launch_bounds__(kNT) k_multiaxpy(const TX* __restrict__ X, int64_t ld, int m,
-                                                   const double* __restrict__ h, double* __restrict__ y,
-                                                   int64_t len, double* __restrict__ partials, int G,
-                                                   const LanczosFlags* __restrict__ fl, int gate) {
-  if (gated(fl, gate)) return;
-  extern __shared__ double sh[];  // m coefficients
-  __shared__ double red[kNT / 32];
-  for (int j = threadIdx.x; j < m; j += kNT) sh[j] = h[j];
-  __syncthreads();
-  int64_t cb, ce;
-  chunk_of(len, G, cb, ce);
-  double nrm = 0.0;
-  for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
-    double t = y[i];
-    for (int j = 0; j < m; ++j) t = fma(-sh[j], (double)X[(int64_t)j * ld + i], t);
-    y[i] = t;
-    nrm = fma(t, t, nrm);
-  }
-  double s = block_sum<kNT>(nrm, red);
-  if (threadIdx.x == 0) partials[blockIdx.x] = s;
-}
-
+// out[j] = f(Σ_g partials[j*G+g]), one warp per j.
 __global__ void __launch_bounds__(kNT) k_reduce(const double* __restrict__ partials, int G, int m, int mode,
-                                                double* __restrict__ out, int it, int lm, double* __restrict__ T,
-                                                LanczosScalars* sc, LanczosFlags* fl, int gate) {
-  if (gated(fl, gate)) return;
-  __shared__ double red[kNT / 32];
-  const int mt = (mode == RED_H) ? m + 1 : m;
-  for (int j = 0; j < mt; ++j) {
-    double x = 0.0;
-    for (int g = threadIdx.x; g < G; g += kNT) x += partials[(int64_t)j * G + g];
-    double s = block_sum<kNT>(x, red);
-    if (threadIdx.x == 0) {
-      switch (mode) {
-        case RED_STORE: out[j] = s; break;
-        case RED_ALPHA: T[(int64_t)it * lm + it] = s; break;
-        case RED_H:
-          if (j < m) out[j] = s;
-          else sc->nrm_old = s;
-          break;
-        case RED_NRM_CHECK:
-          sc->nrm = s;
-          fl->second = (s < 0.5 * sc->nrm_old) ? 1 : 0;
-          if (fl->second) fl->n_second += 1;
-          break;
-        case RED_NRM: sc->nrm = s; break;
-        case RED_INVNORM: out[j] = 1.0 / sqrt(s); break;
-      }
-    }
+                                                double* __restrict__ out) {
+  __shared__ double res[1024];
+  for (int j0 = 0; j0 < m; j0 += 1024) {
+    const int mm = min(1024, m - j0);
+    sum_partials_many<kNT>(partials + (int64_t)j0 * G, G, mm, res);
+    for (int j = threadIdx.x; j < mm; j += kNT) out[j0 + j] = (mode == RED_INVNORM) ? 1.0 / sqrt(res[j]) : res[j];
+    __syncthreads();
   }
-}
-
-// β = ||w||, T[it+1,it] = T[it,it+1] = β (it 0-based).  A zero β means the
-// Krylov space is exhausted: stop with the current T (elit = it+1).
-__global__ void k_beta(double* T, int lm, int it, LanczosScalars* sc, LanczosFlags* fl) {
-  if (fl->done || fl->exhausted) return;
-  double beta = sqrt(sc->nrm);
-  sc->beta = beta;
-  if (!(beta > 0.0) || !(beta < INFINITY)) {
-    fl->exh_k = it + 1;
-    fl->exhausted = 1;
-    return;
-  }
-  sc->inv_beta = 1.0 / beta;
-  T[(int64_t)it * lm + it + 1] = beta;
-  T[(int64_t)(it + 1) * lm + it] = beta;
 }
 
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_scale_store(const double* __restrict__ w, TX* __restrict__ out,
-                                                     const double* __restrict__ scale, int64_t len,
-                                                     const LanczosFlags* __restrict__ fl, int gate) {
-  if (gated(fl, gate)) return;
+                                                     const double* __restrict__ scale, int64_t len) {
   const double s = *scale;
   for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
     out[i] = (TX)(w[i] * s);
+}
+
+// ------------------------------------------------------------ orthogonalisation
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int64_t ld, int it0, double* w,
+                                                  const double* __restrict__ alpha_part, int nalpha,
+                                                  double* __restrict__ pdot, int G, const LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  __shared__ double red[kNT / 32];
+  const double alpha = sum_partials<kNT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
+  const TX* __restrict__ vk = V + (int64_t)it0 * ld;
+  const int m = it0 + 1;
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  for (int j0 = 0; j0 <= m; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
+      double wv;
+      if (j0 == 0) {
+        wv = fma(-alpha, (double)vk[i], w[i]);
+        w[i] = wv;
+      } else {
+        wv = w[i];
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = j0 + q;
+        if (j < m) acc[q] = fma((double)V[(int64_t)j * ld + i], wv, acc[q]);
+        else if (j == m) acc[q] = fma(wv, wv, acc[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q > m) break;
+      double s = block_sum_all<kNT>(acc[q], red);
+      if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+    }
+  }
+}
+
+// Second-pass decision, identical in every CTA: ||w''||² < ||w'||² / 2.
+__device__ __forceinline__ bool need_second(const double* pdot, const double* pn1, int m, int G, double* red) {
+  const double n0 = sum_partials<kNT>(pdot + (int64_t)m * G, G, red);
+  const double n1 = sum_partials<kNT>(pn1, G, red);
+  return n1 < 0.5 * n0;
+}
+
+// w -= Σ_j h_j V_j with h_j = Σ_g ph[j*G+g];  pout[cta] = ||w_chunk||².
+template <class TX>
+__device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t ld, int m, double* w,
+                                              const double* __restrict__ ph, double* __restrict__ pout, int G,
+                                              double* hs, double* red) {
+  sum_partials_many<kNT>(ph, G, m, hs);
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  double nrm = 0.0;
+  for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
+    double t = w[i];
+    for (int j = 0; j < m; ++j) t = fma(-hs[j], (double)V[(int64_t)j * ld + i], t);
+    w[i] = t;
+    nrm = fma(t, t, nrm);
+  }
+  double s = block_sum_all<kNT>(nrm, red);
+  if (threadIdx.x == 0) pout[blockIdx.x] = s;
+}
+
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_orth_axpy(const TX* __restrict__ V, int64_t ld, int it0, double* w,
+                                                   const double* __restrict__ pdot, double* __restrict__ pn1, int G,
+                                                   const LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  extern __shared__ double hs[];
+  __shared__ double red[kNT / 32];
+  orth_subtract<TX>(V, ld, it0 + 1, w, pdot, pn1, G, hs, red);
+}
+
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int64_t ld, int it0,
+                                                   const double* __restrict__ w, const double* __restrict__ pdot,
+                                                   const double* __restrict__ pn1, double* __restrict__ pdot2,
+                                                   int G, const LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  if (!need_second(pdot, pn1, m, G, red)) return;
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  for (int j0 = 0; j0 < m; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
+      const double wv = w[i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (j0 + q < m) acc[q] = fma((double)V[(int64_t)(j0 + q) * ld + i], wv, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q >= m) break;
+      double s = block_sum_all<kNT>(acc[q], red);
+      if (threadIdx.x == 0) pdot2[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+    }
+  }
+}
+
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_orth_axpy2(const TX* __restrict__ V, int64_t ld, int it0, double* w,
+                                                    const double* __restrict__ pdot,
+                                                    const double* __restrict__ pn1,
+                                                    const double* __restrict__ pdot2, double* __restrict__ pn2,
+                                                    int G, const LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  extern __shared__ double hs[];
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  if (!need_second(pdot, pn1, m, G, red)) return;
+  orth_subtract<TX>(V, ld, m, w, pdot2, pn2, G, hs, red);
+}
+
+// β = ||w||, T[it0+1,it0] = T[it0,it0+1] = β, v_{it0+1} = w/β.  A zero β means
+// the Krylov space is exhausted: stop with the current T.
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w, TX* __restrict__ vnext,
+                                                    const double* __restrict__ pdot,
+                                                    const double* __restrict__ pn1,
+                                                    const double* __restrict__ pn2, int G, int it0, double* T,
+                                                    int lm, int64_t len, LanczosScalars* sc, LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  const bool second = need_second(pdot, pn1, m, G, red);
+  const double nrm = sum_partials<kNT>(second ? pn2 : pn1, G, red);
+  const double beta = sqrt(nrm);
+  const bool ok = (beta > 0.0) && (beta < INFINITY);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (ok) {
+      T[(int64_t)it0 * lm + it0 + 1] = beta;
+      T[(int64_t)(it0 + 1) * lm + it0] = beta;
+      sc->beta = beta;
+      sc->inv_beta = 1.0 / beta;
+      fl->second = second ? 1 : 0;
+      if (second) fl->n_second += 1;
+    } else {
+      fl->exh_k = it0 + 1;
+      fl->exhausted = 1;
+    }
+  }
+  if (!ok) return;
+  const double inv = 1.0 / beta;
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
+    vnext[i] = (TX)(w[i] * inv);
 }
 
 // ---------------------------------------------------------------------------
@@ -235,7 +373,10 @@ __global__ void __launch_bounds__(kNT) k_scale_store(const double* __restrict__ 
 // (diagonalize_T!, lanczos_methods.jl:250-258).  After a thick restart T is
 // an arrowhead (rows 0..lock-1 diagonal, coupled to row `lock`) followed by a
 // tridiagonal tail; the LDLᵀ inertia of T - σI is evaluated in O(k) for that
-// shape.  One warp bisects one eigenvalue with 32 trial shifts per step.
+// shape.  A group of kLPE lanes bisects one eigenvalue with kLPE trial shifts
+// per step (FP64 division throughput, not latency, bounds this kernel).
+constexpr int kLPE = 4;
+
 __device__ int sturm_count(const double* a, const double* c2, const double* b2, int lock, int k, double sigma,
                            double pivmin) {
   int cnt = 0;
@@ -257,8 +398,9 @@ __device__ int sturm_count(const double* a, const double* c2, const double* b2, 
   return cnt;
 }
 
-__global__ void k_sturm(const double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
-                        double tol, int64_t mdim, LanczosFlags* fl) {
+__global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
+                        double tol, int64_t mdim, const double* __restrict__ alpha_part, int nalpha,
+                        LanczosFlags* fl) {
   if (fl->done) return;
   if (fl->exhausted && k > fl->exh_k) {
     // the Krylov space ended at exh_k; T_k was never completed
@@ -271,7 +413,22 @@ __global__ void k_sturm(const double* __restrict__ T, int lm, int k, int lock, i
   double* b2 = c2 + lm;      // k-1
   double* lam = b2 + lm;     // num_ev
   __shared__ double s_lo, s_hi, s_piv;
+  __shared__ double red[32];
   const int tid = threadIdx.x;
+  // α of this iteration from the H·v epilogue partials
+  {
+    double x = 0.0;
+    for (int i = tid; i < nalpha; i += blockDim.x) x += alpha_part[(int64_t)(k - 1) * nalpha + i];
+    x = warp_sum(x);
+    if ((tid & 31) == 0) red[tid >> 5] = x;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int wdx = 0; wdx < (int)(blockDim.x >> 5); ++wdx) s += red[wdx];
+      T[(int64_t)(k - 1) * lm + (k - 1)] = s;
+    }
+    __syncthreads();
+  }
   for (int i = tid; i < k; i += blockDim.x) {
     a[i] = T[(int64_t)i * lm + i];
     if (i < lock) { double x = T[(int64_t)i * lm + lock]; c2[i] = x * x; }
@@ -301,22 +458,26 @@ __global__ void k_sturm(const double* __restrict__ T, int lm, int k, int lock, i
   }
   __syncthreads();
   const int n = min(num_ev, k);
-  const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  for (int e = wid; e < n; e += nw) {
+  const int lane = tid & 31;
+  const int grp = tid / kLPE, sub = tid % kLPE, ngrp = blockDim.x / kLPE;
+  const unsigned gmask = ((1u << kLPE) - 1u) << (lane & ~(kLPE - 1));
+  for (int e0 = 0; e0 < n; e0 += ngrp) {
+    const int e = e0 + grp;
+    const bool live = e < n;
     double lo = s_lo, hi = s_hi;
-    for (int step = 0; step < 100; ++step) {
-      double sigma = lo + (hi - lo) * (double)(lane + 1) * (1.0 / 33.0);
-      int cnt = sturm_count(a, c2, b2, lock, k, sigma, s_piv);
-      unsigned le = __ballot_sync(0xffffffffu, cnt <= e);
-      unsigned ge = __ballot_sync(0xffffffffu, cnt >= e + 1);
-      double nlo = lo, nhi = hi;
-      if (le) nlo = __shfl_sync(0xffffffffu, sigma, 31 - __clz(le));
-      if (ge) nhi = __shfl_sync(0xffffffffu, sigma, __ffs(ge) - 1);
-      lo = nlo;
-      hi = nhi;
-      if (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 1e-300) break;
+    for (int step = 0; step < 200; ++step) {
+      const double sigma = lo + (hi - lo) * (double)(sub + 1) * (1.0 / (kLPE + 1));
+      const int cnt = live ? sturm_count(a, c2, b2, lock, k, sigma, s_piv) : 0;
+      const unsigned le = __ballot_sync(0xffffffffu, cnt <= e) & gmask;
+      const unsigned ge = __ballot_sync(0xffffffffu, cnt >= e + 1) & gmask;
+      const double s_le = __shfl_sync(0xffffffffu, sigma, le ? 31 - __clz(le) : lane);
+      const double s_ge = __shfl_sync(0xffffffffu, sigma, ge ? __ffs(ge) - 1 : lane);
+      if (le) lo = s_le;
+      if (ge) hi = s_ge;
+      const bool fin = !live || (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 1e-300);
+      if (__all_sync(0xffffffffu, fin)) break;
     }
-    if (lane == 0) lam[e] = 0.5 * (lo + hi);
+    if (live && sub == 0) lam[e] = 0.5 * (lo + hi);
   }
   __syncthreads();
   if (tid == 0) {
@@ -340,7 +501,7 @@ __global__ void k_sturm(const double* __restrict__ T, int lm, int k, int lock, i
 template <int NT>
 __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int ldt, int n, double* A, double* Z,
                                                double* evals, const LanczosFlags* fl, int gate) {
-  if (gate && (fl->done || fl->exhausted)) return;
+  if (gate && stopped(fl)) return;
   __shared__ double red[NT / 32];
   __shared__ int s_stop;
   extern __shared__ double shj[];
@@ -360,18 +521,14 @@ __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int
   __syncthreads();
   double fro = 0.0;
   for (int idx = tid; idx < n * n; idx += NT) fro += A[idx] * A[idx];
-  fro = block_sum<NT>(fro, red);
-  if (tid == 0) red[0] = fro;
-  __syncthreads();
-  fro = red[0];
-  __syncthreads();
+  fro = block_sum_all<NT>(fro, red);
   for (int sweep = 0; sweep < 64; ++sweep) {
     double off = 0.0;
     for (int idx = tid; idx < n * n; idx += NT) {
       int i = idx % n, j = idx / n;
       if (i < j) off += A[idx] * A[idx];
     }
-    off = block_sum<NT>(off, red);
+    off = block_sum_all<NT>(off, red);
     if (tid == 0) s_stop = (off <= 1e-34 * fro || off == 0.0) ? 1 : 0;
     __syncthreads();
     if (s_stop) break;
@@ -448,7 +605,7 @@ __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int
 // ThickRestart's small part (lanczos_methods.jl:261-271): new arrowhead T.
 __global__ void k_restart_small(double* T, int lm, int ls, const double* evals, const double* vecs,
                                 const LanczosFlags* fl) {
-  if (fl->done || fl->exhausted) return;
+  if (stopped(fl)) return;
   const int m = lm - 1;
   __shared__ double beta;
   if (threadIdx.x == 0) beta = T[(int64_t)(lm - 1) * lm + (lm - 2)];
@@ -463,40 +620,54 @@ __global__ void k_restart_small(double* T, int lm, int ls, const double* evals, 
   }
 }
 
-// U_k = Σ_{j<m} Y[j,k] V_j  (k < ls), FP64 accumulation.
+// U_k = Σ_{j<m} Y[j,k] V_j  (k < ls).  FP64 for the plain form; FP32 with
+// Kahan sums for the mixed form (the result is stored in FP32).
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V, TX* __restrict__ U,
                                                         const double* __restrict__ Y, int m, int ls, int64_t len,
                                                         const LanczosFlags* __restrict__ fl) {
-  if (fl->done || fl->exhausted) return;
-  extern __shared__ double yS[];  // m x ls
-  for (int idx = threadIdx.x; idx < m * ls; idx += kNT) yS[idx] = Y[(int64_t)(idx / m) * m + (idx % m)];
-  __syncthreads();
+  if (stopped(fl)) return;
+  // Y (m x ls, column-major) is small and read through L1
   for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
     for (int k0 = 0; k0 < ls; k0 += 8) {
-      double acc[8];
+      if constexpr (sizeof(TX) == 4) {
+        KahanF acc[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-      for (int j = 0; j < m; ++j) {
-        const double x = (double)V[(int64_t)j * len + i];
+        for (int q = 0; q < 8; ++q) acc[q].init();
+        for (int j = 0; j < m; ++j) {
+          const float x = (float)V[(int64_t)j * len + i];
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (k0 + q < ls) acc[q].add(__fmul_rn((float)__ldg(Y + (int64_t)(k0 + q) * m + j), x));
+        }
 #pragma unroll
         for (int q = 0; q < 8; ++q)
-          if (k0 + q < ls) acc[q] = fma(yS[(k0 + q) * m + j], x, acc[q]);
-      }
+          if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q].get();
+      } else {
+        double acc[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q];
+        for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+        for (int j = 0; j < m; ++j) {
+          const double x = (double)V[(int64_t)j * len + i];
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (k0 + q < ls) acc[q] = fma(__ldg(Y + (int64_t)(k0 + q) * m + j), x, acc[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q];
+      }
     }
   }
 }
 
-// Gram matrix of U (upper triangle, packed row by row) and U_k·v_last.
+// Gram matrix of U (upper triangle, packed row by row) and U_k·v_last, FP64.
 // Entry order: pairs (k,l) with k <= l in row-major order, then g_k.
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX* __restrict__ vl, int ls,
                                               int64_t len, double* __restrict__ partials, int G,
                                               const LanczosFlags* __restrict__ fl) {
-  if (fl->done || fl->exhausted) return;
+  if (stopped(fl)) return;
   constexpr int TILE = 64;
   extern __shared__ double tile[];  // (ls+1) x TILE
   const int P = ls * (ls + 1) / 2 + ls;
@@ -537,9 +708,21 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
   }
 }
 
+__global__ void __launch_bounds__(kNT) k_gram_reduce(const double* __restrict__ partials, int G, int P,
+                                                     double* __restrict__ out, const LanczosFlags* fl) {
+  if (stopped(fl)) return;
+  __shared__ double res[1024];
+  for (int j0 = 0; j0 < P; j0 += 1024) {
+    const int mm = min(1024, P - j0);
+    sum_partials_many<kNT>(partials + (int64_t)j0 * G, G, mm, res);
+    for (int j = threadIdx.x; j < mm; j += kNT) out[j0 + j] = res[j];
+    __syncthreads();
+  }
+}
+
 // Cholesky G = RᵀR, X = R⁻¹ (upper), c = Xᵀ g.  Single thread (ls is small).
 __global__ void k_chol(const double* __restrict__ gram, int ls, double* X, double* cvec, LanczosFlags* fl) {
-  if (fl->done || fl->exhausted || threadIdx.x != 0) return;
+  if (stopped(fl) || threadIdx.x != 0) return;
   extern __shared__ double R[];  // ls x ls, column-major
   auto G = [&](int k, int l) {  // k <= l
     int off = 0;
@@ -579,7 +762,7 @@ __global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U,
                                                        const double* __restrict__ X, const double* __restrict__ cvec,
                                                        int ls, int lm, int64_t len,
                                                        const LanczosFlags* __restrict__ fl) {
-  if (fl->done || fl->exhausted) return;
+  if (stopped(fl)) return;
   extern __shared__ double xs[];  // ls*ls + ls
   for (int idx = threadIdx.x; idx < ls * ls; idx += kNT) xs[idx] = X[idx];
   for (int idx = threadIdx.x; idx < ls; idx += kNT) xs[ls * ls + idx] = cvec[idx];
@@ -618,11 +801,7 @@ inline int grid_for(int64_t len) {
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
-__global__ void k_convert(const double* __restrict__ a, float* __restrict__ b, int64_t len) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
-}
-void launch_scale_store_plain(const double* a, float* b, int64_t len, cudaStream_t st) {
+void launch_convert(const double* a, float* b, int64_t len, cudaStream_t st) {
   k_convert<<<grid_for(len), kNT, 0, st>>>(a, b, len);
 }
 void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st) {
@@ -636,34 +815,34 @@ void launch_from_padded(const DevTables& t, const double* src, double* dst, cuda
   k_from_padded<<<grid_for(t.len_pad), kNT, 0, st>>>(t, src, dst);
 }
 template <class TX>
-void launch_multidot(const LanczosDev& L, const TX* X, int m, const double* y, bool self, const int* gate,
-                     cudaStream_t st) {
-  int g = gate ? *gate : GATE_NONE;
-  k_multidot<TX><<<L.G, kNT, 0, st>>>(X, L.len, m, y, L.len, self ? 1 : 0, L.partials, L.G, L.fl, g);
+void launch_multidot(const LanczosDev& L, const TX* X, int m, const double* y, bool self, cudaStream_t st) {
+  k_multidot<TX><<<L.G, kNT, 0, st>>>(X, L.len, m, y, L.len, self ? 1 : 0, L.partials, L.G);
 }
-void launch_reduce(const LanczosDev& L, int m, ReduceMode mode, double* out, int it, const int* gate,
-                   cudaStream_t st) {
-  int g = gate ? *gate : GATE_NONE;
-  k_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, m, (int)mode, out, it, L.lm, L.T, L.sc, L.fl, g);
+void launch_reduce(const LanczosDev& L, int m, ReduceMode mode, double* out, cudaStream_t st) {
+  k_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, m, (int)mode, out);
 }
 template <class TX>
-void launch_multiaxpy(const LanczosDev& L, const TX* X, int m, double* y, const int* gate, cudaStream_t st) {
-  int g = gate ? *gate : GATE_NONE;
-  k_multiaxpy<TX><<<L.G, kNT, sizeof(double) * (m > 0 ? m : 1), st>>>(X, L.len, m, L.h, y, L.len, L.partials, L.G,
-                                                                        L.fl, g);
+void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const double* scale, cudaStream_t st) {
+  k_scale_store<TX><<<grid_for(L.len), kNT, 0, st>>>(w, out, scale, L.len);
 }
-void launch_beta(const LanczosDev& L, int it, cudaStream_t st) { k_beta<<<1, 1, 0, st>>>(L.T, L.lm, it, L.sc, L.fl); }
 template <class TX>
-void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const double* scale, const int* gate,
-                        cudaStream_t st) {
-  int g = gate ? *gate : GATE_NONE;
-  k_scale_store<TX><<<grid_for(L.len), kNT, 0, st>>>(w, out, scale, L.len, L.fl, g);
+void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaStream_t st) {
+  const int m = it0 + 1;
+  const size_t hsh = sizeof(double) * (size_t)m;
+  k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl);
+  k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, L.fl);
+  k_orth_dot2<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.G, L.fl);
+  k_orth_axpy2<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.pn2, L.G, L.fl);
+  k_orth_scale<TX><<<L.G, kNT, 0, st>>>(w, V + (int64_t)(it0 + 1) * L.len, L.pdot, L.pn1, L.pn2, L.G, it0, L.T,
+                                        L.lm, L.len, L.sc, L.fl);
 }
 void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
-  int warps = L.num_ev < 32 ? L.num_ev : 32;
-  if (warps < 1) warps = 1;
+  int threads = ((L.num_ev * kLPE + 31) / 32) * 32;
+  if (threads > 1024) threads = 1024;
+  if (threads < 32) threads = 32;
   size_t shm = sizeof(double) * (3 * (size_t)L.lm + L.num_ev);
-  k_sturm<<<1, 32 * warps, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.fl);
+  k_sturm<<<1, threads, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.alpha_part, L.nalpha,
+                                   L.fl);
 }
 void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st) {
   int N = n + (n & 1);
@@ -676,11 +855,15 @@ void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st) {
   int m = L.lm - 1;
-  k_restart_rotate<TX><<<grid_for(L.len), kNT, sizeof(double) * m * L.ls, st>>>(V, U, L.jacA, m, L.ls, L.len, L.fl);
+  k_restart_rotate<TX><<<grid_for(L.len), kNT, 0, st>>>(V, U, L.jacA, m, L.ls, L.len, L.fl);
 }
 template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
   k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 64, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
+}
+void launch_gram_reduce(const LanczosDev& L, cudaStream_t st) {
+  const int P = L.ls * (L.ls + 1) / 2 + L.ls;
+  k_gram_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, P, L.gram, L.fl);
 }
 void launch_chol(const LanczosDev& L, cudaStream_t st) {
   k_chol<<<1, 32, sizeof(double) * L.ls * L.ls, st>>>(L.gram, L.ls, L.X, L.cvec, L.fl);
@@ -697,11 +880,9 @@ void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R,
 
 #define SMGPU_INST(TX)                                                                                       \
   template void launch_to_padded<TX>(const DevTables&, const double*, TX*, cudaStream_t);                    \
-  template void launch_multidot<TX>(const LanczosDev&, const TX*, int, const double*, bool, const int*,      \
-                                    cudaStream_t);                                                           \
-  template void launch_multiaxpy<TX>(const LanczosDev&, const TX*, int, double*, const int*, cudaStream_t);  \
-  template void launch_scale_store<TX>(const LanczosDev&, const double*, TX*, const double*, const int*,     \
-                                       cudaStream_t);                                                        \
+  template void launch_multidot<TX>(const LanczosDev&, const TX*, int, const double*, bool, cudaStream_t);   \
+  template void launch_scale_store<TX>(const LanczosDev&, const double*, TX*, const double*, cudaStream_t);   \
+  template void launch_orth_iteration<TX>(const LanczosDev&, TX*, double*, int, cudaStream_t);               \
   template void launch_restart_rotate<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                  \
   template void launch_gram<TX>(const LanczosDev&, const TX*, const TX*, cudaStream_t);                      \
   template void launch_restart_apply<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                   \
