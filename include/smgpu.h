@@ -138,10 +138,11 @@ int smgpu_timings(const smgpu_problem* h, double* times_out);
  * ms_out: mean milliseconds per launch. */
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
-/* Structural statistics of the factorised H (10 entries): [updates per H·v
+/* Structural statistics of the factorised H (11 entries): [updates per H·v
  * (multiply-adds), pn proton pull entries, pn neutron entries, pp entries,
  * nn entries, table bytes on the device, padded vector length, number of
- * links, H·v threads per CTA, H·v rows per CTA (the autotuned shape)]. */
+ * links, H·v threads per CTA, H·v rows per CTA, H·v minimum CTAs per SM
+ * (the autotuned launch shape)]. */
 int smgpu_stats(const smgpu_problem* h, long long* stats_out);
 
 #ifdef __cplusplus

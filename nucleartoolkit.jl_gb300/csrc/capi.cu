@@ -77,7 +77,7 @@ std::vector<float> to_f32(const std::vector<T>& v) {
 // ---- autotuner cache: shape class -> (threads, rows)
 typedef std::tuple<int, int, int, int, int, int> ShapeKey;  // precision, Lp, Ln, vp, vn, mtot2
 std::mutex g_tune_mu;
-std::map<ShapeKey, std::pair<int, int>> g_tune;
+std::map<ShapeKey, std::tuple<int, int, int>> g_tune;  // -> threads, rows, min CTAs per SM
 bool g_tune_file_loaded = false;
 
 void tune_file_load() {
@@ -87,9 +87,10 @@ void tune_file_load() {
   if (!path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  int a[8];
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7]) == 8)
-    g_tune[ShapeKey{a[0], a[1], a[2], a[3], a[4], a[5]}] = {a[6], a[7]};
+  int a[9];
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7],
+                     &a[8]) == 9)
+    g_tune[ShapeKey{a[0], a[1], a[2], a[3], a[4], a[5]}] = std::make_tuple(a[6], a[7], a[8]);
   std::fclose(f);
 }
 void tune_file_store() {
@@ -98,9 +99,9 @@ void tune_file_store() {
   FILE* f = std::fopen(path, "w");
   if (!f) return;
   for (auto& kv : g_tune)
-    std::fprintf(f, "%d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first), std::get<2>(kv.first),
-                 std::get<3>(kv.first), std::get<4>(kv.first), std::get<5>(kv.first), kv.second.first,
-                 kv.second.second);
+    std::fprintf(f, "%d %d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+                 std::get<2>(kv.first), std::get<3>(kv.first), std::get<4>(kv.first), std::get<5>(kv.first),
+                 std::get<0>(kv.second), std::get<1>(kv.second), std::get<2>(kv.second));
   std::fclose(f);
 }
 }  // namespace
@@ -116,7 +117,7 @@ struct smgpu_problem {
   CoefTables<float> c32{};
   const double* d_ep = nullptr;
   const double* d_en = nullptr;
-  HvConfig cfg{128, 4, 0};
+  HvConfig cfg{128, 4, 0, 1};
   std::map<int, std::pair<const int*, const int*>> task_arrays;  // rows -> (task_b, task_p0)
   std::map<int, int> task_count;
   cudaStream_t st = nullptr, st2 = nullptr;
@@ -151,10 +152,11 @@ struct smgpu_problem {
     task_arrays[R] = {tables.upload(tb), tables.upload(tp)};
     task_count[R] = (int)tb.size();
   }
-  void set_config(int nt, int R) {
+  void set_config(int nt, int R, int minb) {
     ensure_tasks(R);
     cfg.nt = nt;
     cfg.rows = R;
+    cfg.minb = minb;
     cfg.ntasks = task_count[R];
     tt.task_b = task_arrays[R].first;
     tt.task_p0 = task_arrays[R].second;
@@ -243,7 +245,7 @@ struct smgpu_problem {
       c32.nn_val = tables.upload(to_f32(T.nn_val));
       c32.vtab = tables.upload(to_f32(vt2));
     }
-    set_config(128, 4);
+    set_config(128, 4, 1);
   }
 
   void hv(const double* v, double* w, const HvEpilogue<double>& epi, cudaStream_t s) {
@@ -261,7 +263,7 @@ struct smgpu_problem {
       tune_file_load();
       auto it = g_tune.find(key);
       if (it != g_tune.end()) {
-        set_config(it->second.first, it->second.second);
+        set_config(std::get<0>(it->second), std::get<1>(it->second), std::get<2>(it->second));
         return;
       }
     }
@@ -285,7 +287,7 @@ struct smgpu_problem {
       int best = -1;
       float best_ms = 1e30f;
       for (int c = 0; c < nc; ++c) {
-        set_config(cand[c].nt, cand[c].rows);
+        set_config(cand[c].nt, cand[c].rows, cand[c].minb);
         float total = 0.f;
         for (int rep = 0; rep < 3; ++rep) {
           SMGPU_CUDA_TRY(cudaEventRecord(a, st));
@@ -304,9 +306,9 @@ struct smgpu_problem {
           best = c;
         }
       }
-      set_config(cand[best].nt, cand[best].rows);
+      set_config(cand[best].nt, cand[best].rows, cand[best].minb);
       std::lock_guard<std::mutex> lk(g_tune_mu);
-      g_tune[key] = {cfg.nt, cfg.rows};
+      g_tune[key] = std::make_tuple(cfg.nt, cfg.rows, cfg.minb);
       tune_file_store();
     } catch (...) {
       if (a) cudaEventDestroy(a);
@@ -412,6 +414,7 @@ struct Solve {
     L.jacA = A.alloc<double>((size_t)lm * lm);
     L.jacZ = A.alloc<double>((size_t)lm * lm);
     L.evals = A.alloc<double>(lm);
+    L.Yf = A.alloc<float>((size_t)lm * ls);
     L.gram = A.alloc<double>(P_gram);
     L.X = A.alloc<double>((size_t)ls * ls);
     L.cvec = A.alloc<double>(ls);
@@ -877,6 +880,7 @@ int smgpu_stats(const smgpu_problem* h, long long* s) {
   s[7] = (long long)T.links.size();
   s[8] = h->cfg.nt;
   s[9] = h->cfg.rows;
+  s[10] = h->cfg.minb;
   return SMGPU_OK;
 }
 

@@ -54,6 +54,7 @@ struct HvConfig {
   int nt;      // threads per CTA
   int rows;    // rows per CTA
   int ntasks;  // CTAs
+  int minb;    // minimum resident CTAs per SM requested from the compiler (caps registers)
 };
 
 // Scalars and flags of the Lanczos driver (device memory, one per solve).
@@ -83,7 +84,28 @@ struct HvEpilogue {
   double* alpha_part;      // per-CTA partial sums of v·Hv (null: none)
 };
 
-#define SMGPU_CUDA_TRY(expr)                                                      \
+#ifdef __CUDACC__
+// Exact float -> double widening with integer instructions only (sign,
+// exponent rebias by 1023-127, mantissa shift).  On this GPU the conversion
+// instruction shares the FP64 pipe with DFMA, which the FP64 dot products
+// already saturate; this form runs on the integer pipe.  Zeros map to zeros;
+// subnormal floats (|x| < 1.2e-38) flush to zero; Krylov vectors hold no
+// infinities or NaNs.
+__device__ __forceinline__ double widen(float x) {
+  const uint32_t u = __float_as_uint(x);
+  const uint32_t e = (u >> 23) & 0xffu;
+  uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+  uint32_t lo = u << 29;
+  if (e == 0u) {
+    hi = u & 0x80000000u;
+    lo = 0u;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+__device__ __forceinline__ double widen(double x) { return x; }
+#endif
+
+#define SMGPU_CUDA_TRY(expr)                                                    \
   do {                                                                            \
     cudaError_t _e = (expr);                                                      \
     if (_e != cudaSuccess) throw ::smgpu::CudaError{_e, #expr, __FILE__, __LINE__}; \

@@ -72,8 +72,8 @@ struct HvArgs {
 
 constexpr int KMAX = 16;
 
-template <class TV, class TC, class Acc, int NT, int R>
-__global__ void __launch_bounds__(NT) hv_tile_kernel(const HvArgs<TV, TC> a) {
+template <class TV, class TC, class Acc, int NT, int R, int MINB>
+__global__ void __launch_bounds__(NT, MINB) hv_tile_kernel(const HvArgs<TV, TC> a) {
   if (a.fl != nullptr && (a.fl->done || a.fl->exhausted)) return;
   const DevTables& t = a.t;
   const int task = blockIdx.x;
@@ -138,20 +138,44 @@ __global__ void __launch_bounds__(NT) hv_tile_kernel(const HvArgs<TV, TC> a) {
       int Kw = K;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) Kw = max(Kw, __shfl_xor_sync(0xffffffffu, Kw, o));
-      int nfk[KMAX], vck[KMAX];
+      // the thread's neutron entries (n' << 14 | signed table column), packed
+      uint32_t ent[KMAX];
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
-        uint32_t e = (k < K) ? a.tt.npn_ent[jb + k] : 0u;
-        nfk[k] = (int)(e >> 14);
-        vck[k] = (int)(e & 0x3fffu);
-      }
+      for (int k = 0; k < KMAX; ++k) ent[k] = (k < K) ? a.tt.npn_ent[jb + k] : 0u;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         if (r >= nr) break;
         const int eb = a.tt.rl[rlb + (int64_t)r * (nl + 1) + j];
         const int ee = a.tt.rl[rlb + (int64_t)r * (nl + 1) + j + 1];
         TC part = (TC)0;
-        for (int e = eb; e < ee; ++e) {
+        int e = eb;
+        // two proton entries in flight: twice the independent gathers per thread
+        for (; e + 1 < ee; e += 2) {
+          const TV* __restrict__ row0 = vs + (int64_t)t.ppn_src[e] * sstride;
+          const TV* __restrict__ row1 = vs + (int64_t)t.ppn_src[e + 1] * sstride;
+          const uint32_t m0 = t.ppn_meta[e], m1 = t.ppn_meta[e + 1];
+          const TC* __restrict__ vr0 = vt + (int)((m0 >> 1) & 0x7fffu) * nB;
+          const TC* __restrict__ vr1 = vt + (int)((m1 >> 1) & 0x7fffu) * nB;
+          TC pe0 = (TC)0, pe1 = (TC)0;
+#pragma unroll
+          for (int k = 0; k < KMAX; ++k) {
+            if (k >= Kw) break;
+            if (k < K) {
+              const int nf = (int)(ent[k] >> 14), vc = (int)(ent[k] & 0x3fffu);
+              pe0 += vr0[vc] * (TC)row0[nf];
+              pe1 += vr1[vc] * (TC)row1[nf];
+            }
+          }
+          if (Kw > KMAX)  // lists longer than the register cache
+            for (int k = KMAX; k < K; ++k) {
+              const uint32_t en = a.tt.npn_ent[jb + k];
+              pe0 += vr0[en & 0x3fffu] * (TC)row0[en >> 14];
+              pe1 += vr1[en & 0x3fffu] * (TC)row1[en >> 14];
+            }
+          part += (m0 & 1u) ? -pe0 : pe0;
+          part += (m1 & 1u) ? -pe1 : pe1;
+        }
+        if (e < ee) {
           const TV* __restrict__ row = vs + (int64_t)t.ppn_src[e] * sstride;
           const uint32_t meta = t.ppn_meta[e];
           const TC* __restrict__ vr = vt + (int)((meta >> 1) & 0x7fffu) * nB;
@@ -159,11 +183,11 @@ __global__ void __launch_bounds__(NT) hv_tile_kernel(const HvArgs<TV, TC> a) {
 #pragma unroll
           for (int k = 0; k < KMAX; ++k) {
             if (k >= Kw) break;
-            if (k < K) pe += vr[vck[k]] * (TC)row[nfk[k]];
+            if (k < K) pe += vr[ent[k] & 0x3fffu] * (TC)row[ent[k] >> 14];
           }
-          if (Kw > KMAX)  // lists longer than the register cache
+          if (Kw > KMAX)
             for (int k = KMAX; k < K; ++k) {
-              uint32_t en = a.tt.npn_ent[jb + k];
+              const uint32_t en = a.tt.npn_ent[jb + k];
               pe += vr[en & 0x3fffu] * (TC)row[en >> 14];
             }
           part += (meta & 1u) ? -pe : pe;
@@ -204,27 +228,32 @@ __global__ void __launch_bounds__(NT) hv_tile_kernel(const HvArgs<TV, TC> a) {
 template <class TV, class TC, class Acc>
 static void launch_cfg(const HvConfig& cfg, const HvArgs<TV, TC>& a, cudaStream_t st) {
   const int grid = cfg.ntasks;
-#define SMGPU_HV_CASE(NT_, R_)                                              \
-  if (cfg.nt == NT_ && cfg.rows == R_) {                                    \
-    hv_tile_kernel<TV, TC, Acc, NT_, R_><<<grid, NT_, 0, st>>>(a);          \
-    return;                                                                 \
+#define SMGPU_HV_CASE(NT_, R_, MB_)                                           \
+  if (cfg.nt == NT_ && cfg.rows == R_ && cfg.minb == MB_) {                   \
+    hv_tile_kernel<TV, TC, Acc, NT_, R_, MB_><<<grid, NT_, 0, st>>>(a);       \
+    return;                                                                   \
   }
-  SMGPU_HV_CASE(128, 1)
-  SMGPU_HV_CASE(128, 2)
-  SMGPU_HV_CASE(128, 4)
-  SMGPU_HV_CASE(128, 8)
-  SMGPU_HV_CASE(192, 2)
-  SMGPU_HV_CASE(192, 4)
-  SMGPU_HV_CASE(256, 1)
-  SMGPU_HV_CASE(256, 2)
-  SMGPU_HV_CASE(256, 4)
-  SMGPU_HV_CASE(256, 8)
+  SMGPU_HV_CASE(128, 1, 1)
+  SMGPU_HV_CASE(128, 2, 1)
+  SMGPU_HV_CASE(128, 4, 1)
+  SMGPU_HV_CASE(128, 8, 1)
+  SMGPU_HV_CASE(128, 1, 8)
+  SMGPU_HV_CASE(128, 2, 6)
+  SMGPU_HV_CASE(128, 4, 6)
+  SMGPU_HV_CASE(192, 2, 4)
+  SMGPU_HV_CASE(256, 1, 1)
+  SMGPU_HV_CASE(256, 2, 1)
+  SMGPU_HV_CASE(256, 4, 1)
+  SMGPU_HV_CASE(256, 2, 3)
+  SMGPU_HV_CASE(256, 4, 3)
 #undef SMGPU_HV_CASE
 }
 
 const HvConfig* hv_candidates(int* count) {
-  static const HvConfig c[] = {{128, 1, 0}, {128, 2, 0}, {128, 4, 0}, {128, 8, 0}, {192, 2, 0},
-                               {192, 4, 0}, {256, 1, 0}, {256, 2, 0}, {256, 4, 0}, {256, 8, 0}};
+  // {threads, rows per CTA, -, min CTAs per SM (register cap)}
+  static const HvConfig c[] = {{128, 1, 0, 1}, {128, 2, 0, 1}, {128, 4, 0, 1}, {128, 8, 0, 1}, {128, 1, 0, 8},
+                               {128, 2, 0, 6}, {128, 4, 0, 6}, {192, 2, 0, 4}, {256, 1, 0, 1}, {256, 2, 0, 1},
+                               {256, 4, 0, 1}, {256, 2, 0, 3}, {256, 4, 0, 3}};
   *count = (int)(sizeof(c) / sizeof(c[0]));
   return c;
 }

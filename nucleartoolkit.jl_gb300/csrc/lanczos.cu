@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int6
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int j = j0 + q;
-        if (j < m) acc[q] = fma((double)X[(int64_t)j * ld + i], yi, acc[q]);
+        if (j < m) acc[q] = fma(widen(X[(int64_t)j * ld + i]), yi, acc[q]);
         else if (j == m && self) acc[q] = fma(yi, yi, acc[q]);
       }
     }
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
     for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
       double wv;
       if (j0 == 0) {
-        wv = fma(-alpha, (double)vk[i], w[i]);
+        wv = fma(-alpha, widen(vk[i]), w[i]);
         w[i] = wv;
       } else {
         wv = w[i];
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int j = j0 + q;
-        if (j < m) acc[q] = fma((double)V[(int64_t)j * ld + i], wv, acc[q]);
+        if (j < m) acc[q] = fma(widen(V[(int64_t)j * ld + i]), wv, acc[q]);
         else if (j == m) acc[q] = fma(wv, wv, acc[q]);
       }
     }
@@ -272,7 +272,7 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
   double nrm = 0.0;
   for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
     double t = w[i];
-    for (int j = 0; j < m; ++j) t = fma(-hs[j], (double)V[(int64_t)j * ld + i], t);
+    for (int j = 0; j < m; ++j) t = fma(-hs[j], widen(V[(int64_t)j * ld + i]), t);
     w[i] = t;
     nrm = fma(t, t, nrm);
   }
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
       const double wv = w[i];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (j0 + q < m) acc[q] = fma((double)V[(int64_t)(j0 + q) * ld + i], wv, acc[q]);
+        if (j0 + q < m) acc[q] = fma(widen(V[(int64_t)(j0 + q) * ld + i]), wv, acc[q]);
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -603,10 +603,11 @@ __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int
 }
 
 // ThickRestart's small part (lanczos_methods.jl:261-271): new arrowhead T.
-__global__ void k_restart_small(double* T, int lm, int ls, const double* evals, const double* vecs,
+__global__ void k_restart_small(double* T, int lm, int ls, const double* evals, const double* vecs, float* vecs_f,
                                 const LanczosFlags* fl) {
   if (stopped(fl)) return;
   const int m = lm - 1;
+  for (int idx = threadIdx.x; idx < m * ls; idx += blockDim.x) vecs_f[idx] = (float)vecs[idx];
   __shared__ double beta;
   if (threadIdx.x == 0) beta = T[(int64_t)(lm - 1) * lm + (lm - 2)];
   __syncthreads();
@@ -624,7 +625,8 @@ __global__ void k_restart_small(double* T, int lm, int ls, const double* evals, 
 // Kahan sums for the mixed form (the result is stored in FP32).
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V, TX* __restrict__ U,
-                                                        const double* __restrict__ Y, int m, int ls, int64_t len,
+                                                        const double* __restrict__ Y, const float* __restrict__ Yf,
+                                                        int m, int ls, int64_t len,
                                                         const LanczosFlags* __restrict__ fl) {
   if (stopped(fl)) return;
   // Y (m x ls, column-major) is small and read through L1
@@ -638,7 +640,7 @@ __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V
           const float x = (float)V[(int64_t)j * len + i];
 #pragma unroll
           for (int q = 0; q < 8; ++q)
-            if (k0 + q < ls) acc[q].add(__fmul_rn((float)__ldg(Y + (int64_t)(k0 + q) * m + j), x));
+            if (k0 + q < ls) acc[q].add(__fmul_rn(__ldg(Yf + (int64_t)(k0 + q) * m + j), x));
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q)
@@ -679,7 +681,7 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
     for (int idx = threadIdx.x; idx < (ls + 1) * TILE; idx += kNT) {
       int j = idx / TILE, x = idx % TILE;
       double val = 0.0;
-      if (x < cnt) val = (j < ls) ? (double)U[(int64_t)j * len + t0 + x] : (double)vl[t0 + x];
+      if (x < cnt) val = (j < ls) ? widen(U[(int64_t)j * len + t0 + x]) : widen(vl[t0 + x]);
       tile[idx] = val;
     }
     __syncthreads();
@@ -763,19 +765,42 @@ __global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U,
                                                        int ls, int lm, int64_t len,
                                                        const LanczosFlags* __restrict__ fl) {
   if (stopped(fl)) return;
-  extern __shared__ double xs[];  // ls*ls + ls
-  for (int idx = threadIdx.x; idx < ls * ls; idx += kNT) xs[idx] = X[idx];
-  for (int idx = threadIdx.x; idx < ls; idx += kNT) xs[ls * ls + idx] = cvec[idx];
+  extern __shared__ double xs[];  // ls*ls + ls doubles, then the same as floats
+  float* xf = (float*)(xs + ls * ls + ls);
+  for (int idx = threadIdx.x; idx < ls * ls; idx += kNT) {
+    xs[idx] = X[idx];
+    xf[idx] = (float)X[idx];
+  }
+  for (int idx = threadIdx.x; idx < ls; idx += kNT) {
+    xs[ls * ls + idx] = cvec[idx];
+    xf[ls * ls + idx] = (float)cvec[idx];
+  }
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
-    double last = (double)V[(int64_t)(lm - 1) * len + i];
-    for (int k = 0; k < ls; ++k) {
-      double q = 0.0;
-      for (int j = 0; j <= k; ++j) q = fma(xs[k * ls + j], (double)U[(int64_t)j * len + i], q);
-      V[(int64_t)k * len + i] = (TX)q;
-      last = fma(-xs[ls * ls + k], q, last);
+    if constexpr (sizeof(TX) == 4) {
+      // mixed form: X is the identity up to O(1e-7); FP32 products, Kahan sums
+      KahanF last;
+      last.init();
+      last.add((float)V[(int64_t)(lm - 1) * len + i]);
+      for (int k = 0; k < ls; ++k) {
+        KahanF q;
+        q.init();
+        for (int j = 0; j <= k; ++j) q.add(__fmul_rn(xf[k * ls + j], (float)U[(int64_t)j * len + i]));
+        const float qv = q.get();
+        V[(int64_t)k * len + i] = (TX)qv;
+        last.add(__fmul_rn(-xf[ls * ls + k], qv));
+      }
+      V[(int64_t)ls * len + i] = (TX)last.get();
+    } else {
+      double last = (double)V[(int64_t)(lm - 1) * len + i];
+      for (int k = 0; k < ls; ++k) {
+        double q = 0.0;
+        for (int j = 0; j <= k; ++j) q = fma(xs[k * ls + j], (double)U[(int64_t)j * len + i], q);
+        V[(int64_t)k * len + i] = (TX)q;
+        last = fma(-xs[ls * ls + k], q, last);
+      }
+      V[(int64_t)ls * len + i] = (TX)last;
     }
-    V[(int64_t)ls * len + i] = (TX)last;
   }
 }
 
@@ -850,12 +875,12 @@ void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t s
   k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
 }
 void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
-  k_restart_small<<<1, 256, 0, st>>>(L.T, L.lm, L.ls, L.evals, L.jacA, L.fl);
+  k_restart_small<<<1, 256, 0, st>>>(L.T, L.lm, L.ls, L.evals, L.jacA, L.Yf, L.fl);
 }
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st) {
   int m = L.lm - 1;
-  k_restart_rotate<TX><<<grid_for(L.len), kNT, 0, st>>>(V, U, L.jacA, m, L.ls, L.len, L.fl);
+  k_restart_rotate<TX><<<grid_for(L.len), kNT, 0, st>>>(V, U, L.jacA, L.Yf, m, L.ls, L.len, L.fl);
 }
 template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
@@ -870,7 +895,8 @@ void launch_chol(const LanczosDev& L, cudaStream_t st) {
 }
 template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st) {
-  k_restart_apply<TX><<<grid_for(L.len), kNT, sizeof(double) * (L.ls * L.ls + L.ls), st>>>(U, V, L.X, L.cvec, L.ls,
+  k_restart_apply<TX><<<grid_for(L.len), kNT, (sizeof(double) + sizeof(float)) * (L.ls * L.ls + L.ls), st>>>(
+      U, V, L.X, L.cvec, L.ls,
                                                                                              L.lm, L.len, L.fl);
 }
 template <class TX>

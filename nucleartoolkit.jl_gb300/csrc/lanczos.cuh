@@ -32,6 +32,7 @@ struct LanczosDev {
   double* jacA;         // lm x lm
   double* jacZ;         // lm x lm
   double* evals;        // lm
+  float* Yf;            // (lm-1) x ls: FP32 copy of the restart rotation
   double* gram;         // ls*(ls+1)/2 + ls (restart Gram matrix, packed)
   double* X;            // ls x ls (restart: inverse Cholesky factor)
   double* cvec;         // ls

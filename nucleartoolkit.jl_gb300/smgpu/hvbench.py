@@ -34,7 +34,8 @@ def main():
     ms = P.time_matvec(reps=a.reps, flush_l2=not a.no_flush)
     st = P.stats()
     out = {"workload": a.workload, "precision": a.precision, "mdim": P.mdim, "ms": ms, "updates": st["updates"],
-           "table_bytes": st["table_bytes"], "links": st["links"]}
+           "table_bytes": st["table_bytes"], "links": st["links"], "hv_threads": st["hv_threads"],
+           "hv_rows": st["hv_rows"], "hv_min_ctas": st["hv_min_ctas"]}
     if a.nnz:
         s = 4 if prec == smgpu.MIXED else 8
         b = a.nnz * (s + 4) + 4 * (P.mdim + 1) + 2 * P.mdim * s

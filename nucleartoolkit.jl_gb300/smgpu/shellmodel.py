@@ -70,10 +70,10 @@ class ShellModelProblem:
         return (ints, coef) if which in (2, 3) else ints
 
     def stats(self):
-        s = np.zeros(10, dtype=np.int64)
+        s = np.zeros(11, dtype=np.int64)
         check(load().smgpu_stats(self._h, _p(s)), self._h)
         keys = ["updates", "pn_proton_entries", "pn_neutron_entries", "pp_entries", "nn_entries", "table_bytes",
-                "len_pad", "links", "hv_threads", "hv_rows"]
+                "len_pad", "links", "hv_threads", "hv_rows", "hv_min_ctas"]
         return dict(zip(keys, map(int, s)))
 
     def timings(self):
