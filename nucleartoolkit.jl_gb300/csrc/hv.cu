@@ -72,33 +72,6 @@ struct HvArgs {
 
 constexpr int KMAX = 16;
 
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-
-// Prefetch into L1 the source rows that the R rows of this CTA read through
-// link slot j (whole rows: the neutron columns read are scattered over them).
-template <class TV, int NT, int R>
-__device__ __forceinline__ void prefetch_link(const DevTables& t, const TileTables& tt, const TV* v, int lb, int nl,
-                                              int64_t rlb, int nr, int j) {
-  if (j >= nl) return;
-  const int L = lb + j;
-  const int s = t.link_a[L].x;
-  const TV* vs = v + t.off_pad[s];
-  const int ss = t.stride[s];
-  constexpr int per_line = 128 / (int)sizeof(TV);
-  const int lines = (ss + per_line - 1) / per_line;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    if (r >= nr) break;
-    const int eb = tt.rl[rlb + (int64_t)r * (nl + 1) + j];
-    const int ee = tt.rl[rlb + (int64_t)r * (nl + 1) + j + 1];
-    const int total = (ee - eb) * lines;
-    for (int idx = threadIdx.x; idx < total; idx += NT) {
-      const int e = eb + idx / lines, l = idx % lines;
-      prefetch_l1(vs + (int64_t)t.ppn_src[e] * ss + l * per_line);
-    }
-  }
-}
-
 template <class TV, class TC, class Acc, int NT, int R, int MINB>
 __global__ void __launch_bounds__(NT, MINB) hv_tile_kernel(const HvArgs<TV, TC> a) {
   if (a.fl != nullptr && (a.fl->done || a.fl->exhausted)) return;
@@ -125,13 +98,11 @@ __global__ void __launch_bounds__(NT, MINB) hv_tile_kernel(const HvArgs<TV, TC> 
     Acc acc[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) acc[r].init();
-    prefetch_link<TV, NT, R>(t, a.tt, v, lb, nl, rlb, nr, 0);
 
     // nn: same proton row, other neutron columns (the column list is shared by the R rows)
     if (act) {
       const int gn = nst + n;
       const int kb = t.nn_ptr[gn], ke = t.nn_ptr[gn + 1];
-#pragma unroll 4
       for (int k = kb; k < ke; ++k) {
         const int c = t.nn_col[k];
         const TC cv = a.c.nn_val[k];
@@ -146,14 +117,11 @@ __global__ void __launch_bounds__(NT, MINB) hv_tile_kernel(const HvArgs<TV, TC> 
       if (r >= nr) break;
       const int g = pst + p0 + r;
       const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
-      if (act) {
-#pragma unroll 4
+      if (act)
         for (int k = kb; k < ke; ++k) acc[r].add(a.c.pp_val[k] * (TC)v[blk + (int64_t)t.pp_col[k] * stride + n]);
-      }
     }
-    // pn, link by link; the next link's source rows are prefetched meanwhile
+    // pn, link by link
     for (int j = 0; j < nl; ++j) {
-      prefetch_link<TV, NT, R>(t, a.tt, v, lb, nl, rlb, nr, j + 1);
       const int L = lb + j;
       const int4 la = t.link_a[L];
       const int nB = la.y;

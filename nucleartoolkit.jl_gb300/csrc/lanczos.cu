@@ -95,6 +95,28 @@ __device__ __forceinline__ int find_block(const int64_t* off, int nb, int64_t i)
   return lo;
 }
 
+// Four consecutive elements (16-byte aligned: vector lengths and chunk starts
+// are multiples of 4) widened to FP64.
+__device__ __forceinline__ void load4(const float* p, double (&o)[4]) {
+  const float4 f = *reinterpret_cast<const float4*>(p);
+  o[0] = widen(f.x);
+  o[1] = widen(f.y);
+  o[2] = widen(f.z);
+  o[3] = widen(f.w);
+}
+__device__ __forceinline__ void load4(const double* p, double (&o)[4]) {
+  const double2 a = *reinterpret_cast<const double2*>(p);
+  const double2 b = *reinterpret_cast<const double2*>(p + 2);
+  o[0] = a.x;
+  o[1] = a.y;
+  o[2] = b.x;
+  o[3] = b.y;
+}
+__device__ __forceinline__ void store4(double* p, const double (&o)[4]) {
+  *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(o[2], o[3]);
+}
+
 // Kahan-compensated FP32 sum.
 struct KahanF {
   float s, c;
@@ -230,19 +252,28 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
     double acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-    for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
-      double wv;
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+      double wv[4];
+      load4(w + i, wv);
       if (j0 == 0) {
-        wv = fma(-alpha, widen(vk[i]), w[i]);
-        w[i] = wv;
-      } else {
-        wv = w[i];
+        double x[4];
+        load4(vk + i, x);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
+        store4(w + i, wv);
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int j = j0 + q;
-        if (j < m) acc[q] = fma(widen(V[(int64_t)j * ld + i]), wv, acc[q]);
-        else if (j == m) acc[q] = fma(wv, wv, acc[q]);
+        if (j < m) {
+          double x[4];
+          load4(V + (int64_t)j * ld + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+        } else if (j == m) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
+        }
       }
     }
 #pragma unroll
@@ -270,11 +301,19 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
   double nrm = 0.0;
-  for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
-    double t = w[i];
-    for (int j = 0; j < m; ++j) t = fma(-hs[j], widen(V[(int64_t)j * ld + i]), t);
-    w[i] = t;
-    nrm = fma(t, t, nrm);
+  for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+    double t[4];
+    load4(w + i, t);
+    for (int j = 0; j < m; ++j) {
+      double x[4];
+      load4(V + (int64_t)j * ld + i, x);
+      const double hj = hs[j];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+    }
+    store4(w + i, t);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
   }
   double s = block_sum_all<kNT>(nrm, red);
   if (threadIdx.x == 0) pout[blockIdx.x] = s;
@@ -305,11 +344,17 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
     double acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-    for (int64_t i = cb + threadIdx.x; i < ce; i += kNT) {
-      const double wv = w[i];
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+      double wv[4];
+      load4(w + i, wv);
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (j0 + q < m) acc[q] = fma(widen(V[(int64_t)(j0 + q) * ld + i]), wv, acc[q]);
+        if (j0 + q < m) {
+          double x[4];
+          load4(V + (int64_t)(j0 + q) * ld + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+        }
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -663,50 +708,83 @@ __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V
   }
 }
 
-// Gram matrix of U (upper triangle, packed row by row) and U_k·v_last, FP64.
+// Double-float accumulator: exact FP32 products (two-product by FMA) summed
+// with TwoSum into an unevaluated (hi, lo) pair — about 2^-48 relative, on
+// the FP32 pipe.  Used for the restart Gram matrix of FP32-stored vectors.
+struct DFAcc {
+  float hi, lo;
+  __device__ __forceinline__ void init() { hi = 0.f; lo = 0.f; }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+  }
+  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ void gram_pair(int pr, int ls, int& k, int& l) {
+  if (pr < ls * (ls + 1) / 2) {
+    k = 0;
+    int rem = pr;
+    while (rem >= ls - k) { rem -= ls - k; ++k; }
+    l = k + rem;
+  } else {
+    k = pr - ls * (ls + 1) / 2;
+    l = ls;  // v_last
+  }
+}
+
+// Gram matrix of U (upper triangle, packed row by row) and U_k·v_last.
 // Entry order: pairs (k,l) with k <= l in row-major order, then g_k.
+// FP64 for FP64 vectors; double-float for FP32 vectors (mixed form).
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX* __restrict__ vl, int ls,
                                               int64_t len, double* __restrict__ partials, int G,
                                               const LanczosFlags* __restrict__ fl) {
   if (stopped(fl)) return;
   constexpr int TILE = 64;
-  extern __shared__ double tile[];  // (ls+1) x TILE
+  extern __shared__ double tile[];  // (ls+1) x TILE of TX
+  TX* tl = reinterpret_cast<TX*>(tile);
   const int P = ls * (ls + 1) / 2 + ls;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
   double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  DFAcc dacc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) dacc[q].init();
   for (int64_t t0 = cb; t0 < ce; t0 += TILE) {
     const int cnt = (int)min((int64_t)TILE, ce - t0);
     for (int idx = threadIdx.x; idx < (ls + 1) * TILE; idx += kNT) {
       int j = idx / TILE, x = idx % TILE;
-      double val = 0.0;
-      if (x < cnt) val = (j < ls) ? widen(U[(int64_t)j * len + t0 + x]) : widen(vl[t0 + x]);
-      tile[idx] = val;
+      TX val = (TX)0;
+      if (x < cnt) val = (j < ls) ? U[(int64_t)j * len + t0 + x] : vl[t0 + x];
+      tl[idx] = val;
     }
     __syncthreads();
+#pragma unroll
     for (int q = 0; q < 8; ++q) {
       int pr = threadIdx.x + q * kNT;
       if (pr >= P) break;
       int k, l;
-      if (pr < ls * (ls + 1) / 2) {
-        k = 0;
-        int rem = pr;
-        while (rem >= ls - k) { rem -= ls - k; ++k; }
-        l = k + rem;
+      gram_pair(pr, ls, k, l);
+      if constexpr (sizeof(TX) == 4) {
+        for (int x = 0; x < cnt; ++x) dacc[q].add_prod(tl[k * TILE + x], tl[l * TILE + x]);
       } else {
-        k = pr - ls * (ls + 1) / 2;
-        l = ls;  // v_last
+        double s = acc[q];
+        for (int x = 0; x < cnt; ++x) s = fma((double)tl[k * TILE + x], (double)tl[l * TILE + x], s);
+        acc[q] = s;
       }
-      double s = acc[q];
-      for (int x = 0; x < cnt; ++x) s = fma(tile[k * TILE + x], tile[l * TILE + x], s);
-      acc[q] = s;
     }
     __syncthreads();
   }
+#pragma unroll
   for (int q = 0; q < 8; ++q) {
     int pr = threadIdx.x + q * kNT;
-    if (pr < P) partials[(int64_t)pr * G + blockIdx.x] = acc[q];
+    if (pr < P) partials[(int64_t)pr * G + blockIdx.x] = (sizeof(TX) == 4) ? dacc[q].get() : acc[q];
   }
 }
 
