@@ -145,6 +145,26 @@ int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
  * (the autotuned launch shape)]. */
 int smgpu_stats(const smgpu_problem* h, long long* stats_out);
 
+/* H·v that allocates nothing.  No counterpart in the reference: it exists for
+ * callers that cannot have the library allocate device memory while they run
+ * — code recording a CUDA stream capture (allocation is not capturable) and
+ * hosts whose device memory is owned by their own pool allocator (a Julia
+ * CuArray pool, a PyTorch caching allocator), which must not see cudaMalloc
+ * or cudaFree from a library in the middle of a step.
+ *   v, w : caller-owned DEVICE buffers of mdim doubles in the reference's
+ *          basis order (the layout of smgpu_matvec's host vectors);
+ *          w = H v is overwritten, the FP64 form is used;
+ *   vhv  : NULL or a caller-owned DEVICE double that receives <v|H|v>.
+ * The only scratch, the per-CTA partial sums of <v|H|v>, is a file-scope
+ * device array of 65,536 doubles (512 KB) that every GPU loading the library
+ * holds until exit; problems whose H·v launch has more CTAs than that, and
+ * handles created with SMGPU_MIXED, are rejected (SMGPU_ERR_LIMIT /
+ * SMGPU_ERR_ARG).  The first call on a device looks up the array's device
+ * address; make that first call before any stream capture.  All calls share
+ * the array (each call rewrites every entry it reads), so calls that overlap
+ * on the GPU race; the call returns when w and *vhv are ready. */
+int smgpu_matvec_noalloc(smgpu_problem* h, const double* v, double* w, double* vhv);
+
 #ifdef __cplusplus
 }
 #endif

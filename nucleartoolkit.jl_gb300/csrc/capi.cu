@@ -885,3 +885,80 @@ int smgpu_stats(const smgpu_problem* h, long long* s) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free H·v (smgpu_matvec_noalloc).
+//
+// For callers that cannot allocate device memory while they run: code inside
+// a CUDA stream capture (allocation calls are not capturable), and hosts whose
+// device memory belongs to their own pool allocator (a Julia CuArray or
+// PyTorch caching pool) and must not see cudaMalloc/cudaFree from a library
+// in the middle of a step.  The only scratch this H·v needs — the per-CTA
+// partial sums of <v|H|v> — lives in the file-scope array below, so the call
+// allocates nothing.  Every GPU that loads the library holds this array
+// (512 KB) until the process exits.
+namespace {
+constexpr int kNoAllocMaxPartials = 1 << 16;  // CTAs of one H·v launch; 65,536 doubles = 512 KB
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_noalloc_partials on the current device.  Host code only
+// holds a host-side stand-in for the symbol, so the address is looked up once
+// per device (with that device current) and cached.
+double* noalloc_scratch() {
+  int dev = -1;
+  SMGPU_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) throw SetupError{SMGPU_ERR_ARG, "device ordinal out of range"};
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    SMGPU_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  return g_noalloc_addr[dev];
+}
+
+__global__ void k_noalloc_vhv(const double* __restrict__ partials, int n, double* __restrict__ out) {
+  __shared__ double red[32];
+  double x = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x += partials[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    *out = s;
+  }
+}
+}  // namespace
+
+extern "C" int smgpu_matvec_noalloc(smgpu_problem* h, const double* v, double* w, double* vhv) {
+  if (!h || !v || !w) return fail(h, SMGPU_ERR_ARG, "null argument");
+  if (h->precision != SMGPU_FP64)
+    return fail(h, SMGPU_ERR_ARG, "smgpu_matvec_noalloc needs a handle created with SMGPU_FP64");
+  if (h->cfg.ntasks > kNoAllocMaxPartials)
+    return fail(h, SMGPU_ERR_LIMIT,
+                "problem too large for smgpu_matvec_noalloc: the H·v launch needs " + std::to_string(h->cfg.ntasks) +
+                    " partial sums, the static scratch holds " + std::to_string(kNoAllocMaxPartials));
+  return guarded(h, [&]() {
+    double* scratch = noalloc_scratch();
+    // the handle's tables viewed in the reference's unpadded layout: block b
+    // at tdims[b], rows of stride nn[b]
+    DevTables t = h->dt;
+    t.stride = h->dt.nn;
+    t.off_pad = h->dt.tdims;
+    t.len_pad = h->T.mdim;
+    HvEpilogue<double> epi{};
+    epi.alpha_part = scratch;
+    launch_hv_fp64(t, h->tt, h->cfg, h->d_ep, h->d_en, h->c64, v, w, epi, h->st);
+    if (vhv) k_noalloc_vhv<<<1, 256, 0, h->st>>>(scratch, h->cfg.ntasks, vhv);
+    SMGPU_CUDA_TRY(cudaGetLastError());
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(h->st));
+    return SMGPU_OK;
+  });
+}

@@ -40,6 +40,7 @@ SIGNATURES = {
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "smgpu_matvec_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
 }
 
 _lib = None
