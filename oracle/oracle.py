@@ -53,6 +53,8 @@ def lib():
         L.orc_trl.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
                               C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_trl_sample.restype = C.c_int
+        L.orc_trl_sample.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]
         L.orc_clebsch.restype = C.c_double
         L.orc_clebsch.argtypes = [C.c_int] * 6
         L.orc_set_threads.argtypes = [C.c_int]
@@ -187,6 +189,14 @@ class OracleProblem:
             e[j] = 1.0
             H[:, j] = self.operate_H(e)
         return H
+
+    def trl_sample(self, num_ev, lm, ls, tol, max_hv):
+        """Time the first `max_hv` H·v iterations of TRL (restarts included)."""
+        out = np.zeros(6)
+        if lib().orc_trl_sample(self._h, num_ev, lm, ls, tol, max_hv, _p(out)) != 0:
+            raise RuntimeError("oracle TRL sample: " + lib().orc_last_error().decode())
+        return dict(t_hv=out[0], t_reorth=out[1], t_restart=out[2], t_total=out[3], n_hv=int(out[4]),
+                    n_restart=int(out[5]))
 
     def trl(self, num_ev, lm=300, ls=20, tol=1e-8, max_restart=10000, v1=None, seed=1234, want_vecs=False):
         L = lib()

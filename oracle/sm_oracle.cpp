@@ -975,7 +975,7 @@ struct TrlResult {
   int elit = 0, n_hv = 0, n_restart = 0;
   bool converged = false;
   std::vector<double> ritz;  // num_ev × mdim
-  double t_hv = 0, t_reorth = 0;
+  double t_hv = 0, t_reorth = 0, t_restart = 0;
 };
 
 }  // namespace
@@ -997,7 +997,7 @@ void ReORTH(int it, double* vt, std::vector<std::vector<double>>& vks, i64 n) {
 // lanczos_methods.jl:1-91 TRL + 250-258 diagonalize_T! + 260-307 ThickRestart,
 // then shellmodel_main.jl:208-224 Ritz vectors.
 TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_restart, const double* v1,
-              u64 seed, bool want_vecs, int num_history) {
+              u64 seed, bool want_vecs, int num_history, int max_hv = 0) {
   i64 mdim = P.mdim;
   num_ev = (int)std::min<i64>(num_ev, mdim);
   TrlResult R;
@@ -1023,6 +1023,8 @@ TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_
       operate_H(P, vk, vkp1);
       R.t_hv += now_s() - t0;
       R.n_hv++;
+      if (max_hv > 0 && R.n_hv >= max_hv) { TF = false; elit = it; goto sample_end; }
+      {
       double talpha = dotp(mdim, vk, vkp1);
       Tm(it, it) = talpha;
       // diagonalize_T!
@@ -1047,10 +1049,12 @@ TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_
       scal(mdim, 1.0 / tbeta, vkp1);
       Tm(it + 1, it) = tbeta;
       Tm(it, it + 1) = tbeta;
+      }
     }
     if (!TF) {
       if (R.n_restart >= max_restart) break;
       R.n_restart++;
+      double t_rs0 = now_s();
       // ThickRestart
       int m = lm - 1;
       std::vector<double> sub((size_t)m * m), vals(m), vecs((size_t)m * m);
@@ -1076,9 +1080,11 @@ TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_
       vks[ls] = vks[lm - 1];
       ReORTH(ls, vks[ls].data(), vks, mdim);
       for (int kk = ls + 2; kk <= lm; ++kk) std::fill(vks[kk - 1].begin(), vks[kk - 1].end(), 0.0);
+      R.t_restart += now_s() - t_rs0;
     }
     k = ls + 1;
   }
+sample_end:
   R.converged = TF;
   R.elit = elit;
   R.en = en[0];
@@ -1289,6 +1295,21 @@ int orc_trl(void* h, int num_ev, int lm, int ls, double tol, int max_restart, co
     if (evecs) std::memcpy(evecs, R.ritz.data(), sizeof(double) * R.ritz.size());
     if (stats) { stats[0] = R.elit; stats[1] = R.n_hv; stats[2] = R.n_restart; stats[3] = R.converged ? 1 : 0; }
     if (times) { times[0] = R.t_hv; times[1] = R.t_reorth; times[2] = now_s() - t0; }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+
+// Timed sample of the TRL loop for the CPU baseline: stops after max_hv
+// H·v products.  out: [t_hv, t_reorth, t_restart, t_total, n_hv, n_restart].
+int orc_trl_sample(void* h, int num_ev, int lm, int ls, double tol, int max_hv, double* out) {
+  try {
+    double t0 = now_s();
+    TrlResult R = TRL(*(Problem*)h, num_ev, lm, ls, tol, 1000000, nullptr, 1234ull, false, 3, max_hv);
+    out[0] = R.t_hv; out[1] = R.t_reorth; out[2] = R.t_restart; out[3] = now_s() - t0;
+    out[4] = R.n_hv; out[5] = R.n_restart;
     return 0;
   } catch (const std::exception& e) {
     g_err = e.what();
