@@ -9,8 +9,9 @@ of both forms against the FP64 oracle, the H·v roofline and the CPU baseline.
 
 --impl reference times the CPU restatement of the reference's path (the
 oracle: operate_H! + TRL with OpenMP over blocks) on all host cores instead;
-each step is a bounded sample (two Lanczos iterations) projected to the
-oracle's full iteration count.
+each step is a bounded sample (the first restart cycle: lm TRL iterations and
+one thick restart) projected to the oracle's full iteration and restart counts
+(tests/golden/oracle_runs.json).
 """
 import argparse
 import json
@@ -283,13 +284,13 @@ def run_gpu(args, dist, rank, local):
     peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
     peak = (peaks or {}).get("hbm_gbs") or HBM_FALLBACK
     peak_src = "measured" if peaks and peaks.get("hbm_gbs") else "fallback"
-    prof = load_json(os.path.join(ROOT, "profiles", "hv_pull_pf4p4n_traffic.json")) or {}
+    prof = load_json(os.path.join(ROOT, "profiles", "hv_tile_pf4p4n_traffic.json")) or {}
     roof = None
     if nnz:
         b_alg = nnz * (4 + 4) + 4 * (mdim + 1) + 2 * 1 * mdim * 4
         achieved = b_alg / (hv_ms_mixed * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": prof.get("mixed_bytes_per_launch"), "kernel": "hv_pull_kernel<float> (FP32-mixed H·v)",
+                "traffic": prof.get("mixed_bytes_per_launch"), "kernel": "hv_tile_kernel<float> (FP32-mixed H·v)",
                 "peak_source": peak_src, "algorithmic_bytes": b_alg,
                 "hv_ms": hv_ms_mixed, "hv_fp64_ms": hv_ms_fp64,
                 "hv_fp64_achieved": (nnz * (8 + 4) + 4 * (mdim + 1) + 2 * mdim * 8) / (hv_ms_fp64 * 1e-3) / 1e9}
