@@ -1,0 +1,204 @@
+// The problem handle behind the C ABI (shared by capi.cu and multi.cu).
+#pragma once
+#include <cstdint>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/smgpu.h"
+#include "device.cuh"
+#include "setup.h"
+
+namespace smgpu {
+
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    size_t b = sizeof(T) * (n > 0 ? n : 1);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) throw CudaError{e, "cudaMalloc", __FILE__, __LINE__};
+    ptrs.push_back(p);
+    bytes += b;
+    return (T*)p;
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    T* p = alloc<T>(v.size());
+    if (!v.empty()) SMGPU_CUDA_TRY(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return p;
+  }
+  void free_all() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+    bytes = 0;
+  }
+};
+
+template <class T>
+std::vector<float> to_f32(const std::vector<T>& v) {
+  std::vector<float> r(v.size());
+  for (size_t i = 0; i < v.size(); ++i) r[i] = (float)v[i];
+  return r;
+}
+
+}  // namespace smgpu
+
+using namespace smgpu;
+
+struct smgpu_problem {
+  int precision = SMGPU_FP64;
+  int vp = 0, vn = 0, mtot2 = 0;
+  Tables T;
+  DeviceArena tables;
+  DevTables dt{};
+  TileTables tt{};
+  CoefTables<double> c64{};
+  CoefTables<float> c32{};
+  const double* d_ep = nullptr;
+  const double* d_en = nullptr;
+  HvConfig cfg{128, 4, 0, 1};
+  std::map<int, std::pair<const int*, const int*>> task_arrays;  // rows -> (task_b, task_p0)
+  std::map<int, int> task_count;
+  cudaStream_t st = nullptr, st2 = nullptr;
+  std::string err;
+  double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double tune_ms[16] = {0};
+  int sms = 152;
+  DeviceArena solver;  // Krylov basis and scratch of the last solve
+
+  ~smgpu_problem() {
+    solver.free_all();
+    tables.free_all();
+    if (st) cudaStreamDestroy(st);
+    if (st2) cudaStreamDestroy(st2);
+  }
+
+  // Row tasks of R rows each, largest blocks first.
+  void ensure_tasks(int R) {
+    if (task_arrays.count(R)) return;
+    std::vector<int> order(T.nb);
+    for (int b = 0; b < T.nb; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return (int64_t)T.nn[x] * (T.ppn_ptr[T.pstart[x + 1]] - T.ppn_ptr[T.pstart[x]] + 1) >
+             (int64_t)T.nn[y] * (T.ppn_ptr[T.pstart[y + 1]] - T.ppn_ptr[T.pstart[y]] + 1);
+    });
+    std::vector<int> tb, tp;
+    for (int b : order)
+      for (int p0 = 0; p0 < T.np[b]; p0 += R) {
+        tb.push_back(b);
+        tp.push_back(p0);
+      }
+    task_arrays[R] = {tables.upload(tb), tables.upload(tp)};
+    task_count[R] = (int)tb.size();
+  }
+  void set_config(int nt, int R, int minb) {
+    ensure_tasks(R);
+    cfg.nt = nt;
+    cfg.rows = R;
+    cfg.minb = minb;
+    cfg.ntasks = task_count[R];
+    tt.task_b = task_arrays[R].first;
+    tt.task_p0 = task_arrays[R].second;
+  }
+
+  void upload() {
+    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    int dev = 0;
+    SMGPU_CUDA_TRY(cudaGetDevice(&dev));
+    SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int nb = T.nb;
+    dt.nb = nb;
+    dt.len_pad = T.len_pad;
+    dt.np = tables.upload(T.np);
+    dt.nn = tables.upload(T.nn);
+    dt.stride = tables.upload(T.stride);
+    dt.off_pad = tables.upload(T.off_pad);
+    dt.pstart = tables.upload(T.pstart);
+    dt.nstart = tables.upload(T.nstart);
+    dt.tdims = tables.upload(T.tdims);
+    dt.pp_ptr = tables.upload(T.pp_ptr);
+    dt.pp_col = tables.upload(T.pp_col);
+    dt.nn_ptr = tables.upload(T.nn_ptr);
+    dt.nn_col = tables.upload(T.nn_col);
+    std::vector<int4> la(T.links.size());
+    std::vector<int64_t> lv(T.links.size()), ln(T.links.size());
+    for (size_t k = 0; k < T.links.size(); ++k) {
+      la[k] = make_int4(T.links[k].s, T.links[k].nB, T.links[k].dm, 0);
+      lv[k] = 2 * T.links[k].vtab_off;  // signed (V, -V) table
+      ln[k] = T.links[k].nptr_off;
+    }
+    dt.link_a = tables.upload(la);
+    dt.link_v = tables.upload(lv);
+    dt.link_n = tables.upload(ln);
+    dt.ppn_src = tables.upload(T.ppn_src);
+    dt.ppn_meta = tables.upload(T.ppn_meta);
+    d_ep = tables.upload(T.ep);
+    d_en = tables.upload(T.en);
+    // row-tile tables: per (row, link slot) first proton entry
+    std::vector<int64_t> rl_base(nb);
+    std::vector<int> rl;
+    for (int b = 0; b < nb; ++b) {
+      rl_base[b] = (int64_t)rl.size();
+      const int lb = T.link_begin[b], nl = T.link_begin[b + 1] - lb;
+      for (int g = T.pstart[b]; g < T.pstart[b + 1]; ++g) {
+        int e = T.ppn_ptr[g];
+        for (int j = 0; j <= nl; ++j) {
+          while (e < T.ppn_ptr[g + 1] && (int)(T.ppn_meta[e] >> 16) < lb + j) ++e;
+          rl.push_back(e);
+        }
+      }
+    }
+    tt.link_begin = tables.upload(T.link_begin);
+    tt.rl_base = tables.upload(rl_base);
+    tt.rl = tables.upload(rl);
+    tt.npn_ptr = tables.upload(T.npn_ptr);
+    // neutron entries with the sign folded into the (V, -V) table index
+    std::vector<uint32_t> ent(T.npn_ent.size());
+    for (size_t li = 0; li < T.links.size(); ++li) {
+      const auto& L = T.links[li];
+      const uint32_t nab = (uint32_t)(L.nA * L.nB);
+      for (int64_t j = T.npn_ptr[L.nptr_off]; j < T.npn_ptr[L.nptr_off + T.nn[L.b]]; ++j) {
+        uint32_t e = T.npn_ent[j];
+        uint32_t col = ((e >> 1) & 0x1fffu) + ((e & 1u) ? nab : 0u);
+        if (col >= (1u << 14)) throw SetupError{SMGPU_ERR_LIMIT, "pn coefficient table too large for the packing"};
+        ent[j] = (e & ~0x3fffu) | col;
+      }
+    }
+    tt.npn_ent = tables.upload(ent);
+    // signed coefficient tables
+    std::vector<double> vt2(2 * T.vtab.size());
+    for (size_t k = 0; k + 1 < T.vtab_off_dm.size(); ++k) {
+      const int64_t o = T.vtab_off_dm[k], n = T.vtab_off_dm[k + 1] - o;
+      for (int64_t x = 0; x < n; ++x) {
+        vt2[2 * o + x] = T.vtab[o + x];
+        vt2[2 * o + n + x] = -T.vtab[o + x];
+      }
+    }
+    if (precision == SMGPU_FP64) {
+      c64.pp_val = tables.upload(T.pp_val);
+      c64.nn_val = tables.upload(T.nn_val);
+      c64.vtab = tables.upload(vt2);
+    } else {
+      c32.pp_val = tables.upload(to_f32(T.pp_val));
+      c32.nn_val = tables.upload(to_f32(T.nn_val));
+      c32.vtab = tables.upload(to_f32(vt2));
+    }
+    set_config(128, 4, 1);
+  }
+
+  void hv(const double* v, double* w, const HvEpilogue<double>& epi, cudaStream_t s) {
+    launch_hv_fp64(dt, tt, cfg, d_ep, d_en, c64, v, w, epi, s);
+  }
+  void hv(const float* v, double* w, const HvEpilogue<float>& epi, cudaStream_t s) {
+    launch_hv_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
+  }
+
+  // Time every candidate launch shape on a device vector and keep the fastest
+  // (defined in capi.cu, next to the shape-class cache).
+  void autotune();
+};
