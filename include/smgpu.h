@@ -66,7 +66,7 @@ typedef struct {
  * element from the nucleus name (util_func.jl:1,13-24; shellmodel_main.jl:
  * 95,116-117,908-916), Mtot = A mod 2 (:110), basis and jump tables
  * (occ :769-848, prep_Hamil_T1 :580-649, prep_Hamil_pn :658-730,
- * prep_pn :1139-1199) built on the GPU. */
+ * prep_pn :1139-1199), built on the host and uploaded once. */
 int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int precision, smgpu_problem** out);
 
 /* Same, from an in-memory description (the data of the reference's SMobject,
@@ -164,6 +164,62 @@ int smgpu_stats(const smgpu_problem* h, long long* stats_out);
  * the array (each call rewrites every entry it reads), so calls that overlap
  * on the GPU race; the call returns when w and *vhv are ready. */
 int smgpu_matvec_noalloc(smgpu_problem* h, const double* v, double* w, double* vhv);
+
+/* ------------------------------------------------------------------------
+ * Interaction samples sharing one basis (the sample loop of prepEC,
+ * src/ShellModel/eigenvector_continuation.jl:102-312: one snt per sample,
+ * the basis of the first, TRL per sample).  Up to 16 samples are solved
+ * together in the FP32-mixed form: one multi-sample H·V per Lanczos
+ * iteration reads the shared jump tables once for all samples; every sample
+ * keeps its own Lanczos matrix, convergence test and thick restart.
+ * Vectors on the host are sample-major: sample s at [s*mdim, (s+1)*mdim). */
+typedef struct smgpu_multi smgpu_multi;
+
+/* Read nsamples snt files (1..16) for one nucleus.  The samples must give the
+ * same valence space and the same non-zero pattern of m-scheme matrix
+ * elements (SMGPU_ERR_LIMIT otherwise).  Replaces the per-sample readsmsnt,
+ * prep_Hamil_T1, prep_Hamil_pn and prep_pn calls of prepEC (:140-153). */
+int smgpu_multi_create_from_snt(const char* const* snt_paths, int nsamples, const char* nucleus,
+                                smgpu_multi** out);
+int smgpu_multi_destroy(smgpu_multi* h);
+/* Message of the last failure on h (NULL: of the last failed create call). */
+const char* smgpu_multi_last_error(const smgpu_multi* h);
+/* mdim, number of samples, and the lane count S the kernels run with
+ * (4, 8 or 16; samples beyond nsamples are idle lanes). */
+int smgpu_multi_dims(const smgpu_multi* h, long long* mdim, int* nsamples, int* lanes);
+
+/* w_s (+)= H_s v_s for every sample s (operate_H! per sample,
+ * lanczos_methods.jl:153), host buffers of nsamples x mdim doubles. */
+int smgpu_multi_matvec(smgpu_multi* h, const double* v, double* w, int accumulate);
+
+/* TRL for the lowest num_ev eigenvalues of every sample (prepEC's per-sample
+ * TRL call, eigenvector_continuation.jl:171-177, without J projection).
+ *   lm, ls, tol, max_restarts: as smgpu_solve (one value for all samples);
+ *   v1: NULL (seeded hash draw, the same for every sample) or nsamples x mdim;
+ *   evals_out: nsamples x num_ev doubles (en[1] of each sample's last test);
+ *   evecs_out: NULL or nsamples x num_ev x mdim (Ritz vectors of the
+ *              converged samples);
+ *   stats_out: NULL or 8 + 4*nsamples ints: [multi-sample H·V launches,
+ *              restarts, all converged, num_ev written, kernel launches,
+ *              lanes, reserved, reserved], then per sample [elit, converged,
+ *              second re-orthogonalisation passes, reserved].
+ * Returns SMGPU_ERR_NOCONV when some sample has not converged after
+ * max_restarts restarts (the other samples' results are still written). */
+int smgpu_multi_solve(smgpu_multi* h, int num_ev, int lm, int ls, double tol, int max_restarts,
+                      const double* v1, double* evals_out, double* evecs_out, int* stats_out);
+
+/* Statistics (8 entries): [multiply-adds per sample per H·V, lanes, device
+ * table bytes (shared structure + interleaved coefficients), padded vector
+ * length, H·V CTAs, and the autotuned launch shape: threads per CTA, minimum
+ * CTAs per SM, neutron entries cached in registers]. */
+int smgpu_multi_stats(const smgpu_multi* h, long long* stats_out);
+
+/* As smgpu_timings, for the last create / solve / matvec call on h. */
+int smgpu_multi_timings(const smgpu_multi* h, double* times_out);
+
+/* Mean milliseconds of one multi-sample H·V launch over `reps` launches on a
+ * device-resident seeded vector (flush_l2 as smgpu_time_matvec). */
+int smgpu_multi_time_matvec(smgpu_multi* h, int reps, int flush_l2, double* ms_out);
 
 #ifdef __cplusplus
 }

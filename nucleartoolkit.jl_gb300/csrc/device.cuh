@@ -84,6 +84,26 @@ struct HvEpilogue {
   double* alpha_part;      // per-CTA partial sums of v·Hv (null: none)
 };
 
+// Coefficients of S interaction samples sharing one basis, interleaved
+// sample-innermost: value k of sample s at [k*S + s] (FP32 tables, FP64
+// one-body diagonals).
+struct MultiCoef {
+  const float* pp_val;
+  const float* nn_val;
+  const float* vtab;
+  const double* ep;
+  const double* en;
+};
+
+struct MultiEpilogue {
+  const int* all_done;      // gate: skip when set (null: always run)
+  const float* vprev;       // w_s -= beta_s * vprev_s (null: no correction)
+  const double* beta_base;  // beta_s = beta_base[s * beta_stride]
+  int beta_stride;
+  double* alpha_part;       // [s * ntasks + task] partial sums of v_s·(Hv)_s (null: none)
+  int* count;               // incremented once per executed launch (null: none)
+};
+
 #ifdef __CUDACC__
 // Exact float -> double widening with integer instructions only (sign,
 // exponent rebias by 1023-127, mantissa shift).  On this GPU the conversion
@@ -125,5 +145,16 @@ void launch_hv_fp64(const DevTables& t, const TileTables& tt, const HvConfig& cf
 void launch_hv_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
                      const double* en, const CoefTables<float>& c, const float* v, double* w,
                      const HvEpilogue<float>& epi, cudaStream_t st);
+// Multi-sample H·V (hv_multi.cu).  S in {4, 8, 16}; tt1 = one-row tasks
+// (ntasks of them); v/w interleaved; cand = index into hv_multi_candidates().
+struct MultiHvConfig {
+  int nt;    // threads per CTA
+  int minb;  // minimum resident CTAs per SM requested from the compiler
+  int km;    // neutron entries cached in registers
+};
+const MultiHvConfig* hv_multi_candidates(int* count);
+bool hv_multi_supported(int S);
+void launch_hv_multi(int S, int cand, const DevTables& t, const TileTables& tt1, int ntasks, const MultiCoef& c,
+                     const float* v, double* w, const MultiEpilogue& epi, cudaStream_t st);
 
 }  // namespace smgpu

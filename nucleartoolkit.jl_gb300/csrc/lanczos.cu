@@ -27,125 +27,13 @@
 #include <cfloat>
 
 #include "lanczos.cuh"
+#include "lanczos_dev.cuh"
 
 namespace smgpu {
 
 namespace {
-constexpr int kNT = 256;  // threads of the streaming kernels
+using namespace dev;
 
-__device__ __forceinline__ bool stopped(const LanczosFlags* fl) { return fl->done || fl->exhausted; }
-
-__device__ __forceinline__ double warp_sum(double x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  return x;
-}
-
-// Deterministic block sum, result returned to every thread.
-template <int NT>
-__device__ __forceinline__ double block_sum_all(double x, double* red) {
-  x = warp_sum(x);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[wid] = x;
-  __syncthreads();
-  double s = 0.0;
-#pragma unroll
-  for (int k = 0; k < NT / 32; ++k) s += red[k];
-  return s;
-}
-
-// Sum of n partials in a fixed order (every thread gets the same value).
-template <int NT>
-__device__ __forceinline__ double sum_partials(const double* __restrict__ p, int n, double* red) {
-  double x = 0.0;
-  for (int i = threadIdx.x; i < n; i += NT) x += p[i];
-  return block_sum_all<NT>(x, red);
-}
-
-// m sums of G partials each, one warp per sum; results into smem out[0..m).
-template <int NT>
-__device__ __forceinline__ void sum_partials_many(const double* __restrict__ p, int G, int m, double* out) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int j = wid; j < m; j += NT / 32) {
-    double x = 0.0;
-    for (int g = lane; g < G; g += 32) x += p[(int64_t)j * G + g];
-    x = warp_sum(x);
-    if (lane == 0) out[j] = x;
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ void chunk_of(int64_t len, int G, int64_t& b, int64_t& e) {
-  int64_t per = (len + G - 1) / G;
-  per = (per + 31) & ~(int64_t)31;
-  b = (int64_t)blockIdx.x * per;
-  e = b + per;
-  if (e > len) e = len;
-  if (b > len) b = len;
-}
-
-__device__ __forceinline__ int find_block(const int64_t* off, int nb, int64_t i) {
-  int lo = 0, hi = nb - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (off[mid] <= i) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
-
-// Four consecutive elements (16-byte aligned: vector lengths and chunk starts
-// are multiples of 4) widened to FP64.
-__device__ __forceinline__ void load4(const float* p, double (&o)[4]) {
-  const float4 f = *reinterpret_cast<const float4*>(p);
-  o[0] = widen(f.x);
-  o[1] = widen(f.y);
-  o[2] = widen(f.z);
-  o[3] = widen(f.w);
-}
-__device__ __forceinline__ void load4(const double* p, double (&o)[4]) {
-  const double2 a = *reinterpret_cast<const double2*>(p);
-  const double2 b = *reinterpret_cast<const double2*>(p + 2);
-  o[0] = a.x;
-  o[1] = a.y;
-  o[2] = b.x;
-  o[3] = b.y;
-}
-__device__ __forceinline__ void store4(double* p, const double (&o)[4]) {
-  *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
-  *reinterpret_cast<double2*>(p + 2) = make_double2(o[2], o[3]);
-}
-
-// Kahan-compensated FP32 sum.
-struct KahanF {
-  float s, c;
-  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
-  __device__ __forceinline__ void add(float x) {
-    float y = __fsub_rn(x, c);
-    float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
-    s = t;
-  }
-  __device__ __forceinline__ float get() const { return __fsub_rn(s, c); }
-};
-
-// Seeded start vector (replaces Random.seed!(1234); randn(mdim),
-// shellmodel_main.jl:939-948): v[M] = u0+u1+u2+u3-2 with
-// u_k = (splitmix64(seed + φ·(4M+k+1)) >> 11)·2^-53.  Integer and exactly
-// rounded double operations only, so host and device agree bit for bit.
-__device__ __forceinline__ double start_elem(uint64_t seed, int64_t i) {
-  double u[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(4 * i + k + 1);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z = z ^ (z >> 31);
-    u[k] = (double)(z >> 11) * 0x1.0p-53;
-  }
-  return __dsub_rn(__dadd_rn(__dadd_rn(u[0], u[1]), __dadd_rn(u[2], u[3])), 2.0);
-}
 
 __global__ void k_start_vector(DevTables t, uint64_t seed, double* __restrict__ w) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
@@ -413,36 +301,8 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
     vnext[i] = (TX)(w[i] * inv);
 }
 
-// ---------------------------------------------------------------------------
-// Lowest eigenvalues of the k x k Lanczos matrix by Sturm counts
-// (diagonalize_T!, lanczos_methods.jl:250-258).  After a thick restart T is
-// an arrowhead (rows 0..lock-1 diagonal, coupled to row `lock`) followed by a
-// tridiagonal tail; the LDLᵀ inertia of T - σI is evaluated in O(k) for that
-// shape.  A group of kLPE lanes bisects one eigenvalue with kLPE trial shifts
-// per step (FP64 division throughput, not latency, bounds this kernel).
-constexpr int kLPE = 4;
-
-__device__ int sturm_count(const double* a, const double* c2, const double* b2, int lock, int k, double sigma,
-                           double pivmin) {
-  int cnt = 0;
-  double acc = 0.0;
-  for (int i = 0; i < lock; ++i) {
-    double d = a[i] - sigma;
-    if (fabs(d) < pivmin) d = -pivmin;
-    if (d < 0.0) ++cnt;
-    acc += c2[i] / d;
-  }
-  double d = (a[lock] - sigma) - acc;
-  if (fabs(d) < pivmin) d = -pivmin;
-  if (d < 0.0) ++cnt;
-  for (int i = lock + 1; i < k; ++i) {
-    d = (a[i] - sigma) - b2[i - 1] / d;
-    if (fabs(d) < pivmin) d = -pivmin;
-    if (d < 0.0) ++cnt;
-  }
-  return cnt;
-}
-
+// Lowest eigenvalues (diagonalize_T!, lanczos_methods.jl:250-258): α from the
+// H·v epilogue partials, then sturm_step.
 __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
                         double tol, int64_t mdim, const double* __restrict__ alpha_part, int nalpha,
                         LanczosFlags* fl) {
@@ -452,12 +312,6 @@ __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num
     if (threadIdx.x == 0) { fl->done = 1; fl->elit = fl->exh_k; }
     return;
   }
-  extern __shared__ double sm[];
-  double* a = sm;            // k
-  double* c2 = a + lm;       // lock
-  double* b2 = c2 + lm;      // k-1
-  double* lam = b2 + lm;     // num_ev
-  __shared__ double s_lo, s_hi, s_piv;
   __shared__ double red[32];
   const int tid = threadIdx.x;
   // α of this iteration from the H·v epilogue partials
@@ -474,177 +328,15 @@ __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num
     }
     __syncthreads();
   }
-  for (int i = tid; i < k; i += blockDim.x) {
-    a[i] = T[(int64_t)i * lm + i];
-    if (i < lock) { double x = T[(int64_t)i * lm + lock]; c2[i] = x * x; }
-    if (i >= lock && i + 1 < k) { double x = T[(int64_t)i * lm + i + 1]; b2[i] = x * x; }
-  }
-  __syncthreads();
-  if (tid == 0) {
-    // Gershgorin interval and pivot floor
-    double lo = INFINITY, hi = -INFINITY, mx = 1.0;
-    for (int i = 0; i < k; ++i) {
-      double r = 0.0;
-      if (i < lock) r = sqrt(c2[i]);
-      else {
-        if (i == lock) for (int j = 0; j < lock; ++j) r += sqrt(c2[j]);
-        if (i > lock) r += sqrt(b2[i - 1]);
-        if (i + 1 < k) r += sqrt(b2[i]);
-      }
-      lo = fmin(lo, a[i] - r);
-      hi = fmax(hi, a[i] + r);
-    }
-    for (int i = 0; i < lock; ++i) mx = fmax(mx, c2[i]);
-    for (int i = lock; i + 1 < k; ++i) mx = fmax(mx, b2[i]);
-    double w = hi - lo;
-    s_lo = lo - 1e-3 * w - 1e-300;
-    s_hi = hi + 1e-3 * w + 1e-300;
-    s_piv = DBL_MIN * mx;
-  }
-  __syncthreads();
-  const int n = min(num_ev, k);
-  const int lane = tid & 31;
-  const int grp = tid / kLPE, sub = tid % kLPE, ngrp = blockDim.x / kLPE;
-  const unsigned gmask = ((1u << kLPE) - 1u) << (lane & ~(kLPE - 1));
-  for (int e0 = 0; e0 < n; e0 += ngrp) {
-    const int e = e0 + grp;
-    const bool live = e < n;
-    double lo = s_lo, hi = s_hi;
-    for (int step = 0; step < 200; ++step) {
-      const double sigma = lo + (hi - lo) * (double)(sub + 1) * (1.0 / (kLPE + 1));
-      const int cnt = live ? sturm_count(a, c2, b2, lock, k, sigma, s_piv) : 0;
-      const unsigned le = __ballot_sync(0xffffffffu, cnt <= e) & gmask;
-      const unsigned ge = __ballot_sync(0xffffffffu, cnt >= e + 1) & gmask;
-      const double s_le = __shfl_sync(0xffffffffu, sigma, le ? 31 - __clz(le) : lane);
-      const double s_ge = __shfl_sync(0xffffffffu, sigma, ge ? __ffs(ge) - 1 : lane);
-      if (le) lo = s_le;
-      if (ge) hi = s_ge;
-      const bool fin = !live || (hi - lo <= 4.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + 1e-300);
-      if (__all_sync(0xffffffffu, fin)) break;
-    }
-    if (live && sub == 0) lam[e] = 0.5 * (lo + hi);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    for (int hh = nh - 1; hh >= 1; --hh)
-      for (int j = 0; j < num_ev; ++j) en[hh * num_ev + j] = en[(hh - 1) * num_ev + j];
-    for (int j = 0; j < n; ++j) en[j] = lam[j];
-    bool conv = true;
-    for (int j = 0; j < num_ev; ++j)
-      if (!(en[num_ev + j] - en[j] < tol)) conv = false;
-    if (conv || (int64_t)k == mdim || (fl->exhausted && k == fl->exh_k)) {
-      fl->done = 1;
-      fl->elit = k;
-    }
-  }
+  sturm_step(T, lm, k, lock, num_ev, en, nh, tol, mdim, fl);
 }
 
-// ---------------------------------------------------------------------------
-// Symmetric eigen-decomposition of T[0:n,0:n] by parallel cyclic Jacobi
-// (round-robin pairing, n/2 disjoint rotations per round) in one CTA.
-// Output: evals ascending, A = eigenvectors (column-major, ld n).
+// Eigenvectors of T[0:n,0:n] (ThickRestart / Ritz vectors), gated on the flags.
 template <int NT>
 __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int ldt, int n, double* A, double* Z,
                                                double* evals, const LanczosFlags* fl, int gate) {
   if (gate && stopped(fl)) return;
-  __shared__ double red[NT / 32];
-  __shared__ int s_stop;
-  extern __shared__ double shj[];
-  const int N = n + (n & 1);
-  const int npair = N / 2;
-  double* cc = shj;
-  double* ss = cc + npair;
-  double* dg = ss + npair;
-  int* pp = (int*)(dg + N);
-  int* qq = pp + npair;
-  const int tid = threadIdx.x;
-  for (int idx = tid; idx < n * n; idx += NT) {
-    int i = idx % n, j = idx / n;
-    A[idx] = T[(int64_t)j * ldt + i];
-    Z[idx] = (i == j) ? 1.0 : 0.0;
-  }
-  __syncthreads();
-  double fro = 0.0;
-  for (int idx = tid; idx < n * n; idx += NT) fro += A[idx] * A[idx];
-  fro = block_sum_all<NT>(fro, red);
-  for (int sweep = 0; sweep < 64; ++sweep) {
-    double off = 0.0;
-    for (int idx = tid; idx < n * n; idx += NT) {
-      int i = idx % n, j = idx / n;
-      if (i < j) off += A[idx] * A[idx];
-    }
-    off = block_sum_all<NT>(off, red);
-    if (tid == 0) s_stop = (off <= 1e-34 * fro || off == 0.0) ? 1 : 0;
-    __syncthreads();
-    if (s_stop) break;
-    for (int r = 0; r < N - 1; ++r) {
-      for (int k = tid; k < npair; k += NT) {
-        int p, q;
-        if (k == 0) { p = N - 1; q = r; }
-        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
-        if (p > q) { int x = p; p = q; q = x; }
-        double c = 1.0, s = 0.0;
-        if (q < n) {
-          double apq = A[(int64_t)q * n + p];
-          if (apq != 0.0) {
-            double app = A[(int64_t)p * n + p], aqq = A[(int64_t)q * n + q];
-            double theta = (aqq - app) / (2.0 * apq);
-            double t = (fabs(theta) > 1e150) ? 0.5 / theta
-                                              : (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
-            c = 1.0 / sqrt(1.0 + t * t);
-            s = t * c;
-          }
-        }
-        pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = s;
-      }
-      __syncthreads();
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        int k = idx / n, i = idx % n;
-        if (ss[k] == 0.0) continue;
-        int p = pp[k], q = qq[k];
-        double c = cc[k], s = ss[k];
-        double aip = A[(int64_t)p * n + i], aiq = A[(int64_t)q * n + i];
-        A[(int64_t)p * n + i] = c * aip - s * aiq;
-        A[(int64_t)q * n + i] = s * aip + c * aiq;
-      }
-      __syncthreads();
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        int k = idx / n, j = idx % n;
-        if (ss[k] == 0.0) continue;
-        int p = pp[k], q = qq[k];
-        double c = cc[k], s = ss[k];
-        double apj = A[(int64_t)j * n + p], aqj = A[(int64_t)j * n + q];
-        A[(int64_t)j * n + p] = c * apj - s * aqj;
-        A[(int64_t)j * n + q] = s * apj + c * aqj;
-      }
-      __syncthreads();
-      for (int k = tid; k < npair; k += NT)
-        if (ss[k] != 0.0) {
-          A[(int64_t)qq[k] * n + pp[k]] = 0.0;
-          A[(int64_t)pp[k] * n + qq[k]] = 0.0;
-        }
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        int k = idx / n, i = idx % n;
-        if (ss[k] == 0.0) continue;
-        int p = pp[k], q = qq[k];
-        double c = cc[k], s = ss[k];
-        double zip = Z[(int64_t)p * n + i], ziq = Z[(int64_t)q * n + i];
-        Z[(int64_t)p * n + i] = c * zip - s * ziq;
-        Z[(int64_t)q * n + i] = s * zip + c * ziq;
-      }
-      __syncthreads();
-    }
-  }
-  for (int i = tid; i < n; i += NT) dg[i] = A[(int64_t)i * n + i];
-  __syncthreads();
-  for (int i = tid; i < n; i += NT) {
-    double d = dg[i];
-    int rank = 0;
-    for (int j = 0; j < n; ++j)
-      if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
-    evals[rank] = d;
-    for (int r = 0; r < n; ++r) A[(int64_t)rank * n + r] = Z[(int64_t)i * n + r];
-  }
+  jacobi_eig<NT>(T, ldt, n, A, Z, evals);
 }
 
 // ThickRestart's small part (lanczos_methods.jl:261-271): new arrowhead T.
@@ -705,36 +397,6 @@ __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V
           if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q];
       }
     }
-  }
-}
-
-// Double-float accumulator: exact FP32 products (two-product by FMA) summed
-// with TwoSum into an unevaluated (hi, lo) pair — about 2^-48 relative, on
-// the FP32 pipe.  Used for the restart Gram matrix of FP32-stored vectors.
-struct DFAcc {
-  float hi, lo;
-  __device__ __forceinline__ void init() { hi = 0.f; lo = 0.f; }
-  __device__ __forceinline__ void add_prod(float a, float b) {
-    const float p = __fmul_rn(a, b);
-    const float e = __fmaf_rn(a, b, -p);
-    const float s = __fadd_rn(hi, p);
-    const float bb = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(err, e));
-  }
-  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
-};
-
-__device__ __forceinline__ void gram_pair(int pr, int ls, int& k, int& l) {
-  if (pr < ls * (ls + 1) / 2) {
-    k = 0;
-    int rem = pr;
-    while (rem >= ls - k) { rem -= ls - k; ++k; }
-    l = k + rem;
-  } else {
-    k = pr - ls * (ls + 1) / 2;
-    l = ls;  // v_last
   }
 }
 

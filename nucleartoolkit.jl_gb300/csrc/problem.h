@@ -45,6 +45,20 @@ std::vector<float> to_f32(const std::vector<T>& v) {
   return r;
 }
 
+// Per ΔM, the pn table [nA][nB] followed by its negation (the kernels fold
+// the neutron sign into the column index).
+inline std::vector<double> signed_vtab(const Tables& T) {
+  std::vector<double> vt2(2 * T.vtab.size());
+  for (size_t k = 0; k + 1 < T.vtab_off_dm.size(); ++k) {
+    const int64_t o = T.vtab_off_dm[k], n = T.vtab_off_dm[k + 1] - o;
+    for (int64_t x = 0; x < n; ++x) {
+      vt2[2 * o + x] = T.vtab[o + x];
+      vt2[2 * o + n + x] = -T.vtab[o + x];
+    }
+  }
+  return vt2;
+}
+
 }  // namespace smgpu
 
 using namespace smgpu;
@@ -171,14 +185,7 @@ struct smgpu_problem {
     }
     tt.npn_ent = tables.upload(ent);
     // signed coefficient tables
-    std::vector<double> vt2(2 * T.vtab.size());
-    for (size_t k = 0; k + 1 < T.vtab_off_dm.size(); ++k) {
-      const int64_t o = T.vtab_off_dm[k], n = T.vtab_off_dm[k + 1] - o;
-      for (int64_t x = 0; x < n; ++x) {
-        vt2[2 * o + x] = T.vtab[o + x];
-        vt2[2 * o + n + x] = -T.vtab[o + x];
-      }
-    }
+    const std::vector<double> vt2 = signed_vtab(T);
     if (precision == SMGPU_FP64) {
       c64.pp_val = tables.upload(T.pp_val);
       c64.nn_val = tables.upload(T.nn_val);

@@ -41,6 +41,15 @@ SIGNATURES = {
     "smgpu_stats": (C.c_int, [_vp, _vp]),
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "smgpu_matvec_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "smgpu_multi_create_from_snt": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.c_char_p, C.POINTER(_vp)]),
+    "smgpu_multi_destroy": (C.c_int, [_vp]),
+    "smgpu_multi_last_error": (C.c_char_p, [_vp]),
+    "smgpu_multi_dims": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "smgpu_multi_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "smgpu_multi_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
+    "smgpu_multi_stats": (C.c_int, [_vp, _vp]),
+    "smgpu_multi_timings": (C.c_int, [_vp, _vp]),
+    "smgpu_multi_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -78,4 +87,11 @@ def load(build_if_missing: bool = True):
 def check(code: int, handle=None):
     if code != OK:
         msg = load().smgpu_last_error(handle)
+        raise SmgpuError(code, (msg or b"").decode(errors="replace"))
+
+
+def check_multi(code: int, handle=None):
+    """check() for smgpu_multi handles."""
+    if code != OK:
+        msg = load().smgpu_multi_last_error(handle)
         raise SmgpuError(code, (msg or b"").decode(errors="replace"))

@@ -111,6 +111,82 @@ class ShellModelProblem:
                     kernel_launches=int(stats[6]), status=rc)
 
 
+class MultiSampleProblem:
+    """Interaction samples sharing one basis, solved together (an
+    ``smgpu_multi`` handle): the sample loop of the reference's ``prepEC``
+    (src/ShellModel/eigenvector_continuation.jl:140-177) with one
+    multi-sample H·V per Lanczos iteration, FP32-mixed."""
+
+    def __init__(self, snt_files, target_nuc: str):
+        L = load()
+        files = [os.fsencode(f) for f in snt_files]
+        arr = (C.c_char_p * len(files))(*files)
+        h = C.c_void_p()
+        rc = L.smgpu_multi_create_from_snt(arr, len(files), target_nuc.encode(), C.byref(h))
+        _lib.check_multi(rc, None)
+        self._h = h
+        md, ns, lanes = C.c_longlong(), C.c_int(), C.c_int()
+        _lib.check_multi(L.smgpu_multi_dims(h, C.byref(md), C.byref(ns), C.byref(lanes)), h)
+        self.mdim = int(md.value)
+        self.nsamples = int(ns.value)
+        self.lanes = int(lanes.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().smgpu_multi_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def stats(self):
+        s = np.zeros(8, dtype=np.int64)
+        _lib.check_multi(load().smgpu_multi_stats(self._h, _p(s)), self._h)
+        keys = ["updates", "lanes", "table_bytes", "len_pad", "hv_ctas", "hv_threads", "hv_min_ctas", "hv_entry_cache"]
+        return dict(zip(keys, map(int, s)))
+
+    def timings(self):
+        t = np.zeros(8)
+        _lib.check_multi(load().smgpu_multi_timings(self._h, _p(t)), self._h)
+        keys = ["setup", "lanczos", "matvec", "capture", "ritz", "solve_wall", "r6", "r7"]
+        return dict(zip(keys, map(float, t)))
+
+    def time_matvec(self, reps=20, flush_l2=True):
+        """Mean ms per multi-sample H·V launch (all samples), CUDA events."""
+        ms = C.c_double()
+        _lib.check_multi(load().smgpu_multi_time_matvec(self._h, int(reps), 1 if flush_l2 else 0, C.byref(ms)),
+                         self._h)
+        return float(ms.value)
+
+    def matvec(self, v, accumulate: bool = False, out=None):
+        """w_s = H_s v_s; v has shape (nsamples, mdim)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if v.shape != (self.nsamples, self.mdim):
+            raise ValueError(f"v must have shape {(self.nsamples, self.mdim)}")
+        w = np.zeros_like(v) if out is None else out
+        _lib.check_multi(load().smgpu_multi_matvec(self._h, _p(v), _p(w), 1 if accumulate else 0), self._h)
+        return w
+
+    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False):
+        nev = min(num_ev, self.mdim)
+        ev = np.zeros((self.nsamples, nev))
+        vecs = np.zeros((self.nsamples, nev, self.mdim)) if want_vecs else None
+        stats = np.zeros(8 + 4 * self.nsamples, dtype=np.int32)
+        v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
+        rc = load().smgpu_multi_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts),
+                                      _p(v1a), _p(ev), _p(vecs), _p(stats))
+        if rc not in (_lib.OK, _lib.ERR_NOCONV):
+            _lib.check_multi(rc, self._h)
+        per = stats[8:].reshape(self.nsamples, 4)
+        return dict(evals=ev, evecs=vecs, n_matvec=int(stats[0]), n_restart=int(stats[1]),
+                    converged=bool(stats[2]) and rc == _lib.OK, kernel_launches=int(stats[4]),
+                    lanes=int(stats[5]), elit=per[:, 0].astype(int), sample_converged=per[:, 1].astype(bool),
+                    n_second_pass=per[:, 2].astype(int), status=rc)
+
+
 def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=False, is_show=False,
             num_history=3, lm=300, ls=20, tol=1.0e-8, in_wf="", mdimmode=False, print_evec=False,
             calc_moment=False, calc_entropy=False, visualize_occ=False, gfactors=(1.0, 0.0, 5.586, -3.826),

@@ -142,11 +142,18 @@ def config_snt(dirpath: str, name: str):
     raise KeyError(name)
 
 
+def multi_snts(dirpath: str, shell: str, vp: int, vn: int, nsamples: int, base_seed: int, base_sigma: float,
+               sigma: float, prefix: str):
+    """Interaction samples sharing one basis: a base draw N(0, base_sigma²)
+    plus a per-sample perturbation N(0, sigma²); sample s uses seed
+    base_seed+1+s."""
+    return [write_snt(os.path.join(dirpath, f"{prefix}_{s:02d}.snt"), shell, base_seed + 1 + s, vp, vn,
+                      sigma=sigma, base_seed=base_seed, base_sigma=base_sigma) for s in range(nsamples)]
+
+
 def pf_multi_snts(dirpath: str, nsamples: int = 16):
     """The 16 pf samples sharing the 48Cr basis: base N(0,1²) + N(0,0.1²)."""
-    base = CONFIG_SEEDS["pf_multi_base"]
-    return [write_snt(os.path.join(dirpath, f"pf_multi_{s:02d}.snt"), "pf", base + 1 + s, 4, 4,
-                      sigma=0.1, base_seed=base, base_sigma=1.0) for s in range(nsamples)]
+    return multi_snts(dirpath, "pf", 4, 4, nsamples, CONFIG_SEEDS["pf_multi_base"], 1.0, 0.1, "pf_multi")
 
 
 def sd_batch_problems(nprob: int = 128):

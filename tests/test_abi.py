@@ -42,6 +42,23 @@ def test_create_without_gpu_fails_loudly():
     assert "no CUDA device" in str(ei.value)
 
 
+def test_multi_create_without_gpu_fails_loudly():
+    from smgpu import MultiSampleProblem, SmgpuError
+    from smgpu import _lib
+    ck = os.path.join(ROOT, "tests", "golden", "ckpot.snt")
+    with pytest.raises(SmgpuError) as ei:
+        MultiSampleProblem([ck, ck], "Be8")
+    assert ei.value.code == _lib.ERR_CUDA
+    assert "no CUDA device" in str(ei.value)
+    # argument checks come before any device work
+    with pytest.raises(SmgpuError) as ei:
+        MultiSampleProblem([ck] * 17, "Be8")
+    assert ei.value.code == _lib.ERR_LIMIT
+    with pytest.raises(SmgpuError) as ei:
+        MultiSampleProblem([], "Be8")
+    assert ei.value.code == _lib.ERR_ARG
+
+
 def test_main_sm_keeps_reference_signature():
     """shellmodel_main.jl:89-92 argument names."""
     from smgpu import main_sm
