@@ -221,6 +221,64 @@ int smgpu_multi_timings(const smgpu_multi* h, double* times_out);
  * device-resident seeded vector (flush_l2 as smgpu_time_matvec). */
 int smgpu_multi_time_matvec(smgpu_multi* h, int reps, int flush_l2, double* ms_out);
 
+/* ------------------------------------------------------------------------
+ * Batches of independent problems (many main_sm calls,
+ * src/ShellModel/shellmodel_main.jl:89-281, each with its own snt file and
+ * nucleus, so each its own basis and dimension).  The batch is solved in the
+ * FP32-mixed form with every launch covering all problems: one H·v launch
+ * over the row tiles of every problem, the re-orthogonalisation over chunks
+ * of the concatenated vectors, one CTA per problem for the small kernels;
+ * the H·v launch shape is autotuned on the whole batch.  Host vectors are
+ * the problems' vectors (reference basis order) concatenated in problem
+ * order: problem p at [moff_p, moff_p + mdim_p), moff_p = sum of the earlier
+ * problems' dimensions. */
+typedef struct smgpu_batch smgpu_batch;
+
+/* nprob (1..4096) snt files and nuclei; problem p is main_sm's set-up of
+ * (snt_paths[p], nuclei[p]) for target_J = [] (readsmsnt, occ, prep_Hamil_T1,
+ * prep_Hamil_pn, prep_pn: shellmodel_main.jl:95-147). */
+int smgpu_batch_create_from_snt(const char* const* snt_paths, const char* const* nuclei, int nprob,
+                                smgpu_batch** out);
+int smgpu_batch_destroy(smgpu_batch* h);
+const char* smgpu_batch_last_error(const smgpu_batch* h);
+/* Sum of the dimensions, number of problems, and (NULL or nprob entries) the
+ * dimension of every problem. */
+int smgpu_batch_dims(const smgpu_batch* h, long long* total_mdim, int* nprob, long long* mdims);
+
+/* w (+)= H_p v_p for every problem (operate_H!, lanczos_methods.jl:153), host
+ * buffers of total_mdim doubles (concatenated problem vectors). */
+int smgpu_batch_matvec(smgpu_batch* h, const double* v, double* w, int accumulate);
+
+/* TRL for the lowest num_ev eigenvalues of every problem (lanczos_methods.jl:
+ * 1-91 with diagonalize_T!/ThickRestart, :250-307), all problems together.
+ *   lm, ls, tol, max_restarts: as smgpu_solve (one value for all problems);
+ *   v1: NULL (seeded hash draw per problem) or total_mdim doubles;
+ *   evals_out: nprob x num_ev doubles; problem p's entries beyond
+ *              min(num_ev, mdim_p) are NaN;
+ *   evecs_out: NULL or num_ev x total_mdim doubles: problem p's Ritz vectors
+ *              at [num_ev*moff_p, num_ev*(moff_p + mdim_p)), one mdim_p run
+ *              per eigenvalue (zeros for unconverged problems);
+ *   stats_out: NULL or 8 + 4*nprob ints: [batched H·v launches, restarts, all
+ *              converged, num_ev, kernel launches, problems, chunks, H·v
+ *              tasks], then per problem [elit, converged, second
+ *              re-orthogonalisation passes, reserved].
+ * Returns SMGPU_ERR_NOCONV when some problem has not converged after
+ * max_restarts restarts (the results of all problems are still written). */
+int smgpu_batch_solve(smgpu_batch* h, int num_ev, int lm, int ls, double tol, int max_restarts,
+                      const double* v1, double* evals_out, double* evecs_out, int* stats_out);
+
+/* Statistics (8 entries): [multiply-adds per batched H·v, problems, chunks,
+ * H·v tasks, and the autotuned launch shape: threads per CTA, rows per CTA,
+ * minimum CTAs per SM; device table bytes]. */
+int smgpu_batch_stats(const smgpu_batch* h, long long* stats_out);
+
+/* As smgpu_timings, for the last create / solve / matvec call on h. */
+int smgpu_batch_timings(const smgpu_batch* h, double* times_out);
+
+/* Mean milliseconds of one batched H·v launch (all problems) over `reps`
+ * launches on a device-resident seeded vector (flush_l2 as smgpu_time_matvec). */
+int smgpu_batch_time_matvec(smgpu_batch* h, int reps, int flush_l2, double* ms_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,93 @@
+// Batched thick-restart Lanczos: many independent shell-model problems of
+// uneven dimension (each its own basis, tables and interaction) iterated in
+// lockstep, FP32-mixed.  Every launch covers the whole batch: the H·v over
+// the union of all problems' row tiles, the re-orthogonalisation over
+// fixed-size chunks of the concatenated vectors (a chunk never crosses a
+// problem), and the small per-problem kernels with one CTA per problem.
+// A converged problem is frozen while the others continue.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "device.cuh"
+#include "hv_tile.cuh"
+
+namespace smgpu {
+
+struct BatchProblemDev {
+  HvArgs<float, float> a;  // tables and coefficients (vector fields unused)
+  int64_t voff;            // offset of the problem's padded vector in the batch vector
+  int64_t len;             // padded length (multiple of 4)
+  int64_t mdim;
+  int64_t moff;            // offset of the problem's unpadded vector in a concatenation of all problems
+  int slot0, nslots;       // H·v tasks (α partial slots) of this problem
+  int chunk0, nchunks;     // streaming chunks of this problem
+};
+
+struct BatchCtl {
+  int all_done;  // every problem has converged
+  int ndone;
+  int pad0, pad1;
+};
+
+struct BatchDev {
+  int nprob, lm, ls, num_ev, nh;
+  double tol;
+  int nchunks;        // chunks of the batch vector
+  int nslots;         // H·v tasks
+  int64_t LEN;        // batch vector length (slot stride of V and U)
+  const BatchProblemDev* probs;
+  const int4* chunks; // (problem, begin, end, -), local element indices, begin a multiple of 4
+  double* T;          // nprob x lm x lm
+  double* en;         // nprob x nh x num_ev
+  double* alpha_part; // lm x nslots
+  double* pdot;       // (lm+2) x nchunks
+  double* pn1;        // nchunks
+  double* pdot2;      // (lm+2) x nchunks
+  double* pn2;        // nchunks
+  double* part;       // gram pairs x nchunks
+  double* jacA;       // nprob x lm x lm
+  double* jacZ;
+  double* evals;      // nprob x lm
+  float* Yf;          // nprob x (lm-1) x ls
+  double* X;          // nprob x ls x ls
+  float* Xf;          // nprob x (ls*ls + ls)
+  double* cvec;       // nprob x ls
+  LanczosFlags* fl;   // nprob
+  BatchCtl* ctl;
+};
+
+// H·v epilogue of a batched launch.
+struct BatchEpi {
+  const BatchCtl* ctl;       // gate (null: always run)
+  const LanczosFlags* fl;    // per-problem gate (null: none)
+  const float* vprev;        // batch vector of the previous Lanczos vector (null: no correction)
+  const double* T;           // β_p = T[p*lm*lm + (it0-1)*lm + it0]
+  int lm, it0;
+  double* alpha_part;        // indexed by task slot (null: none)
+  int* count;                // incremented once per launch while some problem runs (null: none)
+};
+
+struct BatchHvConfig {
+  int nt, rows, minb;
+};
+const BatchHvConfig* hv_batch_candidates(int* count);
+// tasks: (problem, block, first row, α slot), cand: index into hv_batch_candidates()
+void launch_hv_batch(int cand, const BatchProblemDev* probs, const int4* tasks, int ntasks, const float* v, double* w,
+                     const BatchEpi& epi, cudaStream_t st);
+
+void launch_b_start(const BatchDev& B, uint64_t seed, double* w, cudaStream_t st);
+void launch_b_to_padded(const BatchDev& B, const double* src, double* w, cudaStream_t st);  // src: problems' mdim concatenated
+void launch_b_from_padded(const BatchDev& B, const double* w, double* dst, cudaStream_t st);
+void launch_b_convert(const BatchDev& B, const double* w, float* v, cudaStream_t st);
+void launch_b_init(const BatchDev& B, const double* w, float* V0, cudaStream_t st);
+void launch_b_sturm(const BatchDev& B, int k, int lock, cudaStream_t st);
+void launch_b_orth(const BatchDev& B, float* V, double* w, int it0, cudaStream_t st);
+void launch_b_cycle_end(const BatchDev& B, cudaStream_t st);
+void launch_b_restart(const BatchDev& B, float* V, float* U, cudaStream_t st);
+// Ritz vectors of problem p: Jacobi of its T[0:n,0:n], then R (nev x len, FP64, padded)
+void launch_b_jacobi_one(const BatchDev& B, int p, int n, cudaStream_t st);
+void launch_b_ritz(const BatchDev& B, const float* V, int p, int elit, int nev, int64_t len, double* R,
+                   cudaStream_t st);
+
+}  // namespace smgpu

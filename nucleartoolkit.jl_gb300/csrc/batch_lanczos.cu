@@ -1,0 +1,606 @@
+// Batched thick-restart Lanczos kernels (batch.cuh).  Per problem the
+// algorithm and the kernel sequence are those of lanczos.cu — TRL
+// (src/ShellModel/lanczos_methods.jl:1-91), diagonalize_T! (:250-258),
+// ThickRestart (:260-307), ReORTH (shellmodel_main.jl:1005-1012) — for a
+// whole batch of independent problems per launch:
+//   * streaming kernels run one CTA per chunk of the concatenated vectors
+//     (a chunk lies inside one problem) and write per-chunk partial sums;
+//     every consumer sums the partials of its own problem in a fixed order,
+//     so all CTAs of a problem agree bit for bit, as in lanczos.cu;
+//   * small kernels (eigenvalue test, Jacobi, restart matrices, Cholesky)
+//     run one CTA per problem.
+// FP32 Krylov vectors, FP64 dot products, recurrences and small
+// eigenproblems; FP32 Kahan sums for the restart rotation (the mixed form of
+// lanczos.cu).
+#include "batch.cuh"
+#include "lanczos_dev.cuh"
+
+namespace smgpu {
+
+namespace {
+using namespace dev;
+
+__device__ __forceinline__ void problem_finished(BatchCtl* ctl, int nprob) {
+  if (atomicAdd(&ctl->ndone, 1) == nprob - 1) atomicExch(&ctl->all_done, 1);
+}
+
+// m sums out[j] = Σ_{q<n} p[j*stride + q], one warp per sum, into smem.
+template <int NT>
+__device__ __forceinline__ void sum_many_strided(const double* __restrict__ p, int64_t stride, int n, int m,
+                                                 double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < m; j += NT / 32) {
+    double x = 0.0;
+    for (int q = lane; q < n; q += 32) x += p[(int64_t)j * stride + q];
+    x = warp_sum(x);
+    if (lane == 0) out[j] = x;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ vectors
+__global__ void __launch_bounds__(kNT) k_b_start(const BatchDev B, uint64_t seed, double* __restrict__ w) {
+  const int4 ch = B.chunks[blockIdx.x];
+  const BatchProblemDev& P = B.probs[ch.x];
+  const DevTables& t = P.a.t;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    const int b = find_block(t.off_pad, t.nb, i);
+    const int64_t loc = i - t.off_pad[b];
+    const int st = t.stride[b];
+    const int p = (int)(loc / st), n = (int)(loc % st);
+    w[P.voff + i] = (n < t.nn[b]) ? start_elem(seed, t.tdims[b] + (int64_t)p * t.nn[b] + n) : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_b_to_padded(const BatchDev B, const double* __restrict__ src,
+                                                     double* __restrict__ w) {
+  const int4 ch = B.chunks[blockIdx.x];
+  const BatchProblemDev& P = B.probs[ch.x];
+  const DevTables& t = P.a.t;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    const int b = find_block(t.off_pad, t.nb, i);
+    const int64_t loc = i - t.off_pad[b];
+    const int st = t.stride[b];
+    const int p = (int)(loc / st), n = (int)(loc % st);
+    w[P.voff + i] = (n < t.nn[b]) ? src[P.moff + t.tdims[b] + (int64_t)p * t.nn[b] + n] : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_b_from_padded(const BatchDev B, const double* __restrict__ w,
+                                                       double* __restrict__ dst) {
+  const int4 ch = B.chunks[blockIdx.x];
+  const BatchProblemDev& P = B.probs[ch.x];
+  const DevTables& t = P.a.t;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    const int b = find_block(t.off_pad, t.nb, i);
+    const int64_t loc = i - t.off_pad[b];
+    const int st = t.stride[b];
+    const int p = (int)(loc / st), n = (int)(loc % st);
+    if (n < t.nn[b]) dst[P.moff + t.tdims[b] + (int64_t)p * t.nn[b] + n] = w[P.voff + i];
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_b_convert(const double* __restrict__ w, float* __restrict__ v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kNT) v[i] = (float)w[i];
+}
+
+// pn1[c] = ||w chunk||²
+__global__ void __launch_bounds__(kNT) k_b_selfdot(const BatchDev B, const double* __restrict__ w) {
+  __shared__ double red[kNT / 32];
+  const int4 ch = B.chunks[blockIdx.x];
+  const double* wb = w + B.probs[ch.x].voff;
+  double x = 0.0;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) x = fma(wb[i], wb[i], x);
+  x = block_sum_all<kNT>(x, red);
+  if (threadIdx.x == 0) B.pn1[blockIdx.x] = x;
+}
+
+__global__ void __launch_bounds__(kNT) k_b_init_scale(const BatchDev B, const double* __restrict__ w,
+                                                      float* __restrict__ v) {
+  __shared__ double red[kNT / 32];
+  const int4 ch = B.chunks[blockIdx.x];
+  const BatchProblemDev& P = B.probs[ch.x];
+  const double inv = 1.0 / sqrt(sum_partials<kNT>(B.pn1 + P.chunk0, P.nchunks, red));
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) v[P.voff + i] = (float)(w[P.voff + i] * inv);
+}
+
+// ------------------------------------------------------------ one iteration
+// α (from the H·v partials of the problem), w' = w − α v_k, partials of
+// v_j·w' (j <= it0) and of ||w'||² (slot it0+1).
+__global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const float* __restrict__ V, double* w,
+                                                    int it0) {
+  const int c = blockIdx.x;
+  const int4 ch = B.chunks[c];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  __shared__ double red[kNT / 32];
+  const double alpha = sum_partials<kNT>(B.alpha_part + (int64_t)it0 * B.nslots + P.slot0, P.nslots, red);
+  const float* __restrict__ Vb = V + P.voff;
+  const float* __restrict__ vk = Vb + (int64_t)it0 * B.LEN;
+  double* wb = w + P.voff;
+  const int m = it0 + 1;
+  for (int j0 = 0; j0 <= m; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+      double wv[4];
+      load4(wb + i, wv);
+      if (j0 == 0) {
+        double x[4];
+        load4(vk + i, x);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
+        store4(wb + i, wv);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = j0 + q;
+        if (j < m) {
+          double x[4];
+          load4(Vb + (int64_t)j * B.LEN + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+        } else if (j == m) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q > m) break;
+      const double s = block_sum_all<kNT>(acc[q], red);
+      if (threadIdx.x == 0) B.pdot[(int64_t)(j0 + q) * B.nchunks + c] = s;
+    }
+  }
+}
+
+// Second-pass decision of the problem, identical in all its CTAs.
+__device__ __forceinline__ bool b_need_second(const BatchDev& B, const BatchProblemDev& P, int m, double* red) {
+  const double n0 = sum_partials<kNT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
+  const double n1 = sum_partials<kNT>(B.pn1 + P.chunk0, P.nchunks, red);
+  return n1 < 0.5 * n0;
+}
+
+// w -= Σ_j h_j V_j over the chunk; pout[c] = ||w chunk||².
+__device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblemDev& P, const int4 ch,
+                                           const float* __restrict__ V, double* w, int m,
+                                           const double* __restrict__ ph, double* __restrict__ pout, double* hs,
+                                           double* red) {
+  sum_many_strided<kNT>(ph + P.chunk0, B.nchunks, P.nchunks, m, hs);
+  const float* __restrict__ Vb = V + P.voff;
+  double* wb = w + P.voff;
+  double nrm = 0.0;
+  for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+    double t[4];
+    load4(wb + i, t);
+    for (int j = 0; j < m; ++j) {
+      double x[4];
+      load4(Vb + (int64_t)j * B.LEN + i, x);
+      const double hj = hs[j];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+    }
+    store4(wb + i, t);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
+  }
+  const double s = block_sum_all<kNT>(nrm, red);
+  if (threadIdx.x == 0) pout[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kNT) k_b_orth_axpy(const BatchDev B, const float* __restrict__ V, double* w,
+                                                     int it0) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  extern __shared__ double hs[];
+  __shared__ double red[kNT / 32];
+  b_subtract(B, B.probs[ch.x], ch, V, w, it0 + 1, B.pdot, B.pn1, hs, red);
+}
+
+__global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const float* __restrict__ V,
+                                                     const double* __restrict__ w, int it0) {
+  const int c = blockIdx.x;
+  const int4 ch = B.chunks[c];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  if (!b_need_second(B, P, m, red)) return;
+  const float* __restrict__ Vb = V + P.voff;
+  const double* wb = w + P.voff;
+  for (int j0 = 0; j0 < m; j0 += 8) {
+    double acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+      double wv[4];
+      load4(wb + i, wv);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (j0 + q < m) {
+          double x[4];
+          load4(Vb + (int64_t)(j0 + q) * B.LEN + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q >= m) break;
+      const double s = block_sum_all<kNT>(acc[q], red);
+      if (threadIdx.x == 0) B.pdot2[(int64_t)(j0 + q) * B.nchunks + c] = s;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_b_orth_axpy2(const BatchDev B, const float* __restrict__ V, double* w,
+                                                      int it0) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  extern __shared__ double hs[];
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  if (!b_need_second(B, P, m, red)) return;
+  b_subtract(B, P, ch, V, w, m, B.pdot2, B.pn2, hs, red);
+}
+
+// β = ||w||, T entries (by the problem's first CTA), v_{it0+1} = w/β.
+__global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V, const double* __restrict__ w,
+                                                      int it0) {
+  const int c = blockIdx.x;
+  const int4 ch = B.chunks[c];
+  LanczosFlags* f = B.fl + ch.x;
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(f)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  __shared__ double red[kNT / 32];
+  const int m = it0 + 1;
+  const bool second = b_need_second(B, P, m, red);
+  const double nrm = sum_partials<kNT>((second ? B.pn2 : B.pn1) + P.chunk0, P.nchunks, red);
+  const double beta = sqrt(nrm);
+  const bool ok = (beta > 0.0) && (beta < INFINITY);
+  if (c == P.chunk0 && threadIdx.x == 0) {
+    double* T = B.T + (int64_t)ch.x * B.lm * B.lm;
+    if (ok) {
+      T[(int64_t)it0 * B.lm + it0 + 1] = beta;
+      T[(int64_t)(it0 + 1) * B.lm + it0] = beta;
+      f->second = second ? 1 : 0;
+      if (second) f->n_second += 1;
+    } else {
+      f->exh_k = it0 + 1;
+      f->exhausted = 1;
+    }
+  }
+  if (!ok) return;
+  const double inv = 1.0 / beta;
+  float* vn = V + (int64_t)(it0 + 1) * B.LEN + P.voff;
+  const double* wb = w + P.voff;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) vn[i] = (float)(wb[i] * inv);
+}
+
+// Eigenvalue test of every problem (one CTA each): α from the H·v partials,
+// then sturm_step.
+__global__ void k_b_sturm(const BatchDev B, int k, int lock) {
+  const int p = blockIdx.x;
+  LanczosFlags* f = B.fl + p;
+  if (cta_gate(threadIdx.x == 0 && f->done)) return;
+  if (cta_gate(threadIdx.x == 0 && f->exhausted && k > f->exh_k)) {
+    if (threadIdx.x == 0) {
+      f->done = 1;
+      f->elit = f->exh_k;
+      problem_finished(B.ctl, B.nprob);
+    }
+    return;
+  }
+  const BatchProblemDev& P = B.probs[p];
+  double* T = B.T + (int64_t)p * B.lm * B.lm;
+  __shared__ double red[32];
+  {
+    double x = 0.0;
+    const double* ap = B.alpha_part + (int64_t)(k - 1) * B.nslots + P.slot0;
+    for (int i = threadIdx.x; i < P.nslots; i += blockDim.x) x += ap[i];
+    x = warp_sum(x);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int wdx = 0; wdx < (int)(blockDim.x >> 5); ++wdx) s += red[wdx];
+      T[(int64_t)(k - 1) * B.lm + (k - 1)] = s;
+    }
+    __syncthreads();
+  }
+  sturm_step(T, B.lm, k, lock, B.num_ev, B.en + (int64_t)p * B.nh * B.num_ev, B.nh, B.tol, P.mdim, f);
+  if (threadIdx.x == 0 && f->done) problem_finished(B.ctl, B.nprob);
+}
+
+__global__ void k_b_cycle_end(const BatchDev B) {
+  for (int p = threadIdx.x; p < B.nprob; p += blockDim.x) {
+    LanczosFlags* f = B.fl + p;
+    if (!f->done && f->exhausted) {
+      f->done = 1;
+      f->elit = f->exh_k;
+      atomicAdd(&B.ctl->ndone, 1);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(&B.ctl->ndone, 0) >= B.nprob) B.ctl->all_done = 1;
+}
+
+// ------------------------------------------------------------------ restart
+__global__ void __launch_bounds__(256) k_b_jacobi(const BatchDev B, int n, int gate) {
+  const int p = blockIdx.x;
+  if (gate && (B.ctl->all_done || stopped(B.fl + p))) return;
+  const int64_t o = (int64_t)p * B.lm * B.lm;
+  jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
+}
+
+// Jacobi of one problem for its Ritz vectors (grid of one CTA).
+__global__ void __launch_bounds__(256) k_b_jacobi_one(const BatchDev B, int p, int n) {
+  const int64_t o = (int64_t)p * B.lm * B.lm;
+  jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
+}
+
+__global__ void k_b_restart_small(const BatchDev B) {
+  const int p = blockIdx.x;
+  if (B.ctl->all_done || stopped(B.fl + p)) return;
+  const int lm = B.lm, ls = B.ls, m = lm - 1;
+  double* T = B.T + (int64_t)p * lm * lm;
+  const double* ev = B.evals + (int64_t)p * lm;
+  const double* vs = B.jacA + (int64_t)p * lm * lm;
+  float* yf = B.Yf + (int64_t)p * m * ls;
+  for (int idx = threadIdx.x; idx < m * ls; idx += blockDim.x) yf[idx] = (float)vs[idx];
+  __shared__ double beta;
+  if (threadIdx.x == 0) beta = T[(int64_t)(lm - 1) * lm + (lm - 2)];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < lm * lm; idx += blockDim.x) T[idx] = 0.0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < ls; k += blockDim.x) {
+    T[(int64_t)k * lm + k] = ev[k];
+    const double tmp = beta * vs[(int64_t)k * m + (m - 1)];
+    T[(int64_t)k * lm + ls] = tmp;
+    T[(int64_t)ls * lm + k] = tmp;
+  }
+}
+
+// U_k = Σ_{j<m} Y[j,k] V_j over the chunk (FP32 products, Kahan sums).
+__global__ void __launch_bounds__(kNT) k_b_rotate(const BatchDev B, const float* __restrict__ V,
+                                                  float* __restrict__ U) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  const int m = B.lm - 1, ls = B.ls;
+  const float* __restrict__ Y = B.Yf + (int64_t)ch.x * m * ls;
+  const float* __restrict__ Vb = V + P.voff;
+  float* __restrict__ Ub = U + P.voff;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    for (int k0 = 0; k0 < ls; k0 += 8) {
+      KahanF acc[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[q].init();
+      for (int j = 0; j < m; ++j) {
+        const float x = Vb[(int64_t)j * B.LEN + i];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (k0 + q < ls) acc[q].add(__fmul_rn(__ldg(Y + (int64_t)(k0 + q) * m + j), x));
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (k0 + q < ls) Ub[(int64_t)(k0 + q) * B.LEN + i] = acc[q].get();
+    }
+  }
+}
+
+// Chunk partials of the Gram matrix of U and of U_k·v_last (pair order of
+// k_gram), double-float sums: part[pair*nchunks + c].
+__global__ void __launch_bounds__(kNT) k_b_gram(const BatchDev B, const float* __restrict__ U,
+                                                const float* __restrict__ Vlast) {
+  const int c = blockIdx.x;
+  const int4 ch = B.chunks[c];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  constexpr int TILE = 64;
+  extern __shared__ float tl[];  // (ls+1) x TILE
+  const int ls = B.ls;
+  const int NP = ls * (ls + 1) / 2 + ls;
+  const float* __restrict__ Ub = U + P.voff;
+  const float* __restrict__ vl = Vlast + P.voff;
+  for (int c0 = 0; c0 < NP; c0 += 8 * kNT) {
+    DFAcc dacc[8];
+    int kk[8], ll[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      dacc[q].init();
+      const int pr = c0 + threadIdx.x + q * kNT;
+      kk[q] = 0;
+      ll[q] = 0;
+      if (pr < NP) gram_pair(pr, ls, kk[q], ll[q]);
+    }
+    for (int64_t t0 = ch.y; t0 < ch.z; t0 += TILE) {
+      const int cnt = (int)min((int64_t)TILE, ch.z - t0);
+      for (int idx = threadIdx.x; idx < (ls + 1) * TILE; idx += kNT) {
+        const int j = idx / TILE, x = idx % TILE;
+        float val = 0.f;
+        if (x < cnt) val = (j < ls) ? Ub[(int64_t)j * B.LEN + t0 + x] : vl[t0 + x];
+        tl[idx] = val;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int pr = c0 + threadIdx.x + q * kNT;
+        if (pr >= NP) break;
+        for (int x = 0; x < cnt; ++x) dacc[q].add_prod(tl[kk[q] * TILE + x], tl[ll[q] * TILE + x]);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int pr = c0 + threadIdx.x + q * kNT;
+      if (pr < NP) B.part[(int64_t)pr * B.nchunks + c] = dacc[q].get();
+    }
+  }
+}
+
+// Per problem: Gram matrix from the chunk partials, Cholesky G = RᵀR,
+// X = R⁻¹, c = Xᵀ g (as k_chol), FP32 copies for k_b_apply.
+__global__ void k_b_chol(const BatchDev B) {
+  const int p = blockIdx.x;
+  if (B.ctl->all_done || stopped(B.fl + p)) return;
+  const BatchProblemDev& P = B.probs[p];
+  const int ls = B.ls;
+  const int NP = ls * (ls + 1) / 2 + ls;
+  extern __shared__ double sh[];
+  double* g = sh;        // NP
+  double* R = sh + NP;   // ls x ls
+  for (int pr = threadIdx.x; pr < NP; pr += blockDim.x) {
+    double x = 0.0;
+    const double* src = B.part + (int64_t)pr * B.nchunks + P.chunk0;
+    for (int q = 0; q < P.nchunks; ++q) x += src[q];
+    g[pr] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double* X = B.X + (int64_t)p * ls * ls;
+  double* cv = B.cvec + (int64_t)p * ls;
+  float* xf = B.Xf + (int64_t)p * (ls * ls + ls);
+  auto Gm = [&](int k, int l) {  // k <= l
+    int off = 0;
+    for (int r = 0; r < k; ++r) off += ls - r;
+    return g[off + (l - k)];
+  };
+  for (int j = 0; j < ls; ++j) {
+    for (int i = 0; i <= j; ++i) {
+      double t = Gm(i, j);
+      for (int k = 0; k < i; ++k) t -= R[j * ls + k] * R[i * ls + k];
+      if (i == j) {
+        if (!(t > 0.0)) {
+          B.fl[p].bad = 1;
+          t = 1e-300;
+        }
+        R[j * ls + j] = sqrt(t);
+      } else {
+        R[j * ls + i] = t / R[i * ls + i];
+      }
+    }
+  }
+  for (int j = 0; j < ls; ++j) {
+    for (int i = ls - 1; i >= 0; --i) {
+      double t = (i == j) ? 1.0 : 0.0;
+      for (int k = i + 1; k <= j; ++k) t -= R[k * ls + i] * X[j * ls + k];
+      X[j * ls + i] = (i <= j) ? t / R[i * ls + i] : 0.0;
+    }
+  }
+  const int gofs = ls * (ls + 1) / 2;
+  for (int k = 0; k < ls; ++k) {
+    double t = 0.0;
+    for (int j = 0; j <= k; ++j) t += X[k * ls + j] * g[gofs + j];
+    cv[k] = t;
+  }
+  for (int idx = 0; idx < ls * ls; ++idx) xf[idx] = (float)X[idx];
+  for (int k = 0; k < ls; ++k) xf[ls * ls + k] = (float)cv[k];
+}
+
+// V_k = Σ_{j<=k} X[j,k] U_j (k < ls);  V_ls = V_{lm-1} − Σ_k c_k V_k.
+__global__ void __launch_bounds__(kNT) k_b_apply(const BatchDev B, const float* __restrict__ U,
+                                                 float* __restrict__ V) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  const int ls = B.ls, lm = B.lm;
+  const float* __restrict__ xf = B.Xf + (int64_t)ch.x * (ls * ls + ls);
+  const float* __restrict__ Ub = U + P.voff;
+  float* __restrict__ Vb = V + P.voff;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    KahanF last;
+    last.init();
+    last.add(Vb[(int64_t)(lm - 1) * B.LEN + i]);
+    for (int k = 0; k < ls; ++k) {
+      KahanF q;
+      q.init();
+      for (int j = 0; j <= k; ++j) q.add(__fmul_rn(__ldg(xf + k * ls + j), Ub[(int64_t)j * B.LEN + i]));
+      const float qv = q.get();
+      Vb[(int64_t)k * B.LEN + i] = qv;
+      last.add(__fmul_rn(-__ldg(xf + ls * ls + k), qv));
+    }
+    Vb[(int64_t)ls * B.LEN + i] = last.get();
+  }
+}
+
+// R_e = Σ_{k<elit} Y[k,e] V_k of problem p (its chunks), FP64, padded.
+__global__ void __launch_bounds__(kNT) k_b_ritz(const BatchDev B, const float* __restrict__ V, int p, int elit,
+                                                int nev, double* __restrict__ R) {
+  const BatchProblemDev& P = B.probs[p];
+  const double* __restrict__ Y = B.jacA + (int64_t)p * B.lm * B.lm;
+  const float* __restrict__ Vb = V + P.voff;
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < P.len; i += (int64_t)gridDim.x * kNT) {
+    for (int e = 0; e < nev; ++e) {
+      double t = 0.0;
+      for (int k = 0; k < elit; ++k) t = fma(Y[(int64_t)e * elit + k], (double)Vb[(int64_t)k * B.LEN + i], t);
+      R[(int64_t)e * P.len + i] = t;
+    }
+  }
+}
+
+size_t jacobi_smem(int n) {
+  const int N = n + (n & 1);
+  return sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+}
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_b_start(const BatchDev& B, uint64_t seed, double* w, cudaStream_t st) {
+  k_b_start<<<B.nchunks, kNT, 0, st>>>(B, seed, w);
+}
+void launch_b_to_padded(const BatchDev& B, const double* src, double* w, cudaStream_t st) {
+  k_b_to_padded<<<B.nchunks, kNT, 0, st>>>(B, src, w);
+}
+void launch_b_from_padded(const BatchDev& B, const double* w, double* dst, cudaStream_t st) {
+  k_b_from_padded<<<B.nchunks, kNT, 0, st>>>(B, w, dst);
+}
+void launch_b_convert(const BatchDev& B, const double* w, float* v, cudaStream_t st) {
+  int64_t g = (B.LEN + kNT - 1) / kNT;
+  if (g > 152 * 8) g = 152 * 8;
+  k_b_convert<<<(int)(g < 1 ? 1 : g), kNT, 0, st>>>(w, v, B.LEN);
+}
+void launch_b_init(const BatchDev& B, const double* w, float* V0, cudaStream_t st) {
+  k_b_selfdot<<<B.nchunks, kNT, 0, st>>>(B, w);
+  k_b_init_scale<<<B.nchunks, kNT, 0, st>>>(B, w, V0);
+}
+void launch_b_sturm(const BatchDev& B, int k, int lock, cudaStream_t st) {
+  int threads = ((B.num_ev * kLPE + 31) / 32) * 32;
+  if (threads > 1024) threads = 1024;
+  if (threads < 32) threads = 32;
+  const size_t shm = sizeof(double) * (3 * (size_t)B.lm + B.num_ev);
+  k_b_sturm<<<B.nprob, threads, shm, st>>>(B, k, lock);
+}
+void launch_b_orth(const BatchDev& B, float* V, double* w, int it0, cudaStream_t st) {
+  const size_t hsh = sizeof(double) * (size_t)(it0 + 1);
+  k_b_orth_dot<<<B.nchunks, kNT, 0, st>>>(B, V, w, it0);
+  k_b_orth_axpy<<<B.nchunks, kNT, hsh, st>>>(B, V, w, it0);
+  k_b_orth_dot2<<<B.nchunks, kNT, 0, st>>>(B, V, w, it0);
+  k_b_orth_axpy2<<<B.nchunks, kNT, hsh, st>>>(B, V, w, it0);
+  k_b_orth_scale<<<B.nchunks, kNT, 0, st>>>(B, V, w, it0);
+}
+void launch_b_cycle_end(const BatchDev& B, cudaStream_t st) { k_b_cycle_end<<<1, 256, 0, st>>>(B); }
+void launch_b_restart(const BatchDev& B, float* V, float* U, cudaStream_t st) {
+  const int m = B.lm - 1, ls = B.ls;
+  const int NP = ls * (ls + 1) / 2 + ls;
+  k_b_jacobi<<<B.nprob, 256, jacobi_smem(m), st>>>(B, m, 1);
+  k_b_restart_small<<<B.nprob, 256, 0, st>>>(B);
+  k_b_rotate<<<B.nchunks, kNT, 0, st>>>(B, V, U);
+  k_b_gram<<<B.nchunks, kNT, sizeof(float) * (ls + 1) * 64, st>>>(B, U, V + (int64_t)(B.lm - 1) * B.LEN);
+  k_b_chol<<<B.nprob, 128, sizeof(double) * (NP + ls * ls), st>>>(B);
+  k_b_apply<<<B.nchunks, kNT, 0, st>>>(B, U, V);
+}
+void launch_b_jacobi_one(const BatchDev& B, int p, int n, cudaStream_t st) {
+  k_b_jacobi_one<<<1, 256, jacobi_smem(n), st>>>(B, p, n);
+}
+void launch_b_ritz(const BatchDev& B, const float* V, int p, int elit, int nev, int64_t len, double* R,
+                   cudaStream_t st) {
+  int64_t g = (len + kNT - 1) / kNT;
+  if (g > 152 * 4) g = 152 * 4;
+  k_b_ritz<<<(int)(g < 1 ? 1 : g), kNT, 0, st>>>(B, V, p, elit, nev, R);
+}
+
+}  // namespace smgpu

@@ -123,6 +123,18 @@ __device__ __forceinline__ double widen(float x) {
   return __hiloint2double((int)hi, (int)lo);
 }
 __device__ __forceinline__ double widen(double x) { return x; }
+
+// A launch gate evaluated by thread 0 only and broadcast through shared
+// memory.  The Lanczos flags are written by kernels on the other stream
+// while a CTA starts; reading them once per CTA sends every thread the same
+// way, so no thread leaves before a barrier that the others wait at.  Call
+// as cta_gate(threadIdx.x == 0 && <condition>) in one-dimensional CTAs.
+__device__ __forceinline__ bool cta_gate(bool thread0_value) {
+  __shared__ int s_gate;
+  if (threadIdx.x == 0) s_gate = thread0_value ? 1 : 0;
+  __syncthreads();
+  return s_gate != 0;
+}
 #endif
 
 #define SMGPU_CUDA_TRY(expr)                                                    \

@@ -58,7 +58,7 @@ __device__ __forceinline__ void ld4(const float* __restrict__ p, float (&o)[4]) 
 
 template <int S, int NT, int MINB, int KM>
 __global__ void __launch_bounds__(NT, MINB) hv_multi_kernel(const MultiHvArgs<S> a) {
-  if (a.epi.all_done != nullptr && *a.epi.all_done) return;
+  if (a.epi.all_done != nullptr && cta_gate(threadIdx.x == 0 && *a.epi.all_done)) return;
   if (a.epi.count != nullptr && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.epi.count, 1);
   constexpr int Q = S / 4;      // threads per column
   constexpr int CP = NT / Q;    // columns per pass

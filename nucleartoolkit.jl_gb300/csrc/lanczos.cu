@@ -129,7 +129,7 @@ template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                   const double* __restrict__ alpha_part, int nalpha,
                                                   double* __restrict__ pdot, int G, const LanczosFlags* fl) {
-  if (stopped(fl)) return;
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
   const double alpha = sum_partials<kNT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
   const TX* __restrict__ vk = V + (int64_t)it0 * ld;
@@ -211,7 +211,7 @@ template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_axpy(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                    const double* __restrict__ pdot, double* __restrict__ pn1, int G,
                                                    const LanczosFlags* fl) {
-  if (stopped(fl)) return;
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   extern __shared__ double hs[];
   __shared__ double red[kNT / 32];
   orth_subtract<TX>(V, ld, it0 + 1, w, pdot, pn1, G, hs, red);
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
                                                    const double* __restrict__ w, const double* __restrict__ pdot,
                                                    const double* __restrict__ pn1, double* __restrict__ pdot2,
                                                    int G, const LanczosFlags* fl) {
-  if (stopped(fl)) return;
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
   if (!need_second(pdot, pn1, m, G, red)) return;
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kNT) k_orth_axpy2(const TX* __restrict__ V, in
                                                     const double* __restrict__ pn1,
                                                     const double* __restrict__ pdot2, double* __restrict__ pn2,
                                                     int G, const LanczosFlags* fl) {
-  if (stopped(fl)) return;
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   extern __shared__ double hs[];
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
                                                     const double* __restrict__ pn1,
                                                     const double* __restrict__ pn2, int G, int it0, double* T,
                                                     int lm, int64_t len, LanczosScalars* sc, LanczosFlags* fl) {
-  if (stopped(fl)) return;
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
   const bool second = need_second(pdot, pn1, m, G, red);
@@ -306,8 +306,8 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
 __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
                         double tol, int64_t mdim, const double* __restrict__ alpha_part, int nalpha,
                         LanczosFlags* fl) {
-  if (fl->done) return;
-  if (fl->exhausted && k > fl->exh_k) {
+  if (cta_gate(threadIdx.x == 0 && fl->done)) return;
+  if (cta_gate(threadIdx.x == 0 && fl->exhausted && k > fl->exh_k)) {
     // the Krylov space ended at exh_k; T_k was never completed
     if (threadIdx.x == 0) { fl->done = 1; fl->elit = fl->exh_k; }
     return;

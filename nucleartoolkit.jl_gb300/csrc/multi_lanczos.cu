@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kNT) k_m_reduce(const double* __restrict__ par
 __global__ void k_m_alpha(const double* __restrict__ alpha_part, int nalpha, double* T, int lm, int it0,
                           const LanczosFlags* fl, const MultiCtl* ctl) {
   const int s = blockIdx.x;
-  if (ctl->all_done || lane_stopped(fl, s)) return;
+  if (cta_gate(threadIdx.x == 0 && (ctl->all_done || lane_stopped(fl, s)))) return;
   __shared__ double red[kNT / 32];
   const double a = sum_partials<kNT>(alpha_part + (int64_t)s * nalpha, nalpha, red);
   if (threadIdx.x == 0) T[(int64_t)s * lm * lm + (int64_t)it0 * lm + it0] = a;
@@ -171,8 +171,8 @@ __global__ void k_m_sturm(double* T, int lm, int k, int lock, int num_ev, double
                           int64_t mdim, LanczosFlags* fl, MultiCtl* ctl, int S) {
   const int s = blockIdx.x;
   LanczosFlags* f = fl + s;
-  if (f->done) return;
-  if (f->exhausted && k > f->exh_k) {
+  if (cta_gate(threadIdx.x == 0 && f->done)) return;
+  if (cta_gate(threadIdx.x == 0 && f->exhausted && k > f->exh_k)) {
     if (threadIdx.x == 0) {
       f->done = 1;
       f->elit = f->exh_k;
@@ -190,8 +190,7 @@ template <int S>
 __global__ void __launch_bounds__(kNT) k_m_dot(const float* __restrict__ V, int64_t len, int it0, double* w,
                                                const double* __restrict__ T, int lm, double* __restrict__ part, int G,
                                                const LanczosFlags* fl, const MultiCtl* ctl, int first) {
-  if (ctl->all_done) return;
-  if (!first && !ctl->any_second) return;
+  if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (!first && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
   __shared__ double red[(kNT / 32) * 8 * S];
   const int q = threadIdx.x % Q, r = threadIdx.x / Q, s0 = 4 * q;
@@ -247,8 +246,7 @@ __global__ void __launch_bounds__(kNT) k_m_axpy(const float* __restrict__ V, int
                                                 const double* __restrict__ h, double* __restrict__ part, int G,
                                                 const LanczosFlags* fl, const MultiCtl* ctl,
                                                 const int* __restrict__ sec) {
-  if (ctl->all_done) return;
-  if (sec != nullptr && !ctl->any_second) return;
+  if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (sec != nullptr && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
   extern __shared__ double hs[];  // m*S
   __shared__ double red[(kNT / 32) * S];
@@ -283,7 +281,7 @@ __global__ void __launch_bounds__(kNT) k_m_axpy(const float* __restrict__ V, int
 // Second-pass decision per sample: ||w''||² < ||w'||² / 2.
 __global__ void k_m_decide(const double* __restrict__ h1, const double* __restrict__ nrm1, int m, int* sec,
                            const LanczosFlags* fl, MultiCtl* ctl, int S) {
-  if (ctl->all_done) return;
+  if (__shfl_sync(0xffffffffu, ctl->all_done, 0)) return;
   const int s = threadIdx.x;
   bool sc = false;
   if (s < S && !lane_stopped(fl, s)) sc = nrm1[s] < 0.5 * h1[(int64_t)m * S + s];

@@ -119,9 +119,13 @@ struct smgpu_problem {
     tt.task_p0 = task_arrays[R].second;
   }
 
-  void upload() {
-    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+  // Device copies of the tables.  with_streams = false for problems that run
+  // on a batch's streams.
+  void upload(bool with_streams = true) {
+    if (with_streams) {
+      SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+    }
     int dev = 0;
     SMGPU_CUDA_TRY(cudaGetDevice(&dev));
     SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

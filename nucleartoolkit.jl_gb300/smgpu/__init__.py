@@ -1,6 +1,7 @@
 """smgpu — GB300-native valence shell-model eigensolver (NuclearToolkit.jl
 `main_sm` path) behind the C ABI of libsmgpu.so."""
 from ._lib import FP64, MIXED, SmgpuError, library_path, load
-from .shellmodel import MultiSampleProblem, ShellModelProblem, main_sm
+from .shellmodel import BatchProblem, MultiSampleProblem, ShellModelProblem, main_sm
 
-__all__ = ["FP64", "MIXED", "SmgpuError", "ShellModelProblem", "MultiSampleProblem", "main_sm", "load", "library_path"]
+__all__ = ["FP64", "MIXED", "SmgpuError", "ShellModelProblem", "MultiSampleProblem", "BatchProblem", "main_sm", "load",
+           "library_path"]

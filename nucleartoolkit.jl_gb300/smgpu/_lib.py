@@ -50,6 +50,16 @@ SIGNATURES = {
     "smgpu_multi_stats": (C.c_int, [_vp, _vp]),
     "smgpu_multi_timings": (C.c_int, [_vp, _vp]),
     "smgpu_multi_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "smgpu_batch_create_from_snt": (C.c_int, [C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int,
+                                              C.POINTER(_vp)]),
+    "smgpu_batch_destroy": (C.c_int, [_vp]),
+    "smgpu_batch_last_error": (C.c_char_p, [_vp]),
+    "smgpu_batch_dims": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_int), _vp]),
+    "smgpu_batch_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int]),
+    "smgpu_batch_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
+    "smgpu_batch_stats": (C.c_int, [_vp, _vp]),
+    "smgpu_batch_timings": (C.c_int, [_vp, _vp]),
+    "smgpu_batch_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _lib = None
@@ -94,4 +104,11 @@ def check_multi(code: int, handle=None):
     """check() for smgpu_multi handles."""
     if code != OK:
         msg = load().smgpu_multi_last_error(handle)
+        raise SmgpuError(code, (msg or b"").decode(errors="replace"))
+
+
+def check_batch(code: int, handle=None):
+    """check() for smgpu_batch handles."""
+    if code != OK:
+        msg = load().smgpu_batch_last_error(handle)
         raise SmgpuError(code, (msg or b"").decode(errors="replace"))

@@ -187,6 +187,93 @@ class MultiSampleProblem:
                     n_second_pass=per[:, 2].astype(int), status=rc)
 
 
+class BatchProblem:
+    """Independent problems of uneven dimension solved together (an
+    ``smgpu_batch`` handle): many ``main_sm`` set-ups
+    (src/ShellModel/shellmodel_main.jl:89-281), one per (snt, nucleus) pair,
+    iterated in lockstep in the FP32-mixed form."""
+
+    def __init__(self, problems):
+        """problems: sequence of (snt path, nucleus name)."""
+        L = load()
+        snts = [os.fsencode(p[0]) for p in problems]
+        nucs = [p[1].encode() for p in problems]
+        a = (C.c_char_p * len(snts))(*snts)
+        b = (C.c_char_p * len(nucs))(*nucs)
+        h = C.c_void_p()
+        rc = L.smgpu_batch_create_from_snt(a, b, len(snts), C.byref(h))
+        _lib.check_batch(rc, None)
+        self._h = h
+        tot, n = C.c_longlong(), C.c_int()
+        _lib.check_batch(L.smgpu_batch_dims(h, C.byref(tot), C.byref(n), None), h)
+        self.nprob = int(n.value)
+        self.total_mdim = int(tot.value)
+        self.mdims = np.zeros(self.nprob, dtype=np.int64)
+        _lib.check_batch(L.smgpu_batch_dims(h, None, None, _p(self.mdims)), h)
+        self.moff = np.concatenate([[0], np.cumsum(self.mdims)[:-1]]).astype(np.int64)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().smgpu_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def split(self, x):
+        """Concatenated vector -> list of per-problem vectors."""
+        return [x[o:o + m] for o, m in zip(self.moff, self.mdims)]
+
+    def stats(self):
+        s = np.zeros(8, dtype=np.int64)
+        _lib.check_batch(load().smgpu_batch_stats(self._h, _p(s)), self._h)
+        keys = ["updates", "problems", "chunks", "hv_tasks", "hv_threads", "hv_rows", "hv_min_ctas", "table_bytes"]
+        return dict(zip(keys, map(int, s)))
+
+    def timings(self):
+        t = np.zeros(8)
+        _lib.check_batch(load().smgpu_batch_timings(self._h, _p(t)), self._h)
+        keys = ["setup", "lanczos", "matvec", "capture", "ritz", "solve_wall", "r6", "r7"]
+        return dict(zip(keys, map(float, t)))
+
+    def time_matvec(self, reps=20, flush_l2=True):
+        """Mean ms per batched H·v launch (all problems), CUDA events."""
+        ms = C.c_double()
+        _lib.check_batch(load().smgpu_batch_time_matvec(self._h, int(reps), 1 if flush_l2 else 0, C.byref(ms)),
+                         self._h)
+        return float(ms.value)
+
+    def matvec(self, v, accumulate: bool = False, out=None):
+        """w_p = H_p v_p on the concatenated vector (total_mdim entries)."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        if v.shape != (self.total_mdim,):
+            raise ValueError(f"v must have shape ({self.total_mdim},)")
+        w = np.zeros_like(v) if out is None else out
+        _lib.check_batch(load().smgpu_batch_matvec(self._h, _p(v), _p(w), 1 if accumulate else 0), self._h)
+        return w
+
+    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False):
+        ev = np.zeros((self.nprob, num_ev))
+        vecs = np.zeros(num_ev * self.total_mdim) if want_vecs else None
+        stats = np.zeros(8 + 4 * self.nprob, dtype=np.int32)
+        v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
+        rc = load().smgpu_batch_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts),
+                                      _p(v1a), _p(ev), _p(vecs), _p(stats))
+        if rc not in (_lib.OK, _lib.ERR_NOCONV):
+            _lib.check_batch(rc, self._h)
+        per = stats[8:].reshape(self.nprob, 4)
+        evecs = None
+        if want_vecs:
+            evecs = [vecs[num_ev * o:num_ev * (o + m)].reshape(num_ev, m) for o, m in zip(self.moff, self.mdims)]
+        return dict(evals=ev, evecs=evecs, n_matvec=int(stats[0]), n_restart=int(stats[1]),
+                    converged=bool(stats[2]) and rc == _lib.OK, kernel_launches=int(stats[4]),
+                    elit=per[:, 0].astype(int), problem_converged=per[:, 1].astype(bool),
+                    n_second_pass=per[:, 2].astype(int), status=rc)
+
+
 def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=False, is_show=False,
             num_history=3, lm=300, ls=20, tol=1.0e-8, in_wf="", mdimmode=False, print_evec=False,
             calc_moment=False, calc_entropy=False, visualize_occ=False, gfactors=(1.0, 0.0, 5.586, -3.826),

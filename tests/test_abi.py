@@ -59,6 +59,22 @@ def test_multi_create_without_gpu_fails_loudly():
     assert ei.value.code == _lib.ERR_ARG
 
 
+def test_batch_create_without_gpu_fails_loudly():
+    from smgpu import BatchProblem, SmgpuError
+    from smgpu import _lib
+    ck = os.path.join(ROOT, "tests", "golden", "ckpot.snt")
+    with pytest.raises(SmgpuError) as ei:
+        BatchProblem([(ck, "Be8"), (ck, "Li7")])
+    assert ei.value.code == _lib.ERR_CUDA
+    assert "no CUDA device" in str(ei.value)
+    with pytest.raises(SmgpuError) as ei:
+        BatchProblem([(ck, "Be8")] * 4097)
+    assert ei.value.code == _lib.ERR_LIMIT
+    with pytest.raises(SmgpuError) as ei:
+        BatchProblem([])
+    assert ei.value.code == _lib.ERR_ARG
+
+
 def test_main_sm_keeps_reference_signature():
     """shellmodel_main.jl:89-92 argument names."""
     from smgpu import main_sm
