@@ -7,6 +7,9 @@ a CPU, so its result is computed once here and the GPU tests / bench compare
 against the stored values.  Re-run after any change of the synthetic recipe:
 
     python tests/golden/make_oracle_runs.py [names...]
+
+`sd_batch128` records the uneven batch of 128 sd problems (per problem:
+dimension, nnz(H), eigenvalues, iteration counts).
 """
 import json
 import os
@@ -30,11 +33,38 @@ RUNS = {
 }
 
 
+BATCH = ("sd_batch128", 128, (5, 30, 15, 1e-8))
+
+
+def batch_run():
+    """The uneven batch of 128 sd problems: per problem its dimension, nnz(H)
+    and the oracle's eigenvalues and iteration counts."""
+    n, (nev, lm, ls, tol) = BATCH[1], BATCH[2]
+    d = tempfile.mkdtemp()
+    out = dict(nprob=n, num_ev=nev, lm=lm, ls=ls, tol=tol, threads=get_threads(), problems=[])
+    t0 = time.time()
+    for k, (snt, nuc) in enumerate(synth.sd_batch_snts(d, n)):
+        P = OracleProblem(snt, nuc)
+        r = P.trl(nev, lm=lm, ls=ls, tol=tol)
+        out["problems"].append(dict(nucleus=nuc, seed=synth.CONFIG_SEEDS["sd_batch_base"] + k, mdim=P.mdim,
+                                    nnz=P.nnz(), evals=[float(x) for x in r["evals"]], n_hv=r["n_hv"],
+                                    n_restart=r["n_restart"], converged=r["converged"], t_trl=r["t_total"]))
+    out["mdim_total"] = sum(p["mdim"] for p in out["problems"])
+    out["nnz_total"] = sum(p["nnz"] for p in out["problems"])
+    out["t_total"] = time.time() - t0
+    return out
+
+
 def main(names):
     path = os.path.join(HERE, "oracle_runs.json")
     data = json.load(open(path)) if os.path.exists(path) else {}
     d = tempfile.mkdtemp()
     for name in names:
+        if name == BATCH[0]:
+            data[name] = batch_run()
+            print(name, data[name]["mdim_total"], data[name]["nnz_total"], data[name]["t_total"], flush=True)
+            json.dump(data, open(path, "w"), indent=1)
+            continue
         nev, lm, ls, tol = RUNS[name]
         snt, nuc = synth.config_snt(d, name)
         t0 = time.time()
@@ -54,4 +84,4 @@ def main(names):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:] or list(RUNS))
+    main(sys.argv[1:] or list(RUNS) + [BATCH[0]])

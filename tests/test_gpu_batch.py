@@ -84,7 +84,14 @@ def test_batch_solve_vs_oracle(lib, mixed_batch):
             assert np.linalg.norm(O.operate_H(x) - r["evals"][p, k] * x) < RITZ_RESID, (p, nuc, k)
 
 
-def test_batch_of_128_sd_problems(lib, tmp_path):
+@pytest.fixture(scope="module")
+def golden_runs():
+    import json
+    with open(os.path.join(GOLDEN, "oracle_runs.json")) as f:
+        return json.load(f)
+
+
+def test_batch_of_128_sd_problems(lib, tmp_path, golden_runs):
     """The uneven batch of 128 sd problems (dims 28 .. 93,710): every problem
     converges; problems spanning the sizes against the oracle."""
     from smgpu import synth
@@ -94,10 +101,16 @@ def test_batch_of_128_sd_problems(lib, tmp_path):
     r = G.solve(5, lm=30, ls=15, tol=1e-8)
     assert r["converged"] and r["problem_converged"].all()
     order = np.argsort(G.mdims)
-    for p in [int(order[k]) for k in (0, 20, 60, 100, 127)]:
+    for p in [int(order[k]) for k in (0, 20, 60)]:
         ro = _oracle(*probs[p]).trl(5, lm=30, ls=15, tol=1e-8)
         nev = len(ro["evals"])
         assert np.abs(r["evals"][p, :nev] - ro["evals"]).max() <= EIG_MIXED_ATOL, (p, probs[p][1])
+    # every problem against the stored oracle run of the same batch
+    gb = golden_runs["sd_batch128"]
+    for p, q in enumerate(gb["problems"]):
+        assert q["mdim"] == G.mdims[p] and q["nucleus"] == probs[p][1]
+        ref = np.array(q["evals"])
+        assert np.abs(r["evals"][p, :len(ref)] - ref).max() <= EIG_MIXED_ATOL, (p, q["nucleus"])
 
 
 def test_batch_noconv_and_error_paths(lib, mixed_batch, tmp_path):
