@@ -2,6 +2,7 @@
 
     python nucleartoolkit.jl_gb300/smgpu/hvbench.py --workload pf4p4n --precision mixed --reps 20
     python nucleartoolkit.jl_gb300/smgpu/hvbench.py --workload pf4p4n --samples 16 --reps 10 --solve
+    python nucleartoolkit.jl_gb300/smgpu/hvbench.py --batch 128 --reps 10 --solve
 
 Prints one JSON line: mean ms per launch, multiply-adds per launch and the
 CSR-equivalent bandwidth (algorithmic bytes nnz·(s_c+4) + 4·(mdim+1) +
@@ -9,7 +10,9 @@ CSR-equivalent bandwidth (algorithmic bytes nnz·(s_c+4) + 4·(mdim+1) +
 share the indices: nnz·(4 + S·4) + 2·S·mdim·4).  --samples S times the
 multi-sample H·V on S seeded interaction samples of the workload's basis
 (FP32-mixed).  --solve adds one eigensolve (5 lowest, lm=30, ls=15,
-tol=1e-8).  Used for kernel profiling.
+tol=1e-8).  --batch N times the batched H·v over the first N problems of
+the uneven sd batch (FP32-mixed; the bandwidth figure then needs --nnz of the
+whole batch).  Used for kernel profiling.
 """
 import argparse
 import json
@@ -33,12 +36,16 @@ def main():
     ap.add_argument("--samples", type=int, default=0, help="interaction samples sharing the basis (multi-sample H·V)")
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--batch", type=int, default=0, help="problems of the uneven sd batch (batched H·v)")
     ap.add_argument("--solve", action="store_true", help="also run one eigensolve")
     ap.add_argument("--nnz", type=int, default=0, help="structural nnz(H) for the bandwidth figure")
     a = ap.parse_args()
     d = tempfile.mkdtemp()
     out = {"workload": a.workload}
-    if a.samples:
+    if a.batch:
+        P = smgpu.BatchProblem(synth.sd_batch_snts(d, a.batch))
+        out.update(workload=f"sd batch of {a.batch}", precision="mixed", problems=a.batch)
+    elif a.samples:
         shell, vp, vn, nuc = VALENCE[a.workload]
         if a.workload == "pf4p4n":
             files = synth.pf_multi_snts(d, a.samples)
@@ -52,10 +59,12 @@ def main():
         P = smgpu.ShellModelProblem(snt, nuc, prec)
         out.update(precision=a.precision)
     ms = P.time_matvec(reps=a.reps, flush_l2=not a.no_flush)
-    out.update(mdim=P.mdim, ms=ms)
+    out.update(mdim=int(getattr(P, "total_mdim", 0) or P.mdim), ms=ms)
     out.update(P.stats())
     if a.nnz:
-        if a.samples:
+        if a.batch:
+            b = a.nnz * 8 + 4 * (P.total_mdim + a.batch) + 2 * P.total_mdim * 4
+        elif a.samples:
             b = a.nnz * (4 + a.samples * 4) + 2 * a.samples * P.mdim * 4
         else:
             s = 4 if a.precision == "mixed" else 8
