@@ -122,6 +122,14 @@ int smgpu_matvec(smgpu_problem* h, const double* v, double* w, int ncols, int ac
 int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int max_restarts,
                 const double* v1, double* evals_out, double* evecs_out, int* stats_out);
 
+/* <v|J^2|v>/<v|v> for nvec host vectors (mdim doubles each, basis order):
+ * the expectation values main_sm prints as J labels (operate_J! on the Ritz
+ * vectors and J_from_JJ1, shellmodel_main.jl:226-240,1105-1113).  J^2 is
+ * applied on the GPU in FP64 as an operator on the same basis (built on the
+ * first call from the handle's orbits: one-body j(j+1), two-body
+ * J(J+1) - j_a(j_a+1) - j_b(j_b+1) per pair). */
+int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out);
+
 /* Seconds spent in the phases of the last create / solve / matvec call (the
  * reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos", "Rvecs",
  * shellmodel_main.jl:137,159,208).  times_out: 8 doubles:

@@ -176,6 +176,7 @@ int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision
   smgpu_problem* h = new smgpu_problem();
   try {
     h->precision = precision;
+    h->I = I;
     h->vp = vp;
     h->vn = vn;
     h->mtot2 = mtot2;
@@ -675,6 +676,62 @@ int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out) 
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    tmp.free_all();
+    return SMGPU_OK;
+  });
+}
+
+int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out) {
+  if (!h || !vecs || !jj_out || nvec < 1) return fail(h, SMGPU_ERR_ARG, "bad jj arguments");
+  return guarded(h, [&]() {
+    if (!h->jj_op) {
+      smgpu_problem* q = new smgpu_problem();
+      try {
+        q->precision = SMGPU_FP64;
+        q->vp = h->vp;
+        q->vn = h->vn;
+        q->mtot2 = h->mtot2;
+        q->I = jj_interaction(h->I);
+        build_tables(q->I, h->vp, h->vn, h->mtot2, q->T);
+        if (q->T.mdim != h->T.mdim || q->T.pbits != h->T.pbits || q->T.nbits != h->T.nbits)
+          throw SetupError{SMGPU_ERR_DEVICE, "J^2 basis differs from the problem's basis"};
+        q->upload(false);
+      } catch (...) {
+        delete q;
+        throw;
+      }
+      h->jj_op = q;
+    }
+    smgpu_problem* q = h->jj_op;
+    const int64_t mdim = h->T.mdim, len = q->T.len_pad;
+    DeviceArena tmp;
+    try {
+      double* d_in = tmp.alloc<double>(mdim);
+      double* d_out = tmp.alloc<double>(mdim);
+      double* d_v = tmp.alloc<double>(len);
+      double* d_w = tmp.alloc<double>(len);
+      std::vector<double> w(mdim);
+      for (int k = 0; k < nvec; ++k) {
+        const double* v = vecs + (size_t)k * mdim;
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(d_in, v, sizeof(double) * mdim, cudaMemcpyHostToDevice, h->st));
+        SMGPU_CUDA_TRY(cudaMemsetAsync(d_w, 0, sizeof(double) * len, h->st));
+        launch_to_padded<double>(q->dt, d_in, d_v, h->st);
+        q->hv((const double*)d_v, d_w, HvEpilogue<double>{}, h->st);
+        launch_from_padded(q->dt, d_w, d_out, h->st);
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(w.data(), d_out, sizeof(double) * mdim, cudaMemcpyDeviceToHost, h->st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(h->st));
+        double vw = 0.0, vv = 0.0;
+        for (int64_t i = 0; i < mdim; ++i) {
+          vw += v[i] * w[i];
+          vv += v[i] * v[i];
+        }
+        jj_out[k] = vv > 0.0 ? vw / vv : 0.0;
+      }
+      SMGPU_CUDA_TRY(cudaGetLastError());
+    } catch (...) {
+      tmp.free_all();
+      throw;
+    }
     tmp.free_all();
     return SMGPU_OK;
   });

@@ -83,8 +83,11 @@ struct smgpu_problem {
   double tune_ms[16] = {0};
   int sms = 152;
   DeviceArena solver;  // Krylov basis and scratch of the last solve
+  Interaction I;       // the interaction the tables were built from
+  smgpu_problem* jj_op = nullptr;  // J^2 on the same basis (built on first use)
 
   ~smgpu_problem() {
+    delete jj_op;
     solver.free_all();
     tables.free_all();
     if (st) cudaStreamDestroy(st);

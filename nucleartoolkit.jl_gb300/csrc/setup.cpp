@@ -130,6 +130,37 @@ Interaction read_snt(const std::string& path, int Anum) {
   return I;
 }
 
+Interaction jj_interaction(const Interaction& I) {
+  Interaction J;
+  J.lp = I.lp;
+  J.ln = I.ln;
+  J.cp = I.cp;
+  J.cn = I.cn;
+  J.porb = I.porb;
+  J.norb = I.norb;
+  auto jj1 = [](int j2) { return 0.25 * j2 * (j2 + 2); };  // j(j+1) with j = j2/2
+  for (const Orbit& o : I.porb) J.spe_p.push_back(jj1(o.j2));
+  for (const Orbit& o : I.norb) J.spe_n.push_back(jj1(o.j2));
+  for (int kind = 0; kind < 2; ++kind) {
+    const std::vector<Orbit>& orb = kind == 0 ? I.porb : I.norb;
+    const int off = kind == 0 ? 0 : I.lp;
+    for (int a = 0; a < (int)orb.size(); ++a)
+      for (int b = a; b < (int)orb.size(); ++b)
+        for (int Jt = std::abs(orb[a].j2 - orb[b].j2) / 2; Jt <= (orb[a].j2 + orb[b].j2) / 2; ++Jt) {
+          if (a == b && Jt % 2 == 1) continue;
+          const double v = Jt * (Jt + 1.0) - jj1(orb[a].j2) - jj1(orb[b].j2);
+          J.tb[kind].push_back({a + 1 + off, b + 1 + off, a + 1 + off, b + 1 + off, Jt, v});
+        }
+  }
+  for (int a = 0; a < I.lp; ++a)
+    for (int b = 0; b < I.ln; ++b)
+      for (int Jt = std::abs(I.porb[a].j2 - I.norb[b].j2) / 2; Jt <= (I.porb[a].j2 + I.norb[b].j2) / 2; ++Jt) {
+        const double v = Jt * (Jt + 1.0) - jj1(I.porb[a].j2) - jj1(I.norb[b].j2);
+        J.tb[2].push_back({a + 1, I.lp + b + 1, a + 1, I.lp + b + 1, Jt, v});
+      }
+  return J;
+}
+
 void parse_nucleus(const std::string& nuc, int& A, int& Z) {
   static const char* el[] = {
       "n",  "H",  "He", "Li", "Be", "B",  "C",  "N",  "O",  "F",  "Ne", "Na", "Mg", "Al", "Si", "P",  "S",

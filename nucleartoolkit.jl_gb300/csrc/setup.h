@@ -32,6 +32,13 @@ struct SetupError {
 
 // snt text -> Interaction (readsmsnt semantics, shellmodel_main.jl:293-365)
 Interaction read_snt(const std::string& path, int Anum);
+// The total angular momentum squared J^2 of the valence particles written as
+// an interaction on the same orbits: one-body j(j+1) per orbit and the
+// diagonal two-body elements <ab;J|2 j_a.j_b|ab;J> = J(J+1) - j_a(j_a+1) -
+// j_b(j_b+1) for every pp, nn (J even when a == b) and pn pair.  Its m-scheme
+// matrix on a basis is J^2; the reference builds the same operator as jump
+// lists (prep_J / operate_J!, src/ShellModel/shellmodel_main.jl:1439-1650).
+Interaction jj_interaction(const Interaction& I);
 // "Cr48" / "48Cr" -> A and Z (util_func.jl:1,13-24; shellmodel_main.jl:908-916)
 void parse_nucleus(const std::string& nuc, int& A, int& Z);
 

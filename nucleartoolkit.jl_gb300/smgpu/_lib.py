@@ -37,6 +37,7 @@ SIGNATURES = {
     "smgpu_export_jumps": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_longlong), _vp, _vp]),
     "smgpu_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
     "smgpu_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
+    "smgpu_jj": (C.c_int, [_vp, _vp, C.c_int, _vp]),
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),

@@ -88,6 +88,14 @@ class ShellModelProblem:
         check(load().smgpu_time_matvec(self._h, int(reps), 1 if flush_l2 else 0, C.byref(ms)), self._h)
         return float(ms.value)
 
+    def jj(self, vecs):
+        """<v|J^2|v>/<v|v> for each row of vecs (shape (n, mdim) or (mdim,))."""
+        v = np.ascontiguousarray(vecs, dtype=np.float64)
+        n = 1 if v.ndim == 1 else v.shape[0]
+        out = np.zeros(n)
+        check(load().smgpu_jj(self._h, _p(v), n, _p(out)), self._h)
+        return out
+
     # --- compute
     def matvec(self, v, accumulate: bool = False, out=None):
         v = np.ascontiguousarray(v, dtype=np.float64)
@@ -274,6 +282,16 @@ class BatchProblem:
                     n_second_pass=per[:, 2].astype(int), status=rc)
 
 
+def J_from_JJ1(JJ, tol=1.0e-6):
+    """J from <J^2> = J(J+1) (shellmodel_main.jl:1105-1113): the first
+    half-integer J in 0..50 within tol, else -1."""
+    for J2 in range(0, 101):
+        hJ = 0.5 * J2
+        if abs(hJ * (hJ + 1.0) - JJ) < tol:
+            return hJ
+    return -1.0
+
+
 def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=False, is_show=False,
             num_history=3, lm=300, ls=20, tol=1.0e-8, in_wf="", mdimmode=False, print_evec=False,
             calc_moment=False, calc_entropy=False, visualize_occ=False, gfactors=(1.0, 0.0, 5.586, -3.826),
@@ -302,9 +320,12 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
     if mdimmode:
         P.close()
         return None
-    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts)
+    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, want_vecs=verbose)
     en = list(map(float, r["evals"]))
     if verbose:
+        if r["status"] == _lib.OK:
+            # J labels of the Ritz vectors (shellmodel_main.jl:226-240,257)
+            print("J " + str([J_from_JJ1(x) for x in P.jj(r["evecs"])]))
         print("En. " + " ".join(f"{x:10.4f}" for x in en))
         print("Ex. " + " ".join(f"{x - en[0]:10.4f}" for x in en))
         if is_show:

@@ -46,6 +46,8 @@ def lib():
         L.orc_v1_export.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_spe_diag.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.orc_operate_H.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.orc_jj.argtypes = [vp, C.c_void_p]
+        L.orc_jj.restype = C.c_double
         L.orc_nnz.restype = C.c_longlong
         L.orc_nnz.argtypes = [vp]
         L.orc_start_vector.argtypes = [C.c_longlong, C.c_ulonglong, C.c_void_p]
@@ -175,6 +177,11 @@ class OracleProblem:
         twf = np.zeros_like(wf)
         lib().orc_operate_H(self._h, _p(wf), _p(twf))
         return twf
+
+    def jj(self, v) -> float:
+        """<v|J^2|v>/<v|v> by the ladder operator (J^2 = J-J+ + M(M+1))."""
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        return float(lib().orc_jj(self._h, _p(v)))
 
     def nnz(self) -> int:
         """Structural non-zeros of H (distinct (row, col) pairs, diagonal included)."""

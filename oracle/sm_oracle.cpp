@@ -1276,6 +1276,57 @@ void orc_spe_diag(void* h, double* ep, double* en) {
     for (auto& o : b) { double s = 0; for (size_t k = 0; k < o.size(); ++k) s += P->snt.SPEs[1][k] * o[k]; en[kn++] = s; }
 }
 
+// <v|J^2|v> / <v|v> for one vector in basis order.  The reference evaluates
+// J^2 = J-J+ + Jz(Jz+1) with jump lists (prep_J / operate_J!,
+// shellmodel_main.jl:1439-1650, Js initialised to M(M+1) at :151); this
+// restatement applies the ladder operator directly: <v|J-J+|v> = ||J+ v||^2,
+// J+ = sum over species and m-states of sqrt(j(j+1) - m(m+1)) a+_{m+1} a_m.
+// The m-states of an orbit are consecutive in construct_msps order, so the
+// particle moves to the neighbouring position and the fermion sign is +1.
+double orc_jj(void* h, const double* v) {
+  Problem* P = (Problem*)h;
+  const Basis& B = P->B;
+  const int Lp = (int)P->ms.p.size(), Ln = (int)P->ms.n.size();
+  struct KeyHash {
+    size_t operator()(const std::pair<i64, i64>& k) const {
+      return std::hash<i64>()(k.first * 1000003 + k.second);
+    }
+  };
+  std::unordered_map<std::pair<i64, i64>, double, KeyHash> out;
+  double vv = 0.0;
+  for (size_t b = 0; b < B.pbits.size(); ++b) {
+    const auto& pb = B.pbits[b];
+    const auto& nb = B.nbits[b];
+    for (size_t ip = 0; ip < pb.size(); ++ip)
+      for (size_t in = 0; in < nb.size(); ++in) {
+        const double c = v[B.tdims[b] + (i64)ip * (i64)nb.size() + (i64)in];
+        vv += c * c;
+        if (c == 0.0) continue;
+        for (int sp = 0; sp < 2; ++sp) {
+          const auto& ms = sp == 0 ? P->ms.p : P->ms.n;
+          const int L = sp == 0 ? Lp : Ln;
+          const i64 bits = sp == 0 ? pb[ip] : nb[in];
+          for (int k = 1; k < L; ++k) {
+            const auto& a = ms[k - 1];
+            const auto& a1 = ms[k];
+            if (a1[5] != a[5]) continue;  // k is the top m-state of its orbit
+            const i64 bk = onehot(L, k), bk1 = onehot(L, k + 1);
+            if (!(bits & bk) || (bits & bk1)) continue;
+            const double j2 = a[2], m2 = a[4];
+            const double f = 0.5 * std::sqrt(j2 * (j2 + 2.0) - m2 * (m2 + 2.0));
+            const i64 nbits = bits ^ bk ^ bk1;
+            const std::pair<i64, i64> key = sp == 0 ? std::make_pair(nbits, nb[in]) : std::make_pair(pb[ip], nbits);
+            out[key] += f * c;
+          }
+        }
+      }
+  }
+  double jp = 0.0;
+  for (const auto& kv : out) jp += kv.second * kv.second;
+  const double M = 0.5 * P->Mtot;
+  return (jp + M * (M + 1.0) * vv) / vv;
+}
+
 // twf += H wf   (lanczos_methods.jl:153 operate_H! semantics)
 void orc_operate_H(void* h, const double* wf, double* twf) { operate_H(*(Problem*)h, wf, twf); }
 

@@ -216,3 +216,34 @@ def test_main_sm_mirror(lib, golden):
     en = main_sm(CKPOT, "Be8", 10, [], verbose=False)
     for e, ref in zip(en, golden["ckpot_Be8"]["energies"]):
         assert (e - ref) ** 2 < 1e-6
+
+
+def test_main_sm_prints_j_labels(lib, capsys):
+    """main_sm prints the J of every state before the energies
+    (shellmodel_main.jl:226-240,257)."""
+    from smgpu import main_sm
+    main_sm(CKPOT, "Be8", 10, [], verbose=True)
+    out = capsys.readouterr().out
+    assert "J [0.0, 2.0, 4.0, 2.0, 1.0, 2.0, 3.0, 1.0, 0.0, 4.0]" in out
+
+
+def test_jj_on_gpu_matches_oracle(lib, snt_dir):
+    """<J^2> of Ritz vectors: GPU (two-body form of J^2) vs the oracle's
+    ladder operator, FP64 and mixed forms."""
+    from smgpu.shellmodel import J_from_JJ1
+    G = _gpu(CKPOT, "Be8", 0)
+    r = G.solve(10, lm=60, ls=20, tol=1e-10, want_vecs=True)
+    jj = G.jj(r["evecs"])
+    O = _oracle(CKPOT, "Be8")
+    for x, j in zip(r["evecs"], jj):
+        assert abs(j - O.jj(x)) < 1e-9
+    assert [J_from_JJ1(x) for x in jj] == [0, 2, 4, 2, 1, 2, 3, 1, 0, 4]
+    snt, nuc = snt_dir["sd4p4n"]
+    M = _gpu(snt, nuc, 1)
+    r = M.solve(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    O = _oracle(snt, nuc)
+    jj = M.jj(r["evecs"])
+    for x, j in zip(r["evecs"], jj):
+        assert abs(j - O.jj(x)) < 1e-9 * max(1.0, abs(j))
+        twoJ = np.sqrt(1 + 4 * j) - 1
+        assert abs(twoJ - round(twoJ)) < 1e-4

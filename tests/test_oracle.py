@@ -93,3 +93,72 @@ def test_uneven_and_empty_species():
         H = P.dense_H() if P.mdim < 3000 else None
         if H is not None:
             assert np.abs(H - H.T).max() < 1e-12
+
+
+def _jj_snt_text(orbits, core, A):
+    """J^2 written as an snt interaction on the given orbits (one-body
+    j(j+1); diagonal two-body J(J+1) - j_a(j_a+1) - j_b(j_b+1) per pair, J
+    even for a == b in pp/nn).  The library builds the same operator in C++."""
+    k = len(orbits)
+    jj1 = [0.25 * o[2] * (o[2] + 2) for o in orbits]
+    lines = ["! J^2", f" {k} {k} {core[0]} {core[1]}"]
+    for t, tz in ((0, -1), (1, 1)):
+        lines += [f" {i + 1 + t * k} {n} {l} {j2} {tz}" for i, (n, l, j2) in enumerate(orbits)]
+    lines.append(f" {2 * k} 0")
+    lines += [f" {i + 1 + t * k} {i + 1 + t * k} {jj1[i]:.12f}" for t in range(2) for i in range(k)]
+    tb = []
+    for off in (0, k):
+        for a in range(k):
+            for b in range(a, k):
+                for J in range(abs(orbits[a][2] - orbits[b][2]) // 2, (orbits[a][2] + orbits[b][2]) // 2 + 1):
+                    if a == b and J % 2:
+                        continue
+                    tb.append((a + 1 + off, b + 1 + off, a + 1 + off, b + 1 + off, J, J * (J + 1) - jj1[a] - jj1[b]))
+    for a in range(k):
+        for b in range(k):
+            for J in range(abs(orbits[a][2] - orbits[b][2]) // 2, (orbits[a][2] + orbits[b][2]) // 2 + 1):
+                tb.append((a + 1, b + 1 + k, a + 1, b + 1 + k, J, J * (J + 1) - jj1[a] - jj1[b]))
+    lines.append(f" {len(tb)} 0 {A}")
+    lines += [" %d %d %d %d %d %.12f" % t for t in tb]
+    return "\n".join(lines) + "\n"
+
+
+def test_jj_ladder_operator_on_be8_levels():
+    """<J^2> of the ckpot 8Be Ritz vectors is J(J+1) with integer J."""
+    P = OracleProblem(CKPOT, "Be8")
+    r = P.trl(10, lm=60, ls=20, tol=1e-10, want_vecs=True)
+    jj = np.array([P.jj(x) for x in r["evecs"]])
+    J = (-1 + np.sqrt(1 + 4 * jj)) / 2
+    assert np.abs(J - np.round(J)).max() < 1e-8
+    assert list(np.round(J).astype(int)) == [0, 2, 4, 2, 1, 2, 3, 1, 0, 4]
+
+
+@pytest.mark.parametrize("vp,vn", [(2, 2), (1, 2), (3, 1)])
+def test_jj_two_body_form_matches_ladder_operator(tmp_path, vp, vn):
+    """The two-body form of J^2 (what the library applies) against the
+    ladder-operator form of the oracle, on random vectors and on J^2's own
+    spectrum."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(GOLDEN), "..", "nucleartoolkit.jl_gb300"))
+    from smgpu import synth
+    nuc = synth.nucleus_name("sd", vp, vn)
+    f = tmp_path / "jj.snt"
+    f.write_text(_jj_snt_text(synth.SD_ORBITS, synth.SD_CORE, 16 + vp + vn))
+    Jop = OracleProblem(str(f), nuc)
+    # a problem on the same orbits in the same order (usdb.snt lists d3/2 first)
+    ref = OracleProblem(synth.write_snt(str(tmp_path / "h.snt"), "sd", 7, vp, vn), nuc)
+    assert Jop.mdim == ref.mdim
+    ev = np.linalg.eigvalsh(Jop.dense_H())
+    twoJ = -1 + np.sqrt(1 + 4 * ev)
+    assert np.abs(twoJ - np.round(twoJ)).max() < 1e-9
+    rng = np.random.default_rng(vp * 10 + vn)
+    for _ in range(3):
+        v = rng.standard_normal(ref.mdim)
+        two_body = v @ Jop.operate_H(v) / (v @ v)
+        assert abs(two_body - ref.jj(v)) < 1e-10 * max(1.0, abs(two_body))
+    # eigenvectors of a J-conserving H have integer J in both forms
+    r = ref.trl(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    for x in r["evecs"]:
+        a, b = x @ Jop.operate_H(x), ref.jj(x)
+        assert abs(a - b) < 1e-8
+        assert abs(np.sqrt(1 + 4 * b) - np.round(np.sqrt(1 + 4 * b))) < 1e-6
