@@ -66,7 +66,8 @@ typedef struct {
  * element from the nucleus name (util_func.jl:1,13-24; shellmodel_main.jl:
  * 95,116-117,908-916), Mtot = A mod 2 (:110), basis and jump tables
  * (occ :769-848, prep_Hamil_T1 :580-649, prep_Hamil_pn :658-730,
- * prep_pn :1139-1199), built on the host and uploaded once. */
+ * prep_pn :1139-1199): the basis and the jump tables are enumerated on the
+ * GPU, the interaction's operator lists on the host. */
 int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int precision, smgpu_problem** out);
 
 /* Same, from an in-memory description (the data of the reference's SMobject,

@@ -209,7 +209,28 @@ i128 gcd_(i128 a, i128 b) {
 }
 }  // namespace
 
+namespace {
+double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
+}  // namespace
+
+// Memoised per thread: the m-scheme loops ask for the same few hundred
+// coefficients millions of times.
 double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
+  if (tj1 < 0 || tj2 < 0 || tJ < 0 || tj1 > 500 || tj2 > 500 || tJ > 1000 || std::abs(tm1) > 1000 ||
+      std::abs(tm2) > 1000 || std::abs(tM) > 2000)
+    return clebsch_gordan_exact(tj1, tm1, tj2, tm2, tJ, tM);
+  const uint64_t key = ((uint64_t)tj1 << 52) | ((uint64_t)(tm1 + 1024) << 40) | ((uint64_t)tj2 << 31) |
+                       ((uint64_t)(tm2 + 1024) << 19) | ((uint64_t)tJ << 9) | (uint64_t)((tM + 2048) & 0x1ff);
+  thread_local std::unordered_map<uint64_t, std::pair<int, double>> memo;
+  auto it = memo.find(key);
+  if (it != memo.end() && it->second.first == tM) return it->second.second;
+  const double v = clebsch_gordan_exact(tj1, tm1, tj2, tm2, tJ, tM);
+  memo[key] = {tM, v};
+  return v;
+}
+
+namespace {
+double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
   if (tm1 + tm2 != tM) return 0.0;
   if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return 0.0;
   if (((tj1 + tm1) | (tj2 + tm2) | (tJ + tM)) & 1) return 0.0;
@@ -237,53 +258,10 @@ double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
   double v = std::sqrt((double)num / (double)den);
   return S < 0 ? -v : v;
 }
+}  // namespace
 
 // ------------------------------------------------------------- helpers
 namespace {
-inline int popc(uint64_t x) { return __builtin_popcountll(x); }
-
-// ⟨f|a†c|i⟩ for one-hot masks a (create) and c (annihilate).  Returns false
-// when not connectable.  `odd` = parity of the fermion sign count: occupied
-// states at or above c in i, then at or above a after removing c
-// (calc_phase_1!, shellmodel_main.jl:887-897, without its constant offset,
-// which cancels between the proton and neutron factors).
-inline bool apply1(uint64_t i, uint64_t a, uint64_t c, uint64_t& f, int& odd) {
-  if ((i & c) == 0) return false;
-  uint64_t r = i & ~c;
-  if (r & a) return false;
-  int cnt = popc(i & ~(c - 1)) + popc(r & ~(a - 1));
-  f = r | a;
-  odd = cnt & 1;
-  return true;
-}
-// ⟨f|a†b†dc|i⟩ (TF_connectable + calc_phase!, shellmodel_main.jl:850-885).
-inline bool apply2(uint64_t i, const Op2& o, uint64_t& f, int& odd) {
-  if ((i & o.c) != o.c || (i & o.d) != o.d) return false;
-  uint64_t r = i & ~o.c & ~o.d;
-  if ((r & o.a) || (r & o.b)) return false;
-  int cnt = popc(i & ~(o.c - 1));
-  uint64_t x = i & ~o.c;
-  cnt += popc(x & ~(o.d - 1));
-  x &= ~o.d;
-  cnt += popc(x & ~(o.b - 1));
-  x |= o.b;
-  cnt += popc(x & ~(o.a - 1));
-  f = x | o.a;
-  odd = cnt & 1;
-  return true;
-}
-// Index of `x` in a descending list, or -1 (bisearch!, :1068-1083).
-inline int find_desc(const uint64_t* v, int n, uint64_t x) {
-  int lo = 0, hi = n - 1;
-  while (lo <= hi) {
-    int mid = (lo + hi) >> 1;
-    if (v[mid] > x) lo = mid + 1;
-    else if (v[mid] < x) hi = mid - 1;
-    else return mid;
-  }
-  return -1;
-}
-
 struct Key4 {
   uint64_t a, b, c, d;
   bool operator==(const Key4& o) const { return a == o.a && b == o.b && c == o.c && d == o.d; }
@@ -328,27 +306,6 @@ std::vector<int> mstates_of(const std::vector<MState>& ms, int o) {
   return r;
 }
 
-// Lexicographic k-combinations of L m-states as bit strings (descending ints).
-void combos(int L, int k, std::vector<uint64_t>& bits, std::vector<int>& M, const std::vector<MState>& ms) {
-  bits.clear();
-  M.clear();
-  if (k > L) return;
-  std::vector<int> c(k);
-  for (int i = 0; i < k; ++i) c[i] = i;
-  while (true) {
-    uint64_t b = 0;
-    int m = 0;
-    for (int i = 0; i < k; ++i) { b |= bit_of(L, c[i]); m += ms[c[i]].m2; }
-    bits.push_back(b);
-    M.push_back(m);
-    int i = k - 1;
-    while (i >= 0 && c[i] == L - k + i) --i;
-    if (i < 0) break;
-    ++c[i];
-    for (int j = i + 1; j < k; ++j) c[j] = c[j - 1] + 1;
-  }
-}
-
 // prep_Hamil_T1 (:580-649) for one species.
 std::vector<Op2> two_body_ops(const std::vector<Interaction::TB>& tbs, const std::vector<Orbit>& orb,
                               const std::vector<MState>& ms, int loff) {
@@ -380,142 +337,27 @@ std::vector<Op2> two_body_ops(const std::vector<Interaction::TB>& tbs, const std
 }
 }  // namespace
 
-// ------------------------------------------------------------ build_tables
-void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
-  T = Tables();
-  T.msp = msps(I.porb);
-  T.msn = msps(I.norb);
-  T.Lp = (int)T.msp.size();
-  T.Ln = (int)T.msn.size();
-  if (T.Lp > 63 || T.Ln > 63) throw SetupError{SMGPU_ERR_LIMIT, "more than 63 m-states per species"};
-  if (vp < 0 || vn < 0 || vp > T.Lp || vn > T.Ln) throw SetupError{SMGPU_ERR_NUCLEUS, "invalid valence particle numbers"};
+// ------------------------------------------------------------ set-up pieces
+// (composed by build_tables in enum.cu, which enumerates the basis and builds
+// the jump tables on the device)
 
-  // ---- basis (occ, :769-848)
-  std::vector<uint64_t> pall, nall;
-  std::vector<int> Mpall, Mnall;
-  combos(T.Lp, vp, pall, Mpall, T.msp);
-  combos(T.Ln, vn, nall, Mnall, T.msn);
-  std::vector<int> Mps = Mpall, Mns = Mnall;
-  std::sort(Mps.begin(), Mps.end());
-  Mps.erase(std::unique(Mps.begin(), Mps.end()), Mps.end());
-  std::sort(Mns.begin(), Mns.end());
-  Mns.erase(std::unique(Mns.begin(), Mns.end()), Mns.end());
-  std::reverse(Mns.begin(), Mns.end());
-  T.tdims.push_back(0);
-  T.off_pad.push_back(0);
-  T.pstart.push_back(0);
-  T.nstart.push_back(0);
-  for (int Mp : Mps)
-    for (int Mn : Mns) {
-      if (Mp + Mn != mtot2) continue;
-      int np = 0, nn = 0;
-      for (size_t i = 0; i < pall.size(); ++i)
-        if (Mpall[i] == Mp) { T.pbits.push_back(pall[i]); ++np; }
-      for (size_t j = 0; j < nall.size(); ++j)
-        if (Mnall[j] == Mn) { T.nbits.push_back(nall[j]); ++nn; }
-      int stride = (nn + 3) & ~3;
-      T.np.push_back(np);
-      T.nn.push_back(nn);
-      T.stride.push_back(stride);
-      T.mp2.push_back(Mp);
-      T.mn2.push_back(Mn);
-      T.tdims.push_back(T.tdims.back() + (int64_t)np * nn);
-      T.off_pad.push_back(T.off_pad.back() + (int64_t)np * stride);
-      T.pstart.push_back(T.pstart.back() + np);
-      T.nstart.push_back(T.nstart.back() + nn);
-    }
-  T.nb = (int)T.np.size();
-  T.mdim = T.tdims.back();
-  T.len_pad = T.off_pad.back();
-  if (T.mdim == 0) return;
-  const int nb = T.nb;
-  const int64_t NP = T.pstart[nb], NN = T.nstart[nb];
+std::vector<MState> mstates(const std::vector<Orbit>& orb) { return msps(orb); }
 
-  // one-body diagonal: dot(SPEs, jocc) per SD
-  T.ep.assign(NP, 0.0);
-  T.en.assign(NN, 0.0);
-  for (int64_t g = 0; g < NP; ++g) {
-    std::vector<double> occ(I.lp, 0.0);
-    for (int k = 0; k < T.Lp; ++k)
-      if (T.pbits[g] & bit_of(T.Lp, k)) occ[T.msp[k].orbit] += 1.0;
-    double s = 0.0;
-    for (int o = 0; o < I.lp; ++o) s += I.spe_p[o] * occ[o];
-    T.ep[g] = s;
+std::vector<long> conjugate_index(const std::vector<Op2>& ops) {
+  std::unordered_map<Key4, size_t, Key4H> where;
+  for (size_t k = 0; k < ops.size(); ++k) where.emplace(Key4{ops[k].a, ops[k].b, ops[k].c, ops[k].d}, k);
+  std::vector<long> conj(ops.size());
+  for (size_t k = 0; k < ops.size(); ++k) {
+    auto it = where.find(Key4{ops[k].c, ops[k].d, ops[k].a, ops[k].b});
+    conj[k] = it == where.end() ? -1 : (long)it->second;
   }
-  for (int64_t g = 0; g < NN; ++g) {
-    std::vector<double> occ(I.ln, 0.0);
-    for (int k = 0; k < T.Ln; ++k)
-      if (T.nbits[g] & bit_of(T.Ln, k)) occ[T.msn[k].orbit] += 1.0;
-    double s = 0.0;
-    for (int o = 0; o < I.ln; ++o) s += I.spe_n[o] * occ[o];
-    T.en[g] = s;
-  }
+  return conj;
+}
 
-  // ---- pp / nn operators and their pull CSR (prep_Hamil_T1 + prep_2bjumps)
+void build_operators(const Interaction& I, Tables& T) {
+  // ---- pp / nn operators (prep_Hamil_T1, :580-649)
   T.vpp = two_body_ops(I.tb[0], I.porb, T.msp, 0);
   T.vnn = two_body_ops(I.tb[1], I.norb, T.msn, I.lp);
-  auto build_2b = [&](const std::vector<Op2>& ops, const std::vector<uint64_t>& bits, const std::vector<int>& start,
-                      std::vector<int>& ptr, std::vector<int>& col, std::vector<double>& val) {
-    // index of the hermitian conjugate (c,d,a,b) of each operator
-    std::unordered_map<Key4, size_t, Key4H> where;
-    for (size_t k = 0; k < ops.size(); ++k) where.emplace(Key4{ops[k].a, ops[k].b, ops[k].c, ops[k].d}, k);
-    std::vector<long> conj(ops.size());
-    for (size_t k = 0; k < ops.size(); ++k) {
-      auto it = where.find(Key4{ops[k].c, ops[k].d, ops[k].a, ops[k].b});
-      conj[k] = it == where.end() ? -1 : (long)it->second;
-    }
-    int64_t nrow = start[nb];
-    std::vector<std::vector<std::pair<int, double>>> rows(nrow);
-#pragma omp parallel for schedule(dynamic, 16)
-    for (int64_t g = 0; g < nrow; ++g) {
-      int b = (int)(std::upper_bound(start.begin(), start.end(), (int)g) - start.begin()) - 1;
-      const uint64_t* blk = bits.data() + start[b];
-      int n = start[b + 1] - start[b];
-      int i = (int)(g - start[b]);
-      auto& row = rows[g];
-      for (size_t k = 0; k < ops.size(); ++k) {
-        if (ops[k].v == 0.0) continue;
-        uint64_t f;
-        int odd;
-        if (!apply2(bits[g], ops[k], f, odd)) continue;
-        int j = find_desc(blk, n, f);
-        if (j < 0) continue;
-        double v = ops[k].v;
-        if (j < i && conj[k] >= 0) {
-          // the reference stores this pair on row j with the conjugate operator
-          uint64_t f2;
-          int odd2;
-          if (apply2(f, ops[conj[k]], f2, odd2) && f2 == bits[g] && ops[conj[k]].v != 0.0) {
-            v = ops[conj[k]].v;
-            odd = odd2;
-          }
-        }
-        row.push_back({j, odd ? -v : v});
-      }
-      // merge equal columns, keeping the list order inside each column
-      std::stable_sort(row.begin(), row.end(), [](const std::pair<int, double>& x, const std::pair<int, double>& y) {
-        return x.first < y.first;
-      });
-      std::vector<std::pair<int, double>> merged;
-      for (auto& e : row) {
-        if (!merged.empty() && merged.back().first == e.first) merged.back().second += e.second;
-        else merged.push_back(e);
-      }
-      row.swap(merged);
-    }
-    ptr.assign(nrow + 1, 0);
-    for (int64_t g = 0; g < nrow; ++g) ptr[g + 1] = ptr[g] + (int)rows[g].size();
-    col.resize(ptr[nrow]);
-    val.resize(ptr[nrow]);
-    for (int64_t g = 0; g < nrow; ++g)
-      for (size_t k = 0; k < rows[g].size(); ++k) {
-        col[ptr[g] + k] = rows[g][k].first;
-        val[ptr[g] + k] = rows[g][k].second;
-      }
-  };
-  build_2b(T.vpp, T.pbits, T.pstart, T.pp_ptr, T.pp_col, T.pp_val);
-  build_2b(T.vnn, T.nbits, T.nstart, T.nn_ptr, T.nn_col, T.nn_val);
-
   // ---- pn operators (prep_Hamil_pn, :658-730)
   {
     std::vector<int> Mzs;
@@ -554,32 +396,36 @@ void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
     T.vpn.resize(Mzs.size());
     for (size_t k = 0; k < Mzs.size(); ++k) T.vpn[k] = lists[k].ops;
   }
-
-  // V tables: per ΔM, distinct proton operators (a,c) and neutron operators
-  // (b,d) among the non-zero entries, in first-appearance order.
+  // ---- V tables: per ΔM, distinct proton operators (a,c) and neutron
+  // operators (b,d) among the non-zero entries, in first-appearance order.
   const size_t ndm = T.delMs.size();
   T.vtab_off_dm.assign(ndm + 1, 0);
   T.nA_dm.assign(ndm, 0);
   T.nB_dm.assign(ndm, 0);
-  std::vector<std::vector<std::pair<uint64_t, uint64_t>>> Aops(ndm), Bops(ndm);
+  T.Aops_dm.assign(ndm, {});
+  T.Bops_dm.assign(ndm, {});
   for (size_t k = 0; k < ndm; ++k) {
     std::unordered_map<uint64_t, int> ai, bi;
     std::vector<std::pair<int, int>> cells;
     for (const Op2& o : T.vpn[k]) {
       if (o.v == 0.0) { cells.push_back({-1, -1}); continue; }
-      uint64_t ka = o.a * 131ull + o.c * 7919ull + (o.a ^ (o.c << 1));
-      uint64_t kb = o.b * 131ull + o.d * 7919ull + (o.b ^ (o.d << 1));
-      // exact keys: one-hot masks identify m-states uniquely
-      ka = (uint64_t)(63 - __builtin_clzll(o.a)) * 64 + (uint64_t)(63 - __builtin_clzll(o.c));
-      kb = (uint64_t)(63 - __builtin_clzll(o.b)) * 64 + (uint64_t)(63 - __builtin_clzll(o.d));
+      // one-hot masks identify m-states uniquely
+      const uint64_t ka = (uint64_t)(63 - __builtin_clzll(o.a)) * 64 + (uint64_t)(63 - __builtin_clzll(o.c));
+      const uint64_t kb = (uint64_t)(63 - __builtin_clzll(o.b)) * 64 + (uint64_t)(63 - __builtin_clzll(o.d));
       auto pa = ai.find(ka);
-      if (pa == ai.end()) { pa = ai.emplace(ka, (int)Aops[k].size()).first; Aops[k].push_back({o.a, o.c}); }
+      if (pa == ai.end()) {
+        pa = ai.emplace(ka, T.nA_dm[k]++).first;
+        T.Aops_dm[k].push_back(o.a);
+        T.Aops_dm[k].push_back(o.c);
+      }
       auto pb = bi.find(kb);
-      if (pb == bi.end()) { pb = bi.emplace(kb, (int)Bops[k].size()).first; Bops[k].push_back({o.b, o.d}); }
+      if (pb == bi.end()) {
+        pb = bi.emplace(kb, T.nB_dm[k]++).first;
+        T.Bops_dm[k].push_back(o.b);
+        T.Bops_dm[k].push_back(o.d);
+      }
       cells.push_back({pa->second, pb->second});
     }
-    T.nA_dm[k] = (int)Aops[k].size();
-    T.nB_dm[k] = (int)Bops[k].size();
     T.vtab_off_dm[k + 1] = T.vtab_off_dm[k] + (int64_t)T.nA_dm[k] * T.nB_dm[k];
     if (T.nA_dm[k] >= (1 << 15) || T.nB_dm[k] >= (1 << 13))
       throw SetupError{SMGPU_ERR_LIMIT, "too many distinct one-body operators for one ΔM"};
@@ -589,9 +435,12 @@ void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
       T.vtab[T.vtab_off_dm[k] + (int64_t)cells[e].first * T.nB_dm[k] + cells[e].second] = T.vpn[k][e].v;
     }
   }
+}
 
-  // ---- links (prep_pn's bfs/bis, :1139-1151).  The reference indexes its
-  // list of all proton M values by block number; that is reproduced here.
+void build_links(Tables& T, const std::vector<int>& Mps) {
+  // prep_pn's bfs/bis (:1139-1151).  The reference indexes its list of all
+  // proton M values by block number; that is reproduced here.
+  const int nb = T.nb;
   std::vector<std::vector<Tables::Link>> per_b(nb);
   for (int bi = 0; bi < nb; ++bi)
     for (int bf = bi; bf < nb; ++bf) {
@@ -604,6 +453,7 @@ void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
       per_b[bi].push_back(Tables::Link{bi, bf, k, T.nA_dm[k], T.nB_dm[k], T.vtab_off_dm[k], 0});
       if (bf != bi) per_b[bf].push_back(Tables::Link{bf, bi, k, T.nA_dm[k], T.nB_dm[k], T.vtab_off_dm[k], 0});
     }
+  T.links.clear();
   T.link_begin.assign(nb + 1, 0);
   for (int b = 0; b < nb; ++b) {
     std::sort(per_b[b].begin(), per_b[b].end(), [](const Tables::Link& x, const Tables::Link& y) { return x.s < y.s; });
@@ -611,104 +461,16 @@ void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
     T.link_begin[b + 1] = (int)T.links.size();
   }
   if (T.links.size() >= (1u << 16)) throw SetupError{SMGPU_ERR_LIMIT, "too many block links"};
-
-  // ---- neutron pull CSR per link
   int64_t nptr_total = 0;
-  for (auto& L : T.links) { L.nptr_off = nptr_total; nptr_total += T.nn[L.b] + 1; }
-  T.npn_ptr.assign(nptr_total, 0);
-  {
-    std::vector<std::vector<uint32_t>> per_link(T.links.size());
-#pragma omp parallel for schedule(dynamic, 1)
-    for (long li = 0; li < (long)T.links.size(); ++li) {
-      const auto& L = T.links[li];
-      bool fwd = L.s >= L.b;
-      const uint64_t* src = T.nbits.data() + T.nstart[L.s];
-      int nsrc = T.nn[L.s];
-      auto& out = per_link[li];
-      int64_t* ptr = T.npn_ptr.data() + L.nptr_off;
-      ptr[0] = 0;
-      for (int n = 0; n < T.nn[L.b]; ++n) {
-        uint64_t sd = T.nbits[T.nstart[L.b] + n];
-        for (int ib = 0; ib < L.nB; ++ib) {
-          uint64_t opb = Bops[L.dm][ib].first, opd = Bops[L.dm][ib].second;
-          uint64_t f;
-          int odd;
-          if (fwd) {
-            if (!apply1(sd, opb, opd, f, odd)) continue;
-          } else {
-            uint64_t back;
-            int dummy;
-            if (!apply1(sd, opd, opb, f, dummy)) continue;  // d†b maps output n to source n'
-            if (!apply1(f, opb, opd, back, odd) || back != sd) continue;
-          }
-          int j = find_desc(src, nsrc, f);
-          if (j < 0) continue;
-          if (j >= (1 << 18)) throw SetupError{SMGPU_ERR_LIMIT, "neutron block too large"};
-          out.push_back(((uint32_t)j << 14) | ((uint32_t)ib << 1) | (uint32_t)odd);
-        }
-        ptr[n + 1] = (int64_t)out.size();
-      }
-    }
-    int64_t base = 0;
-    for (size_t li = 0; li < T.links.size(); ++li) {
-      int64_t* ptr = T.npn_ptr.data() + T.links[li].nptr_off;
-      for (int n = 0; n <= T.nn[T.links[li].b]; ++n) ptr[n] += base;
-      T.npn_ent.insert(T.npn_ent.end(), per_link[li].begin(), per_link[li].end());
-      base += (int64_t)per_link[li].size();
-    }
+  for (auto& L : T.links) {
+    L.nptr_off = nptr_total;
+    nptr_total += T.nn[L.b] + 1;
   }
+}
 
-  // ---- proton pull entries per output proton row
-  {
-    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> rows(NP);
-#pragma omp parallel for schedule(dynamic, 8)
-    for (int64_t g = 0; g < NP; ++g) {
-      int b = (int)(std::upper_bound(T.pstart.begin(), T.pstart.end(), (int)g) - T.pstart.begin()) - 1;
-      uint64_t sd = T.pbits[g];
-      for (int li = T.link_begin[b]; li < T.link_begin[b + 1]; ++li) {
-        const auto& L = T.links[li];
-        bool fwd = L.s >= L.b;
-        const uint64_t* src = T.pbits.data() + T.pstart[L.s];
-        int nsrc = T.np[L.s];
-        for (int ia = 0; ia < L.nA; ++ia) {
-          uint64_t opa = Aops[L.dm][ia].first, opc = Aops[L.dm][ia].second;
-          uint64_t f;
-          int odd;
-          if (fwd) {
-            if (!apply1(sd, opa, opc, f, odd)) continue;
-          } else {
-            uint64_t back;
-            int dummy;
-            if (!apply1(sd, opc, opa, f, dummy)) continue;
-            if (!apply1(f, opa, opc, back, odd) || back != sd) continue;
-          }
-          int j = find_desc(src, nsrc, f);
-          if (j < 0) continue;
-          rows[g].push_back({(uint32_t)j, ((uint32_t)li << 16) | ((uint32_t)ia << 1) | (uint32_t)odd});
-        }
-      }
-    }
-    T.ppn_ptr.assign(NP + 1, 0);
-    for (int64_t g = 0; g < NP; ++g) T.ppn_ptr[g + 1] = T.ppn_ptr[g] + (int)rows[g].size();
-    T.ppn_src.resize(T.ppn_ptr[NP]);
-    T.ppn_meta.resize(T.ppn_ptr[NP]);
-    for (int64_t g = 0; g < NP; ++g)
-      for (size_t k = 0; k < rows[g].size(); ++k) {
-        T.ppn_src[T.ppn_ptr[g] + k] = rows[g][k].first;
-        T.ppn_meta[T.ppn_ptr[g] + k] = rows[g][k].second;
-      }
-  }
-
-  T.Aops_dm.assign(ndm, {});
-  T.Bops_dm.assign(ndm, {});
-  for (size_t k = 0; k < ndm; ++k) {
-    for (auto& pr : Aops[k]) { T.Aops_dm[k].push_back(pr.first); T.Aops_dm[k].push_back(pr.second); }
-    for (auto& pr : Bops[k]) { T.Bops_dm[k].push_back(pr.first); T.Bops_dm[k].push_back(pr.second); }
-  }
-
-  // ---- multiply-adds per H·v
+void count_updates(Tables& T) {
   int64_t upd = 0;
-  for (int b = 0; b < nb; ++b) {
+  for (int b = 0; b < T.nb; ++b) {
     upd += (int64_t)T.np[b] * T.nn[b];  // diagonal
     upd += (int64_t)(T.pp_ptr[T.pstart[b + 1]] - T.pp_ptr[T.pstart[b]]) * T.nn[b];
     upd += (int64_t)(T.nn_ptr[T.nstart[b + 1]] - T.nn_ptr[T.nstart[b]]) * T.np[b];
@@ -717,9 +479,8 @@ void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T) {
   for (int64_t k = 0; k < (int64_t)T.ppn_meta.size(); ++k) link_pcount[T.ppn_meta[k] >> 16]++;
   for (size_t li = 0; li < T.links.size(); ++li) {
     const auto& L = T.links[li];
-    int64_t nent = T.npn_ptr[L.nptr_off + T.nn[L.b]] - T.npn_ptr[L.nptr_off];
-    // each proton entry of the link pairs with every neutron entry of the link
-    // (averaged: exact count is sum over rows; rows of one link share the CSR)
+    const int64_t nent = T.npn_ptr[L.nptr_off + T.nn[L.b]] - T.npn_ptr[L.nptr_off];
+    // every proton entry of a row meets every neutron entry of the link once
     upd += link_pcount[li] * nent;
   }
   T.updates = upd;

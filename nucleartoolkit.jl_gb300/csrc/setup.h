@@ -96,12 +96,30 @@ struct Tables {
   std::vector<double> vtab;  // V tables [nA x nB] per delMs index (only ΔM >= 0 used)
   std::vector<int64_t> vtab_off_dm;
   std::vector<int> nA_dm, nB_dm;
-  std::vector<std::vector<uint64_t>> Aops_dm, Bops_dm;  // per dm: (bit_a<<32|bit_c) style pairs, see setup.cpp
+  std::vector<std::vector<uint64_t>> Aops_dm, Bops_dm;  // per dm: one-hot (a, c) / (b, d) mask pairs, flattened
   // statistics
   int64_t updates = 0;
 };
 
-// Full host set-up of one problem.  vp, vn valence numbers, mtot2 doubled M.
+// Full set-up of one problem (enum.cu): the basis and the jump tables are
+// enumerated on the device and copied into T; the interaction-dependent
+// operator lists are built on the host.  vp, vn valence numbers, mtot2
+// doubled M.  Needs a CUDA device.
 void build_tables(const Interaction& I, int vp, int vn, int mtot2, Tables& T);
+
+// Host pieces of the set-up (setup.cpp), used by build_tables.
+// m-states of a species in construct_msps order (shellmodel_main.jl:373-384).
+std::vector<MState> mstates(const std::vector<Orbit>& orb);
+// prep_Hamil_T1 / prep_Hamil_pn (:580-730): the m-scheme pp, nn and per-ΔM pn
+// operator lists, the per-ΔM V tables and their distinct one-body operators
+// (T.msp and T.msn must be set).
+void build_operators(const Interaction& I, Tables& T);
+// Index of the hermitian conjugate (c,d,a,b) of every operator, or -1.
+std::vector<long> conjugate_index(const std::vector<Op2>& ops);
+// prep_pn's block links (:1139-1151) and the neutron-pointer offsets of
+// every link; Mps = every proton M value of the species (doubled), ascending.
+void build_links(Tables& T, const std::vector<int>& Mps);
+// Multiply-adds of one H·v (T.updates).
+void count_updates(Tables& T);
 
 }  // namespace smgpu
