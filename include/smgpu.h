@@ -70,6 +70,12 @@ typedef struct {
  * GPU, the interaction's operator lists on the host. */
 int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int precision, smgpu_problem** out);
 
+/* Same for main_sm with target_J = [twoJ/2]: the basis has Mtot = twoJ
+ * (shellmodel_main.jl:112-116); twoJ must have the parity of A
+ * (SMGPU_ERR_NUCLEUS otherwise). */
+int smgpu_problem_create_from_snt_J(const char* snt_path, const char* nucleus, int twoJ, int precision,
+                                    smgpu_problem** out);
+
 /* Same, from an in-memory description (the data of the reference's SMobject,
  * shellmodel_main.jl:38-53). */
 int smgpu_problem_create(const smgpu_problem_desc* desc, int precision, smgpu_problem** out);
@@ -131,6 +137,19 @@ int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int ma
  * J(J+1) - j_a(j_a+1) - j_b(j_b+1) per pair). */
 int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out);
 
+/* J-projected ("double") Lanczos for the lowest num_ev states of total
+ * angular momentum twoJ/2: TRL with doubleLanczos = true
+ * (lanczos_methods.jl:1-91) — every new Krylov vector is projected onto J by
+ * an inner Lanczos on J^2 (Jlanczos / ThickRestart_J, :93-151, tolerance
+ * 1e-7 on J(J+1)) and re-orthogonalised.  The handle must come from
+ * smgpu_problem_create_from_snt_J with the same twoJ; ls >= 2 (it is also
+ * the length of the inner Lanczos).  Arguments and outputs as smgpu_solve;
+ * J^2 is built on the first call (as smgpu_jj).  Runs in FP64 for either
+ * precision of the handle (FP32 Krylov vectors hold rounding components of
+ * every J, from which lower-lying states of other J re-emerge). */
+int smgpu_solve_J(smgpu_problem* h, int twoJ, int num_ev, int lm, int ls, double tol, int max_restarts,
+                  const double* v1, double* evals_out, double* evecs_out, int* stats_out);
+
 /* Seconds spent in the phases of the last create / solve / matvec call (the
  * reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos", "Rvecs",
  * shellmodel_main.jl:137,159,208).  times_out: 8 doubles:
@@ -173,6 +192,21 @@ int smgpu_stats(const smgpu_problem* h, long long* stats_out);
  * the array (each call rewrites every entry it reads), so calls that overlap
  * on the GPU race; the call returns when w and *vhv are ready. */
 int smgpu_matvec_noalloc(smgpu_problem* h, const double* v, double* w, double* vhv);
+
+/* ------------------------------------------------------------------------
+ * `.wav` files (writeRitzvecs / read_wav / read_appwav,
+ * src/ShellModel/shellmodel_main.jl:967-1003,1215-1229): int32 neig, int32
+ * Mtot (doubled), float64 E[neig], int32 2J[neig], float64 V[neig][mdim],
+ * native little-endian.  Host-only calls (no GPU needed); errors are
+ * reported by smgpu_wav_last_error(). */
+int smgpu_write_wav(const char* path, long long mdim, int mtot2, int nev, const double* evals, const int* twoJ,
+                    const double* vecs);
+/* Number of vectors and Mtot of a file whose size matches dimension mdim. */
+int smgpu_read_wav_header(const char* path, long long mdim, int* nev, int* mtot2);
+/* The first min(neig, nev_max) energies, 2J labels and vectors (any output
+ * may be NULL). */
+int smgpu_read_wav(const char* path, long long mdim, int nev_max, double* evals, int* twoJ, double* vecs);
+const char* smgpu_wav_last_error(void);
 
 /* ------------------------------------------------------------------------
  * Interaction samples sharing one basis (the sample loop of prepEC,

@@ -195,6 +195,30 @@ int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision
   return SMGPU_OK;
 }
 
+// J^2 as an FP64 operator on the basis of h (built on first use).
+smgpu_problem* ensure_jj_op(smgpu_problem* h) {
+  if (!h->jj_op) {
+    smgpu_problem* q = new smgpu_problem();
+    try {
+      q->precision = SMGPU_FP64;
+      q->vp = h->vp;
+      q->vn = h->vn;
+      q->mtot2 = h->mtot2;
+      q->I = jj_interaction(h->I);
+      build_tables(q->I, h->vp, h->vn, h->mtot2, q->T);
+      if (q->T.mdim != h->T.mdim || q->T.pbits != h->T.pbits || q->T.nbits != h->T.nbits ||
+          q->T.stride != h->T.stride)
+        throw SetupError{SMGPU_ERR_DEVICE, "J^2 basis differs from the problem's basis"};
+      q->upload(false);
+    } catch (...) {
+      delete q;
+      throw;
+    }
+    h->jj_op = q;
+  }
+  return h->jj_op;
+}
+
 // ------------------------------------------------------------------ solver
 template <class TX>
 struct Solve {
@@ -319,6 +343,262 @@ struct Solve {
     return ex;
   }
 
+  // ---- J projection (doubleLanczos, lanczos_methods.jl:1-151): an inner
+  // Lanczos on J^2 = J-J+ + M(M+1) (the basis has M = J) projects every new
+  // Krylov vector onto J.  Vector work on the device, the small matrices of
+  // the inner Lanczos on the host with their eigen-decompositions on the
+  // device; control flow as the reference's Jlanczos / ThickRestart_J.
+  smgpu_problem* Jop = nullptr;
+  double eval_jj = -1.0;
+  int lnJ = 0;
+  double* Q = nullptr;    // lnJ x len inner Krylov vectors (FP64)
+  double* jx = nullptr;   // combination / projected vector
+  double* js = nullptr;   // device dot products (lm + 2)
+  double* jn = nullptr;   // device norms (2)
+  double* jT = nullptr;   // small matrix for the device eigensolver
+  double* jA = nullptr;
+  double* jZ = nullptr;
+  double* jev = nullptr;
+  std::vector<double> Jm;  // inner Lanczos matrix (host, lnJ x lnJ, column-major)
+
+  void alloc_j(int ls) {
+    DeviceArena& A = P->solver;
+    lnJ = ls;
+    Q = A.alloc<double>((size_t)lnJ * L.len);
+    jx = A.alloc<double>(L.len);
+    js = A.alloc<double>((size_t)L.lm + 2);
+    jn = A.alloc<double>(2);
+    jT = A.alloc<double>((size_t)lnJ * lnJ);
+    jA = A.alloc<double>((size_t)lnJ * lnJ);
+    jZ = A.alloc<double>((size_t)lnJ * lnJ);
+    jev = A.alloc<double>(lnJ);
+    SMGPU_CUDA_TRY(cudaMemsetAsync(Q, 0, sizeof(double) * (size_t)lnJ * L.len, P->st));
+  }
+  double host_scalar(const double* d) {
+    double x = 0.0;
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(&x, d, sizeof(double), cudaMemcpyDeviceToHost, P->st));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+    return x;
+  }
+  // eigenvalues (ascending) and eigenvectors (column-major) of Jm[0:n,0:n]
+  void small_eig(int n, std::vector<double>& vals, std::vector<double>* vecs) {
+    std::vector<double> sub((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) sub[(size_t)j * n + i] = Jm[(size_t)j * lnJ + i];
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(jT, sub.data(), sizeof(double) * sub.size(), cudaMemcpyHostToDevice, P->st));
+    launch_small_eig(jT, n, jA, jZ, jev, P->st);
+    vals.resize(n);
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(vals.data(), jev, sizeof(double) * n, cudaMemcpyDeviceToHost, P->st));
+    if (vecs) {
+      vecs->resize((size_t)n * n);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(vecs->data(), jA, sizeof(double) * n * n, cudaMemcpyDeviceToHost, P->st));
+    }
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+  }
+  // y -= its components along the first m columns of X (two CGS passes)
+  template <class TY>
+  void cgs(const TY* X, int m, double* y) {
+    for (int pass = 0; pass < 2 && m > 0; ++pass) {
+      launch_multidot<TY>(L, X, m, y, false, P->st);
+      launch_reduce(L, m, RED_STORE, js, P->st);
+      launch_axpy_dev<TY>(X, L.len, m, js, y, L.len, P->st);
+    }
+  }
+  // ||y||; y /= ||y|| into out
+  template <class TO>
+  double normalize(const double* y, TO* out) {
+    launch_multidot<double>(L, y, 1, y, false, P->st);
+    launch_reduce(L, 1, RED_STORE, jn, P->st);
+    launch_reduce(L, 1, RED_INVNORM, jn + 1, P->st);
+    launch_scale_store<TO>(L, y, out, jn + 1, P->st);
+    return std::sqrt(host_scalar(jn));
+  }
+  // lanczos_methods.jl:132-151 with ls = 1 (the arrow element goes to row 2
+  // and column k, as in the reference)
+  void thick_restart_j(int lmj) {
+    const int m = lmj - 1;
+    std::vector<double> vals, vecs;
+    small_eig(m, vals, &vecs);
+    int k = 0;
+    for (int i = 1; i < m; ++i)
+      if (std::fabs(vals[i] - eval_jj) < std::fabs(vals[k] - eval_jj)) k = i;
+    const double beta = Jm[(size_t)(lmj - 1) * lnJ + (lmj - 2)];
+    std::fill(Jm.begin(), Jm.end(), 0.0);
+    Jm[0] = vals[k];
+    const double tmp = beta * vecs[(size_t)k * m + (m - 1)];
+    Jm[(size_t)k * lnJ + 1] = tmp;
+    Jm[(size_t)1 * lnJ + k] = tmp;
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(js, vecs.data() + (size_t)k * m, sizeof(double) * m, cudaMemcpyHostToDevice, P->st));
+    launch_combine(Q, L.len, m, js, jx, L.len, P->st);
+    normalize<double>(jx, Q);
+    if (lmj - 1 != 1)
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(Q + L.len, Q + (size_t)(lmj - 1) * L.len, sizeof(double) * L.len,
+                                     cudaMemcpyDeviceToDevice, P->st));
+    if (lnJ > 2)
+      SMGPU_CUDA_TRY(cudaMemsetAsync(Q + 2 * L.len, 0, sizeof(double) * (size_t)(lnJ - 2) * L.len, P->st));
+  }
+  // lanczos_methods.jl:93-131 Jlanczos on Q[0] (Q[0] returns the projection)
+  void jlanczos() {
+    const double Jtol = 1.e-7;
+    Jm.assign((size_t)lnJ * lnJ, 0.0);
+    auto JM = [&](int i, int j) -> double& { return Jm[(size_t)(j - 1) * lnJ + (i - 1)]; };
+    int eljit = 1, k = 1, inow = k, rounds = 0;
+    bool JTF = false;
+    std::vector<double> vals;
+    while (!JTF) {
+      if (++rounds > 1000) throw SetupError{SMGPU_ERR_NOCONV, "J projection did not converge"};
+      for (int it = k; it <= lnJ - 1; ++it) {
+        inow = it;
+        double* vk = Q + (size_t)(it - 1) * L.len;
+        double* vkp1 = Q + (size_t)it * L.len;
+        Jop->hv((const double*)vk, vkp1, HvEpilogue<double>{}, P->st);  // J^2 vk = (J-J+ + eval_jj) vk
+        launch_multidot<double>(L, vk, 1, vkp1, false, P->st);
+        launch_reduce(L, 1, RED_STORE, js, P->st);
+        JM(it, it) = host_scalar(js);
+        small_eig(it, vals, nullptr);
+        if (std::fabs(vals[0] - eval_jj) < Jtol) {
+          eljit = it;
+          JTF = true;
+          break;
+        }
+        cgs<double>(Q, it, vkp1);
+        const double beta = normalize<double>(vkp1, vkp1);
+        JM(it + 1, it) = beta;
+        JM(it, it + 1) = beta;
+        eljit = it;
+      }
+      if (!JTF) {
+        thick_restart_j(eljit + 1);
+        k = 2;
+      }
+    }
+    if (inow > k) thick_restart_j(eljit + 1);
+  }
+  // Krylov vector `slot` := its J projection, re-orthogonalised against the
+  // slots before it and normalised (lanczos_methods.jl:24-28,64-76).
+  void project(int slot) {
+    TX* v = V + (size_t)slot * L.len;
+    if (lnJ > 1)
+      SMGPU_CUDA_TRY(cudaMemsetAsync(Q + L.len, 0, sizeof(double) * (size_t)(lnJ - 1) * L.len, P->st));
+    launch_widen<TX>(v, Q, L.len, P->st);
+    jlanczos();
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(jx, Q, sizeof(double) * L.len, cudaMemcpyDeviceToDevice, P->st));
+    cgs<TX>(V, slot, jx);
+    normalize<TX>(jx, v);
+  }
+
+  int run_projected(int num_ev, int lm, int ls, double tol, int max_restarts, const double* v1,
+                    double* evals_out, double* evecs_out, int* stats_out) {
+    const int64_t mdim = P->T.mdim;
+    const int nev = (int)std::min<int64_t>(num_ev, mdim);
+    const double tw0 = now_s();
+    alloc(lm, ls, num_ev, tol);
+    alloc_j(ls);
+    cudaStream_t s = P->st, s2 = P->st2;
+    double* v1dev = nullptr;
+    if (v1) {
+      v1dev = P->solver.alloc<double>(mdim);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(v1dev, v1, sizeof(double) * mdim, cudaMemcpyHostToDevice, s));
+    }
+    cudaEvent_t e0, e1, e2, e_fork;
+    SMGPU_CUDA_TRY(cudaEventCreate(&e0));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e1));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e2));
+    SMGPU_CUDA_TRY(cudaEventCreateWithFlags(&e_fork, cudaEventDisableTiming));
+    SMGPU_CUDA_TRY(cudaEventRecord(e0, s));
+    if (v1dev) launch_to_padded<double>(P->dt, v1dev, w, s);
+    else launch_start_vector(P->dt, 1234ull, w, s);
+    init_start();
+    // the start vector is projected and normalised (lanczos_methods.jl:24-28)
+    launch_widen<TX>(V, Q, L.len, s);
+    jlanczos();
+    normalize<TX>(Q, V);
+    int n_restart = 0, status = SMGPU_OK, elit = 0, n_hv = 0;
+    bool done = false;
+    LanczosFlags fl{};
+    int kstart = 1, lock = 0;
+    while (true) {
+      for (int it = kstart; it <= lm - 1; ++it) {
+        iteration(it, lock, e_fork);
+        ++n_hv;
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(s2));
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(&fl, L.fl, sizeof(LanczosFlags), cudaMemcpyDeviceToHost, s));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+        if (fl.done) {
+          done = true;
+          elit = fl.elit;
+          break;
+        }
+        if (fl.exhausted) {
+          done = true;
+          elit = fl.exh_k;
+          break;
+        }
+        const double tbeta = host_scalar(L.T + (size_t)(it - 1) * lm + it);
+        if (tbeta < 1.e-7) {  // lanczos_methods.jl:65
+          done = true;
+          elit = it;
+          break;
+        }
+        project(it);
+      }
+      if (done) break;
+      ++n_restart;
+      if (n_restart > max_restarts) {
+        status = SMGPU_ERR_NOCONV;
+        break;
+      }
+      restart(s);
+      kstart = ls + 1;
+      lock = ls;
+    }
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(evals_out, L.en, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
+    SMGPU_CUDA_TRY(cudaEventRecord(e1, s));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    if (status == SMGPU_ERR_NOCONV) elit = 0;
+    long long launches = 0;
+    if (evecs_out && elit > 0) {
+      double* R = P->solver.alloc<double>((size_t)nev * L.len);
+      double* tmp = P->solver.alloc<double>(mdim);
+      launch_jacobi(L, elit, false, s);
+      launch_ritz<TX>(L, V, elit, nev, R, s);
+      for (int e = 0; e < nev; ++e) {
+        double* r = R + (size_t)e * L.len;
+        launch_multidot<double>(L, r, 1, r, false, s);
+        launch_reduce(L, 1, RED_INVNORM, L.h + e, s);
+        launch_scale_store<double>(L, r, r, L.h + e, s);
+        launch_from_padded(P->dt, r, tmp, s);
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(evecs_out + (size_t)e * mdim, tmp, sizeof(double) * mdim,
+                                       cudaMemcpyDeviceToHost, s));
+      }
+    }
+    SMGPU_CUDA_TRY(cudaEventRecord(e2, s));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(s));
+    SMGPU_CUDA_TRY(cudaGetLastError());
+    float ms1 = 0.f, ms2 = 0.f;
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms1, e0, e1));
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms2, e1, e2));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    cudaEventDestroy(e_fork);
+    if (fl.bad) return fail(P, SMGPU_ERR_DEVICE, "restart Gram matrix was not positive definite");
+    if (stats_out) {
+      stats_out[0] = elit;
+      stats_out[1] = n_hv;
+      stats_out[2] = n_restart;
+      stats_out[3] = done ? 1 : 0;
+      stats_out[4] = nev;
+      stats_out[5] = fl.n_second;
+      stats_out[6] = (int)launches;
+      stats_out[7] = 0;
+    }
+    P->times[1] = ms1 * 1e-3;
+    P->times[4] = ms2 * 1e-3;
+    P->times[5] = now_s() - tw0;
+    return status;
+  }
+
   int run(int num_ev, int lm, int ls, double tol, int max_restarts, const double* v1, double* evals_out,
           double* evecs_out, int* stats_out) {
     const int64_t mdim = P->T.mdim;
@@ -441,6 +721,21 @@ int smgpu_problem_create_from_snt(const char* snt_path, const char* nucleus, int
     if (vp < 0 || vn < 0) throw SetupError{SMGPU_ERR_NUCLEUS, "nucleus lies below the snt core"};
     int mtot2 = (A % 2 == 0) ? 0 : 1;  // shellmodel_main.jl:110
     return create_common(I, vp, vn, mtot2, precision, out);
+  });
+}
+
+int smgpu_problem_create_from_snt_J(const char* snt_path, const char* nucleus, int twoJ, int precision,
+                                    smgpu_problem** out) {
+  if (!snt_path || !nucleus || !out || twoJ < 0) return fail(nullptr, SMGPU_ERR_ARG, "null argument or negative 2J");
+  *out = nullptr;
+  return guarded(nullptr, [&]() {
+    int A = 0, Z = 0;
+    parse_nucleus(nucleus, A, Z);
+    if (A % 2 != twoJ % 2) throw SetupError{SMGPU_ERR_NUCLEUS, "invalid target J for this nucleus"};  // :116
+    Interaction I = read_snt(snt_path, A);
+    int vp = Z - I.cp, vn = (A - Z) - I.cn;
+    if (vp < 0 || vn < 0) throw SetupError{SMGPU_ERR_NUCLEUS, "nucleus lies below the snt core"};
+    return create_common(I, vp, vn, twoJ, precision, out);  // Mtot = tJ (:113)
   });
 }
 
@@ -636,6 +931,28 @@ int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int ma
   });
 }
 
+int smgpu_solve_J(smgpu_problem* h, int twoJ, int num_ev, int lm, int ls, double tol, int max_restarts,
+                  const double* v1, double* evals_out, double* evecs_out, int* stats_out) {
+  if (!h || !evals_out) return fail(h, SMGPU_ERR_ARG, "null argument");
+  if (num_ev < 1 || lm < 3 || ls < 2 || ls > lm - 2 || ls > 60 || lm > 1000 || num_ev > lm - 1 || !(tol > 0.0))
+    return fail(h, SMGPU_ERR_ARG, "need 1 <= num_ev < lm, 2 <= ls <= min(lm-2, 60), lm <= 1000, tol > 0");
+  if (twoJ != h->mtot2)
+    return fail(h, SMGPU_ERR_ARG, "the handle's basis has 2M = " + std::to_string(h->mtot2) +
+                                      "; create it with smgpu_problem_create_from_snt_J for 2J = " +
+                                      std::to_string(twoJ));
+  return guarded(h, [&]() {
+    const double eval_jj = 0.5 * twoJ * (0.5 * twoJ + 1.0);  // shellmodel_main.jl:114
+    // FP64 in both forms: FP32 Krylov vectors carry rounding components of
+    // every J at 1e-7, from which the Lanczos process recovers lower-lying
+    // states of other J faster than the projection removes them.
+    h->ensure_fp64();
+    Solve<double> s{h};
+    s.Jop = ensure_jj_op(h);
+    s.eval_jj = eval_jj;
+    return s.run_projected(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
+  });
+}
+
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out) {
   if (!h || !ms_out || reps < 1) return fail(h, SMGPU_ERR_ARG, "bad time_matvec arguments");
   return guarded(h, [&]() {
@@ -684,25 +1001,7 @@ int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out) 
 int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out) {
   if (!h || !vecs || !jj_out || nvec < 1) return fail(h, SMGPU_ERR_ARG, "bad jj arguments");
   return guarded(h, [&]() {
-    if (!h->jj_op) {
-      smgpu_problem* q = new smgpu_problem();
-      try {
-        q->precision = SMGPU_FP64;
-        q->vp = h->vp;
-        q->vn = h->vn;
-        q->mtot2 = h->mtot2;
-        q->I = jj_interaction(h->I);
-        build_tables(q->I, h->vp, h->vn, h->mtot2, q->T);
-        if (q->T.mdim != h->T.mdim || q->T.pbits != h->T.pbits || q->T.nbits != h->T.nbits)
-          throw SetupError{SMGPU_ERR_DEVICE, "J^2 basis differs from the problem's basis"};
-        q->upload(false);
-      } catch (...) {
-        delete q;
-        throw;
-      }
-      h->jj_op = q;
-    }
-    smgpu_problem* q = h->jj_op;
+    smgpu_problem* q = ensure_jj_op(h);
     const int64_t mdim = h->T.mdim, len = q->T.len_pad;
     DeviceArena tmp;
     try {

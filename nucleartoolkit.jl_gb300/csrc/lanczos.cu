@@ -557,6 +557,46 @@ __global__ void __launch_bounds__(kNT) k_ritz(const TX* __restrict__ V, const do
   }
 }
 
+// ---------------------------------------------------------------------------
+// Vector helpers of the J-projected Lanczos (lanczos_methods.jl:93-151).
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_widen(const TX* __restrict__ in, double* __restrict__ out, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
+    out[i] = (double)in[i];
+}
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_narrow(const double* __restrict__ in, TX* __restrict__ out, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
+    out[i] = (TX)in[i];
+}
+// y -= Σ_{j<m} h_j X_j  (h on the device)
+template <class TX>
+__global__ void __launch_bounds__(kNT) k_axpy_dev(const TX* __restrict__ X, int64_t ld, int m,
+                                                  const double* __restrict__ h, double* __restrict__ y, int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    double t = y[i];
+    for (int j = 0; j < m; ++j) t = fma(-h[j], (double)X[(int64_t)j * ld + i], t);
+    y[i] = t;
+  }
+}
+// out = Σ_{j<m} c_j Q_j  (c on the device, column stride cst)
+__global__ void __launch_bounds__(kNT) k_combine(const double* __restrict__ Q, int64_t ld, int m,
+                                                 const double* __restrict__ c, double* __restrict__ out,
+                                                 int64_t len) {
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    double t = 0.0;
+    for (int j = 0; j < m; ++j) t = fma(c[j], Q[(int64_t)j * ld + i], t);
+    out[i] = t;
+  }
+}
+
+// Eigen-decomposition of a small symmetric matrix in device memory (column-
+// major n x n, ld n): one CTA of parallel Jacobi.
+__global__ void __launch_bounds__(256) k_small_eig(const double* __restrict__ T, int n, double* A, double* Z,
+                                                   double* evals) {
+  jacobi_eig<256>(T, n, n, A, Z, evals);
+}
+
 inline int grid_for(int64_t len) {
   int64_t g = (len + kNT - 1) / kNT;
   if (g > 152 * 8) g = 152 * 8;
@@ -644,6 +684,27 @@ void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R,
   k_ritz<TX><<<grid_for(L.len), kNT, 0, st>>>(V, L.jacA, elit, nev, R, L.len);
 }
 
+template <class TX>
+void launch_widen(const TX* in, double* out, int64_t len, cudaStream_t st) {
+  k_widen<TX><<<grid_for(len), kNT, 0, st>>>(in, out, len);
+}
+template <class TX>
+void launch_narrow(const double* in, TX* out, int64_t len, cudaStream_t st) {
+  k_narrow<TX><<<grid_for(len), kNT, 0, st>>>(in, out, len);
+}
+template <class TX>
+void launch_axpy_dev(const TX* X, int64_t ld, int m, const double* h, double* y, int64_t len, cudaStream_t st) {
+  k_axpy_dev<TX><<<grid_for(len), kNT, 0, st>>>(X, ld, m, h, y, len);
+}
+void launch_combine(const double* Q, int64_t ld, int m, const double* c, double* out, int64_t len, cudaStream_t st) {
+  k_combine<<<grid_for(len), kNT, 0, st>>>(Q, ld, m, c, out, len);
+}
+void launch_small_eig(const double* T, int n, double* A, double* Z, double* evals, cudaStream_t st) {
+  const int N = n + (n & 1);
+  const size_t shm = sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+  k_small_eig<<<1, 256, shm, st>>>(T, n, A, Z, evals);
+}
+
 #define SMGPU_INST(TX)                                                                                       \
   template void launch_to_padded<TX>(const DevTables&, const double*, TX*, cudaStream_t);                    \
   template void launch_multidot<TX>(const LanczosDev&, const TX*, int, const double*, bool, cudaStream_t);   \
@@ -652,7 +713,10 @@ void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R,
   template void launch_restart_rotate<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                  \
   template void launch_gram<TX>(const LanczosDev&, const TX*, const TX*, cudaStream_t);                      \
   template void launch_restart_apply<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                   \
-  template void launch_ritz<TX>(const LanczosDev&, const TX*, int, int, double*, cudaStream_t);
+  template void launch_ritz<TX>(const LanczosDev&, const TX*, int, int, double*, cudaStream_t);               \
+  template void launch_widen<TX>(const TX*, double*, int64_t, cudaStream_t);                                 \
+  template void launch_narrow<TX>(const double*, TX*, int64_t, cudaStream_t);                                \
+  template void launch_axpy_dev<TX>(const TX*, int64_t, int, const double*, double*, int64_t, cudaStream_t);
 SMGPU_INST(double)
 SMGPU_INST(float)
 #undef SMGPU_INST

@@ -65,6 +65,16 @@ template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st);
 template <class TX>
 void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R, cudaStream_t st);
+// J-projected Lanczos helpers: FP64 copies, y -= Σ h_j X_j, out = Σ c_j Q_j,
+// and a one-CTA eigen-decomposition of a small matrix in device memory.
+template <class TX>
+void launch_widen(const TX* in, double* out, int64_t len, cudaStream_t st);
+template <class TX>
+void launch_narrow(const double* in, TX* out, int64_t len, cudaStream_t st);
+template <class TX>
+void launch_axpy_dev(const TX* X, int64_t ld, int m, const double* h, double* y, int64_t len, cudaStream_t st);
+void launch_combine(const double* Q, int64_t ld, int m, const double* c, double* out, int64_t len, cudaStream_t st);
+void launch_small_eig(const double* T, int n, double* A, double* Z, double* evals, cudaStream_t st);
 template <class TX>
 void launch_to_padded(const DevTables& t, const double* src, TX* dst, cudaStream_t st);
 void launch_from_padded(const DevTables& t, const double* src, double* dst, cudaStream_t st);

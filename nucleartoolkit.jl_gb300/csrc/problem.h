@@ -205,6 +205,15 @@ struct smgpu_problem {
     set_config(128, 4, 1);
   }
 
+  // FP64 coefficient tables for a handle created in the mixed form (the
+  // J-projected solve always runs in FP64).
+  void ensure_fp64() {
+    if (c64.pp_val) return;
+    c64.pp_val = tables.upload(T.pp_val);
+    c64.nn_val = tables.upload(T.nn_val);
+    c64.vtab = tables.upload(signed_vtab(T));
+  }
+
   void hv(const double* v, double* w, const HvEpilogue<double>& epi, cudaStream_t s) {
     launch_hv_fp64(dt, tt, cfg, d_ep, d_en, c64, v, w, epi, s);
   }

@@ -28,6 +28,7 @@ MIXED = 1
 _vp = C.c_void_p
 SIGNATURES = {
     "smgpu_problem_create_from_snt": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(_vp)]),
+    "smgpu_problem_create_from_snt_J": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(_vp)]),
     "smgpu_problem_create": (C.c_int, [_vp, C.c_int, C.POINTER(_vp)]),
     "smgpu_problem_destroy": (C.c_int, [_vp]),
     "smgpu_last_error": (C.c_char_p, [_vp]),
@@ -38,10 +39,15 @@ SIGNATURES = {
     "smgpu_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
     "smgpu_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_jj": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "smgpu_solve_J": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "smgpu_matvec_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "smgpu_write_wav": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, C.c_int, _vp, _vp, _vp]),
+    "smgpu_read_wav_header": (C.c_int, [C.c_char_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "smgpu_read_wav": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, _vp, _vp, _vp]),
+    "smgpu_wav_last_error": (C.c_char_p, []),
     "smgpu_multi_create_from_snt": (C.c_int, [C.POINTER(C.c_char_p), C.c_int, C.c_char_p, C.POINTER(_vp)]),
     "smgpu_multi_destroy": (C.c_int, [_vp]),
     "smgpu_multi_last_error": (C.c_char_p, [_vp]),
@@ -112,4 +118,11 @@ def check_batch(code: int, handle=None):
     """check() for smgpu_batch handles."""
     if code != OK:
         msg = load().smgpu_batch_last_error(handle)
+        raise SmgpuError(code, (msg or b"").decode(errors="replace"))
+
+
+def check_wav(code: int):
+    """check() for the .wav calls."""
+    if code != OK:
+        msg = load().smgpu_wav_last_error()
         raise SmgpuError(code, (msg or b"").decode(errors="replace"))

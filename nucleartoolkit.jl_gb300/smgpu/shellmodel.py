@@ -21,10 +21,16 @@ def _p(a):
 class ShellModelProblem:
     """One M-scheme problem resident on the GPU (an ``smgpu_problem`` handle)."""
 
-    def __init__(self, sntf: str, target_nuc: str, precision: int = FP64):
+    def __init__(self, sntf: str, target_nuc: str, precision: int = FP64, twoJ=None):
+        """twoJ: build the basis of Mtot = twoJ for the J-projected solve
+        (main_sm's target_J = [twoJ]); None: Mtot = A mod 2."""
         L = load()
         h = C.c_void_p()
-        rc = L.smgpu_problem_create_from_snt(os.fsencode(sntf), target_nuc.encode(), int(precision), C.byref(h))
+        if twoJ is None:
+            rc = L.smgpu_problem_create_from_snt(os.fsencode(sntf), target_nuc.encode(), int(precision), C.byref(h))
+        else:
+            rc = L.smgpu_problem_create_from_snt_J(os.fsencode(sntf), target_nuc.encode(), int(twoJ), int(precision),
+                                                   C.byref(h))
         check(rc, None)
         self._h = h
         self.precision = precision
@@ -40,6 +46,7 @@ class ShellModelProblem:
         self.Mp = np.zeros(self.nblocks, dtype=np.int32)
         self.Mn = np.zeros(self.nblocks, dtype=np.int32)
         check(L.smgpu_blocks(h, _p(self.np_), _p(self.nn_), _p(self.Mp), _p(self.Mn)), h)
+        self.mtot2 = int(self.Mp[0] + self.Mn[0]) if self.nblocks else 0  # doubled total M
 
     def close(self):
         if getattr(self, "_h", None):
@@ -104,14 +111,20 @@ class ShellModelProblem:
         check(load().smgpu_matvec(self._h, _p(v), _p(w), ncols, 1 if accumulate else 0), self._h)
         return w
 
-    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False):
+    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False, twoJ=None):
+        """Lowest num_ev eigenvalues; twoJ: J-projected (double) Lanczos for
+        total angular momentum twoJ/2 (the handle must have Mtot = twoJ)."""
         nev = min(num_ev, self.mdim)
         ev = np.zeros(nev)
         vecs = np.zeros((nev, self.mdim)) if want_vecs else None
         stats = np.zeros(8, dtype=np.int32)
         v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
-        rc = load().smgpu_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts), _p(v1a),
-                                _p(ev), _p(vecs), _p(stats))
+        if twoJ is None:
+            rc = load().smgpu_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts), _p(v1a),
+                                    _p(ev), _p(vecs), _p(stats))
+        else:
+            rc = load().smgpu_solve_J(self._h, int(twoJ), int(num_ev), int(lm), int(ls), float(tol),
+                                      int(max_restarts), _p(v1a), _p(ev), _p(vecs), _p(stats))
         if rc not in (_lib.OK, _lib.ERR_NOCONV):
             check(rc, self._h)
         return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_matvec=int(stats[1]), n_restart=int(stats[2]),
@@ -304,28 +317,51 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
     plain FP64 form or the FP32-mixed form.  Features of the reference outside
     the eigensolver path raise ``NotImplementedError``.
     """
+    tJ = None
     if target_J is not None and len(target_J) > 0:
-        raise NotImplementedError("J-projected Lanczos (target_J non-empty) is not in this library")
-    unsupported = dict(save_wav=save_wav, is_block=is_block, in_wf=bool(in_wf), calc_moment=calc_moment,
-                       calc_entropy=calc_entropy, visualize_occ=visualize_occ, print_evec=print_evec,
-                       truncation=bool(truncation_scheme), debugmode=bool(debugmode))
+        # shellmodel_main.jl:109-116: one target 2J; the basis has Mtot = 2J
+        if len(target_J) > 1:
+            raise ValueError("Invalid `target_J` Multiple J is not supported now.")
+        tJ = int(target_J[0])
+    unsupported = dict(is_block=is_block, calc_moment=calc_moment, calc_entropy=calc_entropy,
+                       visualize_occ=visualize_occ, print_evec=print_evec, truncation=bool(truncation_scheme),
+                       debugmode=bool(debugmode))
     bad = [k for k, v in unsupported.items() if v]
     if bad:
         raise NotImplementedError("not supported by the GPU eigensolver: " + ", ".join(bad))
     if num_history != 3:
         raise NotImplementedError("num_history other than 3")
-    P = ShellModelProblem(sntf, target_nuc, precision)
+    P = ShellModelProblem(sntf, target_nuc, precision, twoJ=tJ)
     if verbose:
-        print(f"{target_nuc:>6s}  mdim: {P.mdim:12d} ({np.log10(max(P.mdim, 1)):5.2f}) ")
+        print(f"{target_nuc:>6s}  mdim: {P.mdim:12d} ({np.log10(max(P.mdim, 1)):5.2f}) "
+              + (f" 2J={tJ}" if tJ is not None else ""))
     if mdimmode:
         P.close()
         return None
-    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, want_vecs=verbose)
+    v1 = None
+    if in_wf:
+        # read_appwav with q = 1: the first vector of the file starts the Lanczos
+        from .wav import read_wav
+        v1, _ = read_wav(in_wf, P.mdim, 1)
+    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, v1=v1, want_vecs=verbose or save_wav,
+                twoJ=tJ)
     en = list(map(float, r["evals"]))
-    if verbose:
-        if r["status"] == _lib.OK:
-            # J labels of the Ritz vectors (shellmodel_main.jl:226-240,257)
-            print("J " + str([J_from_JJ1(x) for x in P.jj(r["evecs"])]))
+    totJs = None
+    if r["status"] == _lib.OK and r["evecs"] is not None:
+        # J labels of the Ritz vectors (shellmodel_main.jl:226-240)
+        totJs = [J_from_JJ1(x) for x in P.jj(r["evecs"])]
+    if save_wav and totJs is not None:
+        # writeRitzvecs to ./<nucleus>_<interaction>.wav (:248-253)
+        from .wav import write_wav
+        csnt = os.path.basename(sntf).split(".")[0]
+        oupf = f"./{target_nuc}_{csnt}.wav" if tJ is None else f"./{target_nuc}_{csnt}_j{tJ}.wav"
+        write_wav(oupf, P.mtot2, en, [int(2 * j) for j in totJs], r["evecs"])
+    if verbose and tJ is not None:
+        # :261-264
+        print(f"2J= {int(2 * totJs[0]) if totJs else tJ}  En." + " ".join(f"{x:12.5f}" for x in en))
+    elif verbose:
+        if totJs is not None:
+            print("J " + str(totJs))
         print("En. " + " ".join(f"{x:10.4f}" for x in en))
         print("Ex. " + " ".join(f"{x - en[0]:10.4f}" for x in en))
         if is_show:

@@ -53,7 +53,9 @@ def lib():
         L.orc_start_vector.argtypes = [C.c_longlong, C.c_ulonglong, C.c_void_p]
         L.orc_trl.restype = C.c_int
         L.orc_trl.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
-                              C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                              C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.orc_create_M.restype = vp
+        L.orc_create_M.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
         L.orc_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_trl_sample.restype = C.c_int
         L.orc_trl_sample.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]
@@ -100,9 +102,14 @@ class OracleProblem:
     """One shell-model problem set up exactly as ``main_sm`` does it
     (readsmsnt → occ → prep_Hamil_T1 → prep_Hamil_pn → prep_pn)."""
 
-    def __init__(self, sntf: str, nuc: str):
+    def __init__(self, sntf: str, nuc: str, mtot2=None):
+        """mtot2: doubled total M of the basis (None: A mod 2, as main_sm
+        without target_J; target_J = [tJ] uses mtot2 = tJ)."""
         L = lib()
-        self._h = L.orc_create(os.fsencode(sntf), nuc.encode())
+        if mtot2 is None:
+            self._h = L.orc_create(os.fsencode(sntf), nuc.encode())
+        else:
+            self._h = L.orc_create_M(os.fsencode(sntf), nuc.encode(), int(mtot2))
         if not self._h:
             raise ValueError("oracle: " + L.orc_last_error().decode())
         self.mdim = int(L.orc_mdim(self._h))
@@ -205,7 +212,10 @@ class OracleProblem:
         return dict(t_hv=out[0], t_reorth=out[1], t_restart=out[2], t_total=out[3], n_hv=int(out[4]),
                     n_restart=int(out[5]))
 
-    def trl(self, num_ev, lm=300, ls=20, tol=1e-8, max_restart=10000, v1=None, seed=1234, want_vecs=False):
+    def trl(self, num_ev, lm=300, ls=20, tol=1e-8, max_restart=10000, v1=None, seed=1234, want_vecs=False,
+            eval_jj=None):
+        """TRL; eval_jj = J(J+1) turns on the J-projected double Lanczos
+        (target_J; the basis must have M = J)."""
         L = lib()
         k = min(num_ev, self.mdim)
         ev = np.zeros(k)
@@ -217,7 +227,8 @@ class OracleProblem:
             v1 = np.ascontiguousarray(v1, dtype=np.float64)
             v1p = _p(v1)
         rc = L.orc_trl(self._h, num_ev, lm, ls, tol, max_restart, v1p, seed, _p(ev),
-                       _p(vecs) if want_vecs else None, _p(stats), _p(times))
+                       _p(vecs) if want_vecs else None, _p(stats), _p(times),
+                       -1.0 if eval_jj is None else float(eval_jj))
         if rc != 0:
             raise RuntimeError("oracle TRL: " + L.orc_last_error().decode())
         return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_hv=int(stats[1]), n_restart=int(stats[2]),

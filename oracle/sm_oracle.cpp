@@ -994,10 +994,148 @@ void ReORTH(int it, double* vt, std::vector<std::vector<double>>& vks, i64 n) {
   }
 }
 
+// SD pair -> basis index, for the ladder operators below.
+struct PairHash {
+  size_t operator()(const std::pair<i64, i64>& k) const { return std::hash<i64>()(k.first * 1000003 + k.second); }
+};
+typedef std::unordered_map<std::pair<i64, i64>, i64, PairHash> BasisIndex;
+
+BasisIndex index_basis(const Problem& P) {
+  BasisIndex at;
+  const Basis& B = P.B;
+  for (size_t b = 0; b < B.pbits.size(); ++b)
+    for (size_t ip = 0; ip < B.pbits[b].size(); ++ip)
+      for (size_t in = 0; in < B.nbits[b].size(); ++in)
+        at[{B.pbits[b][ip], B.nbits[b][in]}] = B.tdims[b] + (i64)ip * (i64)B.nbits[b].size() + (i64)in;
+  return at;
+}
+
+// out = (J- J+) v on the M basis: the product that operate_J! applies
+// (shellmodel_main.jl:1566-1650, jump lists from prep_J :1439-1565),
+// restated with the ladder operators J+- = sum sqrt(j(j+1) - m(m+-1)) a+_{m+-1} a_m
+// over both species.  Neighbouring m-states of an orbit are adjacent in
+// construct_msps order, so every move has fermion sign +1.
+void operate_JmJp(const Problem& P, const BasisIndex& at, const double* v, double* out) {
+  const Basis& B = P.B;
+  const int Lp = (int)P.ms.p.size(), Ln = (int)P.ms.n.size();
+  std::unordered_map<std::pair<i64, i64>, double, PairHash> up;
+  for (size_t b = 0; b < B.pbits.size(); ++b)
+    for (size_t ip = 0; ip < B.pbits[b].size(); ++ip)
+      for (size_t in = 0; in < B.nbits[b].size(); ++in) {
+        const double c = v[B.tdims[b] + (i64)ip * (i64)B.nbits[b].size() + (i64)in];
+        if (c == 0.0) continue;
+        for (int sp = 0; sp < 2; ++sp) {
+          const auto& ms = sp == 0 ? P.ms.p : P.ms.n;
+          const int L = sp == 0 ? Lp : Ln;
+          const i64 bits = sp == 0 ? B.pbits[b][ip] : B.nbits[b][in];
+          for (int k = 1; k < L; ++k) {
+            if (ms[k][5] != ms[k - 1][5]) continue;
+            const i64 bk = onehot(L, k), bk1 = onehot(L, k + 1);
+            if (!(bits & bk) || (bits & bk1)) continue;
+            const double j2 = ms[k - 1][2], m2 = ms[k - 1][4];
+            const double f = 0.5 * std::sqrt(j2 * (j2 + 2.0) - m2 * (m2 + 2.0));
+            const i64 nb = bits ^ bk ^ bk1;
+            up[sp == 0 ? std::make_pair(nb, B.nbits[b][in]) : std::make_pair(B.pbits[b][ip], nb)] += f * c;
+          }
+        }
+      }
+  std::fill(out, out + P.mdim, 0.0);
+  for (const auto& kv : up) {
+    for (int sp = 0; sp < 2; ++sp) {
+      const auto& ms = sp == 0 ? P.ms.p : P.ms.n;
+      const int L = sp == 0 ? Lp : Ln;
+      const i64 bits = sp == 0 ? kv.first.first : kv.first.second;
+      for (int k = 1; k < L; ++k) {
+        if (ms[k][5] != ms[k - 1][5]) continue;
+        const i64 bk = onehot(L, k), bk1 = onehot(L, k + 1);
+        if (!(bits & bk1) || (bits & bk)) continue;
+        const double j2 = ms[k][2], m2 = ms[k][4];
+        const double f = 0.5 * std::sqrt(j2 * (j2 + 2.0) - m2 * (m2 - 2.0));
+        const i64 nb = bits ^ bk ^ bk1;
+        auto it = at.find(sp == 0 ? std::make_pair(nb, kv.first.second) : std::make_pair(kv.first.first, nb));
+        if (it != at.end()) out[it->second] += f * kv.second;
+      }
+    }
+  }
+}
+
+// lanczos_methods.jl:132-151 ThickRestart_J (ls = 1): keep the Ritz vector of
+// the eigenvalue closest to eval_jj; the arrow element goes to row ls+1 and
+// column k as in the reference.
+void ThickRestart_J(std::vector<std::vector<double>>& vks, std::vector<double>& Tm, int ldT, int lm, double eval_jj,
+                    i64 mdim) {
+  auto T = [&](int i, int j) -> double& { return Tm[(size_t)(j - 1) * ldT + (i - 1)]; };
+  const int m = lm - 1, ls = 1;
+  std::vector<double> sub((size_t)m * m), vals(m), vecs((size_t)m * m);
+  for (int j = 1; j <= m; ++j)
+    for (int i = 1; i <= m; ++i) sub[(size_t)(j - 1) * m + (i - 1)] = T(i, j);
+  sym_eig(m, sub.data(), vals.data(), vecs.data());
+  int k = 1;
+  for (int i = 2; i <= m; ++i)
+    if (std::fabs(vals[i - 1] - eval_jj) < std::fabs(vals[k - 1] - eval_jj)) k = i;
+  const double beta = T(lm - 1, lm);
+  std::fill(Tm.begin(), Tm.end(), 0.0);
+  T(1, 1) = vals[k - 1];
+  const double tmp = beta * vecs[(size_t)(k - 1) * m + (lm - 2)];
+  T(ls + 1, k) = tmp;
+  T(k, ls + 1) = tmp;
+  std::vector<double> uk(mdim, 0.0);
+  for (int j = 1; j <= m; ++j) axpy(mdim, vecs[(size_t)(k - 1) * m + (j - 1)], vks[j - 1].data(), uk.data());
+  const double nrm = 1.0 / std::sqrt(dotp(mdim, uk.data(), uk.data()));
+  for (i64 i = 0; i < mdim; ++i) vks[0][i] = uk[i] * nrm;
+  vks[1] = vks[lm - 1];
+  for (int kk = ls + 2; kk <= (int)vks.size(); ++kk) std::fill(vks[kk - 1].begin(), vks[kk - 1].end(), 0.0);
+}
+
+// lanczos_methods.jl:93-131 Jlanczos: Lanczos on J^2 = J-J+ + eval_jj (the
+// space has M = J) from Jvs[0] until the lowest Ritz value is within Jtol of
+// eval_jj; Jvs[0] returns the projection.
+void Jlanczos(const Problem& P, const BasisIndex& at, std::vector<std::vector<double>>& Jvs, double eval_jj,
+              double Jtol) {
+  const i64 mdim = P.mdim;
+  const int lnJ = (int)Jvs.size();
+  std::vector<double> Jmat((size_t)lnJ * lnJ, 0.0);
+  auto Jm = [&](int i, int j) -> double& { return Jmat[(size_t)(j - 1) * lnJ + (i - 1)]; };
+  int eljit = 1, k = 1, inow = k;
+  bool JTF = false;
+  std::vector<double> w;
+  while (!JTF) {
+    for (int it = k; it <= lnJ - 1; ++it) {
+      inow = it;
+      double* vk = Jvs[it - 1].data();
+      double* vkp1 = Jvs[it].data();
+      operate_JmJp(P, at, vk, vkp1);
+      axpy(mdim, eval_jj, vk, vkp1);
+      Jm(it, it) = dotp(mdim, vk, vkp1);
+      std::vector<double> sub((size_t)it * it);
+      for (int j = 1; j <= it; ++j)
+        for (int i = 1; i <= it; ++i) sub[(size_t)(j - 1) * it + (i - 1)] = Jm(i, j);
+      w.assign(it, 0.0);
+      sym_eig(it, sub.data(), w.data(), nullptr);
+      if (std::fabs(w[0] - eval_jj) < Jtol) {
+        eljit = it;
+        JTF = true;
+        break;
+      }
+      ReORTH(it, vkp1, Jvs, mdim);
+      const double beta = std::sqrt(dotp(mdim, vkp1, vkp1));
+      scal(mdim, 1.0 / beta, vkp1);
+      Jm(it + 1, it) = beta;
+      Jm(it, it + 1) = beta;
+      eljit = it;
+    }
+    if (!JTF) {
+      ThickRestart_J(Jvs, Jmat, lnJ, eljit + 1, eval_jj, mdim);
+      k = 2;
+    }
+  }
+  if (inow > k) ThickRestart_J(Jvs, Jmat, lnJ, eljit + 1, eval_jj, mdim);
+}
+
 // lanczos_methods.jl:1-91 TRL + 250-258 diagonalize_T! + 260-307 ThickRestart,
 // then shellmodel_main.jl:208-224 Ritz vectors.
 TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_restart, const double* v1,
-              u64 seed, bool want_vecs, int num_history, int max_hv = 0) {
+              u64 seed, bool want_vecs, int num_history, int max_hv = 0, double eval_jj = -1.0) {
   i64 mdim = P.mdim;
   num_ev = (int)std::min<i64>(num_ev, mdim);
   TrlResult R;
@@ -1012,6 +1150,19 @@ TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_
     for (i64 i = 0; i < mdim; ++i) vks[0][i] = start_elem(seed, i);
   }
   scal(mdim, 1.0 / std::sqrt(dotp(mdim, vks[0].data(), vks[0].data())), vks[0].data());
+  // doubleLanczos (target_J): J-projection of every new Krylov vector
+  const bool dl = eval_jj >= 0.0;
+  const double Jtol = 1.e-7;
+  std::vector<std::vector<double>> Jvs;
+  BasisIndex bindex;
+  if (dl) {
+    bindex = index_basis(P);
+    Jvs.assign(ls, std::vector<double>(mdim, 0.0));
+    Jvs[0] = vks[0];
+    Jlanczos(P, bindex, Jvs, eval_jj, Jtol);
+    vks[0] = Jvs[0];
+    scal(mdim, 1.0 / std::sqrt(dotp(mdim, vks[0].data(), vks[0].data())), vks[0].data());
+  }
   bool TF = false;
   int elit = 1, k = 1;
   std::vector<double> wbuf, Zbuf;
@@ -1049,6 +1200,15 @@ TrlResult TRL(const Problem& P, int num_ev, int lm, int ls, double tol, int max_
       scal(mdim, 1.0 / tbeta, vkp1);
       Tm(it + 1, it) = tbeta;
       Tm(it, it + 1) = tbeta;
+      if (dl) {
+        if (tbeta < Jtol) { TF = true; elit = it; break; }
+        for (size_t q = 1; q < Jvs.size(); ++q) std::fill(Jvs[q].begin(), Jvs[q].end(), 0.0);
+        std::memcpy(Jvs[0].data(), vkp1, sizeof(double) * mdim);
+        Jlanczos(P, bindex, Jvs, eval_jj, Jtol);
+        std::memcpy(vkp1, Jvs[0].data(), sizeof(double) * mdim);
+        ReORTH(it, vkp1, vks, mdim);
+        scal(mdim, 1.0 / std::sqrt(dotp(mdim, vkp1, vkp1)), vkp1);
+      }
       }
     }
     if (!TF) {
@@ -1105,7 +1265,7 @@ sample_end:
 }
 
 // shellmodel_main.jl:89-147 main_sm set-up (target_J = [], no truncation).
-Problem* build_problem(const std::string& sntf, const std::string& nuc, int nthreads_for_tasks) {
+Problem* build_problem(const std::string& sntf, const std::string& nuc, int nthreads_for_tasks, int mtot_override = -1) {
   Problem* P = new Problem();
   // util_func.jl:1 reg = r"[0-9]+": first run of digits is A
   size_t d0 = nuc.find_first_of("0123456789");
@@ -1115,6 +1275,11 @@ Problem* build_problem(const std::string& sntf, const std::string& nuc, int nthr
   P->Anum = std::stoi(anum);
   P->snt = readsmsnt(sntf, P->Anum);
   P->Mtot = (P->Anum % 2 == 0) ? 0 : 1;
+  // target_J = [tJ]: Mtot = tJ (shellmodel_main.jl:112-115)
+  if (mtot_override >= 0) {
+    if (mtot_override % 2 != P->Anum % 2) throw Err{"invalid target J for this nucleus"};
+    P->Mtot = mtot_override;
+  }
   // replace(target_nuc, string(Anum) => "")
   std::string el = nuc;
   size_t pos = el.find(std::to_string(P->Anum));
@@ -1163,6 +1328,17 @@ int orc_get_threads() { return n_threads(); }
 void* orc_create(const char* sntf, const char* nuc) {
   try {
     return build_problem(sntf, nuc, n_threads());
+  } catch (const Err& e) {
+    g_err = e.msg;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+  }
+  return nullptr;
+}
+// main_sm with target_J = [tJ]: the basis of Mtot = tJ (doubled).
+void* orc_create_M(const char* sntf, const char* nuc, int mtot) {
+  try {
+    return build_problem(sntf, nuc, n_threads(), mtot);
   } catch (const Err& e) {
     g_err = e.msg;
   } catch (const std::exception& e) {
@@ -1338,10 +1514,10 @@ void orc_start_vector(long long mdim, unsigned long long seed, double* v) {
 
 // Full thick-restart Lanczos.  stats: [elit, n_hv, n_restart, converged]; times: [t_hv, t_reorth, t_total].
 int orc_trl(void* h, int num_ev, int lm, int ls, double tol, int max_restart, const double* v1,
-            unsigned long long seed, double* evals, double* evecs, int* stats, double* times) {
+            unsigned long long seed, double* evals, double* evecs, int* stats, double* times, double eval_jj) {
   try {
     double t0 = now_s();
-    TrlResult R = TRL(*(Problem*)h, num_ev, lm, ls, tol, max_restart, v1, seed, evecs != nullptr, 3);
+    TrlResult R = TRL(*(Problem*)h, num_ev, lm, ls, tol, max_restart, v1, seed, evecs != nullptr, 3, 0, eval_jj);
     for (size_t i = 0; i < R.en.size(); ++i) evals[i] = R.en[i];
     if (evecs) std::memcpy(evecs, R.ritz.data(), sizeof(double) * R.ritz.size());
     if (stats) { stats[0] = R.elit; stats[1] = R.n_hv; stats[2] = R.n_restart; stats[3] = R.converged ? 1 : 0; }

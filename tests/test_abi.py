@@ -90,8 +90,8 @@ def test_main_sm_keeps_reference_signature():
 
 def test_main_sm_rejects_unsupported_paths():
     from smgpu import main_sm
-    with pytest.raises(NotImplementedError):
-        main_sm("x.snt", "Be8", 1, [0])
+    with pytest.raises(ValueError):
+        main_sm("x.snt", "Be8", 1, [0, 2])  # one target J only (shellmodel_main.jl:109)
     with pytest.raises(NotImplementedError):
         main_sm("x.snt", "Be8", 1, [], is_block=True)
 
@@ -120,3 +120,33 @@ def test_synthetic_snt_is_readable_by_the_oracle(tmp_path):
     H = P.dense_H()
     import numpy as np
     assert np.abs(H - H.T).max() < 1e-12
+
+
+def test_wav_round_trip_and_layout(tmp_path):
+    """smgpu_write_wav / smgpu_read_wav (host-only calls) against the byte
+    layout of writeRitzvecs (shellmodel_main.jl:1215-1229)."""
+    import struct
+    import numpy as np
+    from smgpu import SmgpuError
+    from smgpu import _lib
+    from smgpu.wav import read_wav, read_wav_full, write_wav
+    rng = np.random.default_rng(1)
+    mdim, nev = 37, 3
+    e = np.array([-31.119, -27.3, -19.162])
+    j = [0, 4, 8]
+    v = rng.standard_normal((nev, mdim))
+    p = tmp_path / "Be8_ckpot.wav"
+    write_wav(str(p), 0, e, j, v)
+    raw = p.read_bytes()
+    ref = struct.pack("<ii", nev, 0) + struct.pack("<3d", *e) + struct.pack("<3i", *j) + v.astype("<f8").tobytes()
+    assert raw == ref
+    e2, j2, v2, mt = read_wav_full(str(p), mdim)
+    assert mt == 0 and np.array_equal(e2, e) and list(j2) == j and np.array_equal(v2, v)
+    x, jj = read_wav(str(p), mdim, 2)
+    assert np.array_equal(x, v[1]) and jj == 4
+    with pytest.raises(SmgpuError) as ei:
+        read_wav(str(p), mdim + 1, 1)
+    assert ei.value.code == _lib.ERR_PARSE
+    with pytest.raises(SmgpuError) as ei:
+        read_wav(str(tmp_path / "missing.wav"), mdim, 1)
+    assert ei.value.code == _lib.ERR_IO

@@ -247,3 +247,53 @@ def test_jj_on_gpu_matches_oracle(lib, snt_dir):
         assert abs(j - O.jj(x)) < 1e-9 * max(1.0, abs(j))
         twoJ = np.sqrt(1 + 4 * j) - 1
         assert abs(twoJ - round(twoJ)) < 1e-4
+
+
+def test_main_sm_save_wav_and_in_wf(lib, tmp_path, monkeypatch):
+    """save_wav writes ./Be8_ckpot.wav (writeRitzvecs, shellmodel_main.jl:
+    248-253); in_wf restarts from its first vector (read_appwav, :196-198)."""
+    from smgpu import main_sm
+    from smgpu.wav import read_wav_full
+    monkeypatch.chdir(tmp_path)
+    en = main_sm(CKPOT, "Be8", 5, [], save_wav=True, verbose=False)
+    e, j, v, mt = read_wav_full(str(tmp_path / "Be8_ckpot.wav"), 51)
+    assert mt == 0 and np.allclose(e, en, rtol=0, atol=0)
+    assert list(j) == [0, 4, 8, 4, 2]
+    assert np.allclose(np.linalg.norm(v, axis=1), 1.0, atol=1e-10)
+    en2 = main_sm(CKPOT, "Be8", 5, [], in_wf=str(tmp_path / "Be8_ckpot.wav"), verbose=False)
+    assert np.allclose(en2, en, rtol=1e-8, atol=0)
+
+
+@pytest.mark.parametrize("snt,nuc,twoJ,nev", [(CKPOT, "Be8", 0, 2), (CKPOT, "Be8", 4, 3), (CKPOT, "Be8", 6, 1),
+                                              (USDB, "Ne20", 4, 3), (USDB, "Na21", 3, 2)])
+def test_j_projected_lanczos_vs_oracle(lib, snt, nuc, twoJ, nev):
+    """target_J = [twoJ]: the double Lanczos (lanczos_methods.jl:1-151) on
+    the GPU against the oracle's restatement; handles of both precisions
+    (the projected solve runs in FP64); the Ritz vectors have <J^2> = J(J+1)."""
+    from oracle.oracle import OracleProblem
+    J = twoJ / 2
+    O = OracleProblem(snt, nuc, mtot2=twoJ)
+    ro = O.trl(nev, lm=30, ls=15, tol=1e-8, eval_jj=J * (J + 1))
+    assert ro["converged"]
+    for prec in (0, 1):
+        G = _gpu_J(snt, nuc, prec, twoJ)
+        r = G.solve(nev, lm=30, ls=15, tol=1e-8, twoJ=twoJ, want_vecs=True)
+        assert r["converged"], prec
+        assert np.allclose(r["evals"], ro["evals"], rtol=EIG_FP64_RTOL, atol=0), (prec, r["evals"], ro["evals"])
+        jj = G.jj(r["evecs"])
+        assert np.abs(jj - J * (J + 1)).max() < 1e-5, jj
+
+
+def _gpu_J(snt, nuc, prec, twoJ):
+    from smgpu import ShellModelProblem
+    return ShellModelProblem(snt, nuc, prec, twoJ=twoJ)
+
+
+def test_main_sm_target_j(lib, golden, capsys):
+    """main_sm(..., [0]) gives the J = 0 levels of the ckpot 8Be spectrum
+    (levels 1 and 9 of test/ShellModel_test.jl:8-15)."""
+    from smgpu import main_sm
+    en = main_sm(CKPOT, "Be8", 2, [0])
+    ref = golden["ckpot_Be8"]["energies"]
+    assert (en[0] - ref[0]) ** 2 < 1e-6 and (en[1] - ref[8]) ** 2 < 1e-6
+    assert "2J= 0  En." in capsys.readouterr().out
