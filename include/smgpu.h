@@ -150,6 +150,16 @@ int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out);
 int smgpu_solve_J(smgpu_problem* h, int twoJ, int num_ev, int lm, int ls, double tol, int max_restarts,
                   const double* v1, double* evals_out, double* evecs_out, int* stats_out);
 
+/* Block thick-restart Lanczos, main_sm's is_block = true with block size q
+ * (TRBL, lanczos_methods.jl:312-423, bl_QR!, bl_ReORTH, add_bl_T!,
+ * bl_ThickRestart): blocks of q vectors, ls/q kept blocks at a restart, the
+ * block T diagonalised every iteration; FP64 for either handle precision.
+ * v1: NULL (q seeded hash draws, seeds 1234..1234+q-1, orthonormalised) or
+ * q x mdim; stats_out[1] counts single-vector H·v; stats_out[7] = q.  Other
+ * arguments and outputs as smgpu_solve. */
+int smgpu_solve_block(smgpu_problem* h, int q, int num_ev, int lm, int ls, double tol, int max_restarts,
+                      const double* v1, double* evals_out, double* evecs_out, int* stats_out);
+
 /* Seconds spent in the phases of the last create / solve / matvec call (the
  * reference's TimerOutputs sections "prep. 1b&2b-jumps", "Lanczos", "Rvecs",
  * shellmodel_main.jl:137,159,208).  times_out: 8 doubles:

@@ -705,6 +705,265 @@ struct Solve {
   }
 };
 
+// ------------------------------------------------------------------ block
+// Block thick-restart Lanczos TRBL (lanczos_methods.jl:312-423) with q
+// vectors per block, FP64: bl_operate_H! as q H·v launches, bl_ReORTH
+// (:425-436), bl_QR! (shellmodel_main.jl:1049-1066), add_bl_T! (:1201-1205),
+// bl_ThickRestart (lanczos_methods.jl:647-716) and the block Ritz vectors
+// (shellmodel_main.jl:208-224).  Vector work (H·v, dot products, updates,
+// combinations) on the device; the block T matrix is kept on the host and
+// diagonalised on the device every iteration; control flow on the host.
+struct BlockSolve {
+  smgpu_problem* P;
+  int q = 2;
+  LanczosDev L{};
+  double* V = nullptr;   // nblk*q vectors of len
+  double* U = nullptr;   // ls_sub*q vectors
+  double* w = nullptr;
+  double* js = nullptr;  // device scalars
+  double* dT = nullptr;  // small matrix for the eigensolver
+  double* dA = nullptr;
+  double* dZ = nullptr;
+  double* dev = nullptr;
+  std::vector<double> T;  // lm x lm, column-major (host)
+  int lm = 0;
+
+  double* vec(int slot) { return V + (size_t)slot * L.len; }
+  double host(const double* d) {
+    double x = 0.0;
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(&x, d, sizeof(double), cudaMemcpyDeviceToHost, P->st));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+    return x;
+  }
+  double& Tm(int i, int j) { return T[(size_t)(j - 1) * lm + (i - 1)]; }  // 1-based
+  // eigenvalues (ascending) and, if vecs, eigenvectors of T[1:n,1:n]
+  void eig(int n, std::vector<double>& vals, std::vector<double>* vecs) {
+    std::vector<double> sub((size_t)n * n);
+    for (int j = 1; j <= n; ++j)
+      for (int i = 1; i <= n; ++i) sub[(size_t)(j - 1) * n + (i - 1)] = Tm(i, j);
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(dT, sub.data(), sizeof(double) * sub.size(), cudaMemcpyHostToDevice, P->st));
+    launch_small_eig(dT, n, dA, dZ, dev, P->st);
+    vals.resize(n);
+    SMGPU_CUDA_TRY(cudaMemcpyAsync(vals.data(), dev, sizeof(double) * n, cudaMemcpyDeviceToHost, P->st));
+    if (vecs) {
+      vecs->resize((size_t)n * n);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(vecs->data(), dA, sizeof(double) * n * n, cudaMemcpyDeviceToHost, P->st));
+    }
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(P->st));
+  }
+  // js[0..m) = X_j . y for the m vectors at X
+  void dots(const double* X, int m, const double* y) {
+    launch_multidot<double>(L, X, m, y, false, P->st);
+    launch_reduce(L, m, RED_STORE, js, P->st);
+  }
+  // y -= sum_j js[j] X_j
+  void sub(const double* X, int m, double* y) { launch_axpy_dev<double>(X, L.len, m, js, y, L.len, P->st); }
+  // bl_QR! on the q vectors at slot0 (modified Gram-Schmidt); R (q x q, R[j*q+k]) on the host
+  void qr(int slot0, std::vector<double>& R) {
+    R.assign((size_t)q * q, 0.0);
+    for (int j = 0; j < q; ++j) {
+      double* qj = vec(slot0 + j);
+      launch_multidot<double>(L, qj, 1, qj, false, P->st);
+      launch_reduce(L, 1, RED_STORE, js + q, P->st);
+      launch_reduce(L, 1, RED_INVNORM, js + q + 1, P->st);
+      launch_scale_store<double>(L, qj, qj, js + q + 1, P->st);
+      R[(size_t)j * q + j] = std::sqrt(host(js + q));
+      for (int k = j + 1; k < q; ++k) {
+        dots(qj, 1, vec(slot0 + k));
+        R[(size_t)j * q + k] = host(js);
+        sub(qj, 1, vec(slot0 + k));
+      }
+    }
+  }
+
+  int run(int q_, int num_ev, int lm_, int ls, double tol, int max_restarts, const double* v1, double* evals_out,
+          double* evecs_out, int* stats_out) {
+    q = q_;
+    lm = lm_;
+    const int64_t mdim = P->T.mdim;
+    const int nev = (int)std::min<int64_t>(num_ev, mdim);
+    const int ls_sub = ls / q, itmax = lm / q - 1, nblk = lm / q;
+    const double tw0 = now_s();
+    DeviceArena& A = P->solver;
+    A.free_all();
+    L.G = 2 * P->sms;
+    L.len = P->T.len_pad;
+    L.partials = A.alloc<double>((size_t)(q + 3) * L.G);
+    V = A.alloc<double>((size_t)nblk * q * L.len);
+    U = A.alloc<double>((size_t)std::max(1, ls_sub * q) * L.len);
+    w = A.alloc<double>(L.len);
+    js = A.alloc<double>((size_t)std::max(q * q, lm) + 8);
+    dT = A.alloc<double>((size_t)lm * lm);
+    dA = A.alloc<double>((size_t)lm * lm);
+    dZ = A.alloc<double>((size_t)lm * lm);
+    dev = A.alloc<double>(lm);
+    cudaStream_t st = P->st;
+    SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(double) * (size_t)nblk * q * L.len, st));
+    T.assign((size_t)lm * lm, 0.0);
+    std::vector<std::vector<double>> en(3, std::vector<double>(num_ev, 1.0e4));
+    cudaEvent_t e0, e1, e2;
+    SMGPU_CUDA_TRY(cudaEventCreate(&e0));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e1));
+    SMGPU_CUDA_TRY(cudaEventCreate(&e2));
+    double* v1dev = nullptr;
+    if (v1) {
+      v1dev = A.alloc<double>((size_t)q * mdim);
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(v1dev, v1, sizeof(double) * q * mdim, cudaMemcpyHostToDevice, st));
+    }
+    SMGPU_CUDA_TRY(cudaEventRecord(e0, st));
+    // start block: initialize_bl_wav (shellmodel_main.jl:950-965) + bl_QR!
+    for (int i = 0; i < q; ++i) {
+      if (v1dev) launch_to_padded<double>(P->dt, v1dev + (size_t)i * mdim, vec(i), st);
+      else launch_start_vector(P->dt, 1234ull + (uint64_t)i, vec(i), st);
+      for (int k = i - 1; k >= 0; --k) {
+        dots(vec(k), 1, vec(i));
+        sub(vec(k), 1, vec(i));
+      }
+      launch_multidot<double>(L, vec(i), 1, vec(i), false, st);
+      launch_reduce(L, 1, RED_INVNORM, js + q + 1, st);
+      launch_scale_store<double>(L, vec(i), vec(i), js + q + 1, st);
+    }
+    std::vector<double> Beta;
+    qr(0, Beta);
+    bool TF = false;
+    int elit = 1, inow = 1, itmin = 1, n_restart = 0, n_hv = 0, status = SMGPU_OK;
+    std::vector<double> vals, vecs, Rm((size_t)q * q);
+    while (!TF) {
+      for (int it = itmin; it <= itmax; ++it) {
+        inow = it;
+        const int v0 = (it - 1) * q, h0 = it * q;
+        for (int i = 0; i < q; ++i) P->hv((const double*)vec(v0 + i), vec(h0 + i), HvEpilogue<double>{}, st);
+        n_hv += q;
+        for (int i = 0; i < q; ++i) {  // js[i*q + j] = V_i . HV_j
+          launch_multidot<double>(L, vec(h0), q, vec(v0 + i), false, st);
+          launch_reduce(L, q, RED_STORE, js + (size_t)i * q, st);
+        }
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(Rm.data(), js, sizeof(double) * q * q, cudaMemcpyDeviceToHost, st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        bool sym = true;  // Rm[i*q+j] = V_i . HV_j
+        for (int i = 0; i < q; ++i)
+          for (int j = 0; j < q; ++j)
+            if (Rm[(size_t)i * q + j] != Rm[(size_t)j * q + i]) sym = false;
+        if (!sym)
+          for (int i = 0; i < q; ++i)
+            for (int j = i; j < q; ++j) Rm[(size_t)i * q + j] = Rm[(size_t)j * q + i];
+        for (int i = 0; i < q; ++i)
+          for (int j = 0; j < q; ++j) Tm(q * it - q + 1 + i, q * it - q + 1 + j) = Rm[(size_t)i * q + j];
+        // diagonalize_T!(it*q) (lanczos_methods.jl:250-258)
+        const int kk = it * q;
+        eig(kk, vals, nullptr);
+        for (int h = 2; h >= 1; --h) en[h] = en[h - 1];
+        for (int i = 0; i < std::min(num_ev, kk); ++i) en[0][i] = vals[i];
+        bool ok = true;
+        for (int i = 0; i < num_ev; ++i)
+          if (!(en[1][i] - en[0][i] < tol)) ok = false;
+        if (ok) TF = true;
+        // HV -= R V, bl_ReORTH, bl_QR!, add_bl_T!
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(js, Rm.data(), sizeof(double) * q * q, cudaMemcpyHostToDevice, st));
+        for (int i = 0; i < q; ++i)
+          launch_axpy_dev<double>(vec(v0), L.len, q, js + (size_t)i * q, vec(h0 + i), L.len, st);
+        for (int l = it - 1; l >= 1; --l)
+          for (int i = 0; i < q; ++i) {
+            dots(vec((l - 1) * q), q, vec(h0 + i));
+            sub(vec((l - 1) * q), q, vec(h0 + i));
+          }
+        qr(h0, Beta);
+        for (int i = 0; i < q; ++i)
+          for (int j = 0; j < q; ++j) {
+            Tm(q * it + 1 + i, q * it - q + 1 + j) = Beta[(size_t)i * q + j];
+            Tm(q * it - q + 1 + j, q * it + 1 + i) = Beta[(size_t)i * q + j];
+          }
+        if (TF) {
+          elit = it;
+          break;
+        }
+      }
+      if (TF) break;
+      ++n_restart;
+      if (n_restart > max_restarts) {
+        status = SMGPU_ERR_NOCONV;
+        break;
+      }
+      // bl_ThickRestart (lanczos_methods.jl:647-716)
+      const int lmq = q * inow, lsq = q * ls_sub;
+      eig(lmq, vals, &vecs);
+      auto VV = [&](int row, int col) { return vecs[(size_t)(col - 1) * lmq + (row - 1)]; };
+      std::fill(T.begin(), T.end(), 0.0);
+      for (int k = 1; k <= lsq; ++k) Tm(k, k) = vals[k - 1];
+      for (int a = 1; a <= q; ++a)
+        for (int k = 1; k <= lsq; ++k) {
+          double r = 0.0;
+          for (int b = 1; b <= q; ++b) r += Beta[(size_t)(a - 1) * q + (b - 1)] * VV(lmq - q + b, k);
+          Tm(lsq + a, k) = r;
+          Tm(k, lsq + a) = r;
+        }
+      for (int k = 1; k <= lsq; ++k) {
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(js, vecs.data() + (size_t)(k - 1) * lmq, sizeof(double) * lmq,
+                                       cudaMemcpyHostToDevice, st));
+        launch_combine(V, L.len, lmq, js, U + (size_t)(k - 1) * L.len, L.len, st);
+      }
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(V, U, sizeof(double) * (size_t)lsq * L.len, cudaMemcpyDeviceToDevice, st));
+      SMGPU_CUDA_TRY(cudaMemcpyAsync(vec(ls_sub * q), vec(inow * q), sizeof(double) * (size_t)q * L.len,
+                                     cudaMemcpyDeviceToDevice, st));
+      if (nblk > ls_sub + 1)
+        SMGPU_CUDA_TRY(cudaMemsetAsync(vec((ls_sub + 1) * q), 0,
+                                       sizeof(double) * (size_t)(nblk - ls_sub - 1) * q * L.len, st));
+      for (int i = 2; i <= ls_sub + 1; ++i) {
+        for (int j = i - 1; j >= 1; --j)
+          for (int a = 0; a < q; ++a) {
+            dots(vec((j - 1) * q), q, vec((i - 1) * q + a));
+            sub(vec((j - 1) * q), q, vec((i - 1) * q + a));
+          }
+        qr((i - 1) * q, Beta);
+      }
+      itmin = ls_sub + 1;
+    }
+    for (int i = 0; i < nev; ++i) evals_out[i] = en[0][i];
+    SMGPU_CUDA_TRY(cudaEventRecord(e1, st));
+    if (evecs_out && TF) {
+      const int m = elit * q;
+      eig(m, vals, &vecs);
+      double* R = A.alloc<double>(L.len);
+      double* tmp = A.alloc<double>(mdim);
+      for (int e = 0; e < nev; ++e) {
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(js, vecs.data() + (size_t)e * m, sizeof(double) * m, cudaMemcpyHostToDevice,
+                                       st));
+        launch_combine(V, L.len, m, js, R, L.len, st);
+        launch_multidot<double>(L, R, 1, R, false, st);
+        launch_reduce(L, 1, RED_INVNORM, js + q + 1, st);
+        launch_scale_store<double>(L, R, R, js + q + 1, st);
+        launch_from_padded(P->dt, R, tmp, st);
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(evecs_out + (size_t)e * mdim, tmp, sizeof(double) * mdim,
+                                       cudaMemcpyDeviceToHost, st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
+      }
+    }
+    SMGPU_CUDA_TRY(cudaEventRecord(e2, st));
+    SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
+    SMGPU_CUDA_TRY(cudaGetLastError());
+    float ms1 = 0.f, ms2 = 0.f;
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms1, e0, e1));
+    SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms2, e1, e2));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (stats_out) {
+      stats_out[0] = elit;
+      stats_out[1] = n_hv;
+      stats_out[2] = n_restart;
+      stats_out[3] = TF ? 1 : 0;
+      stats_out[4] = nev;
+      stats_out[5] = 0;
+      stats_out[6] = 0;
+      stats_out[7] = q;
+    }
+    P->times[1] = ms1 * 1e-3;
+    P->times[4] = ms2 * 1e-3;
+    P->times[5] = now_s() - tw0;
+    return status;
+  }
+};
+
 }  // namespace
 
 // =========================================================================
@@ -950,6 +1209,19 @@ int smgpu_solve_J(smgpu_problem* h, int twoJ, int num_ev, int lm, int ls, double
     s.Jop = ensure_jj_op(h);
     s.eval_jj = eval_jj;
     return s.run_projected(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
+  });
+}
+
+int smgpu_solve_block(smgpu_problem* h, int q, int num_ev, int lm, int ls, double tol, int max_restarts,
+                      const double* v1, double* evals_out, double* evecs_out, int* stats_out) {
+  if (!h || !evals_out) return fail(h, SMGPU_ERR_ARG, "null argument");
+  if (q < 1 || q > 8 || num_ev < 1 || lm < 2 * q || ls < q || ls / q + 1 > lm / q - 1 || lm > 1000 ||
+      !(tol > 0.0))
+    return fail(h, SMGPU_ERR_ARG, "need 1 <= q <= 8, ls >= q, ls/q + 2 <= lm/q, lm <= 1000, tol > 0");
+  return guarded(h, [&]() {
+    h->ensure_fp64();
+    BlockSolve s{h};
+    return s.run(q, num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
   });
 }
 

@@ -39,6 +39,8 @@ SIGNATURES = {
     "smgpu_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
     "smgpu_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_jj": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "smgpu_solve_block": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
+                                    _vp]),
     "smgpu_solve_J": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),

@@ -111,15 +111,20 @@ class ShellModelProblem:
         check(load().smgpu_matvec(self._h, _p(v), _p(w), ncols, 1 if accumulate else 0), self._h)
         return w
 
-    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False, twoJ=None):
+    def solve(self, num_ev, lm=300, ls=20, tol=1e-8, max_restarts=10000, v1=None, want_vecs=False, twoJ=None,
+              block=None):
         """Lowest num_ev eigenvalues; twoJ: J-projected (double) Lanczos for
-        total angular momentum twoJ/2 (the handle must have Mtot = twoJ)."""
+        total angular momentum twoJ/2 (the handle must have Mtot = twoJ);
+        block = q: block Lanczos with q vectors per block (TRBL)."""
         nev = min(num_ev, self.mdim)
         ev = np.zeros(nev)
         vecs = np.zeros((nev, self.mdim)) if want_vecs else None
         stats = np.zeros(8, dtype=np.int32)
         v1a = None if v1 is None else np.ascontiguousarray(v1, dtype=np.float64)
-        if twoJ is None:
+        if block is not None:
+            rc = load().smgpu_solve_block(self._h, int(block), int(num_ev), int(lm), int(ls), float(tol),
+                                          int(max_restarts), _p(v1a), _p(ev), _p(vecs), _p(stats))
+        elif twoJ is None:
             rc = load().smgpu_solve(self._h, int(num_ev), int(lm), int(ls), float(tol), int(max_restarts), _p(v1a),
                                     _p(ev), _p(vecs), _p(stats))
         else:
@@ -323,7 +328,8 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
         if len(target_J) > 1:
             raise ValueError("Invalid `target_J` Multiple J is not supported now.")
         tJ = int(target_J[0])
-    unsupported = dict(is_block=is_block, calc_moment=calc_moment, calc_entropy=calc_entropy,
+    unsupported = dict(block_with_target_J=is_block and tJ is not None, calc_moment=calc_moment,
+                       calc_entropy=calc_entropy,
                        visualize_occ=visualize_occ, print_evec=print_evec, truncation=bool(truncation_scheme),
                        debugmode=bool(debugmode))
     bad = [k for k, v in unsupported.items() if v]
@@ -340,11 +346,17 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
         return None
     v1 = None
     if in_wf:
-        # read_appwav with q = 1: the first vector of the file starts the Lanczos
+        # read_appwav: the first vector (q of them for a block) starts the Lanczos
         from .wav import read_wav
-        v1, _ = read_wav(in_wf, P.mdim, 1)
+        vs, _ = read_wav(in_wf, P.mdim, all=True)
+        if is_block:
+            if len(vs) < q:
+                raise ValueError("#(appwav) must be >= q")
+            v1 = np.array(vs[:q])
+        else:
+            v1 = vs[0]
     r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, v1=v1, want_vecs=verbose or save_wav,
-                twoJ=tJ)
+                twoJ=tJ, block=int(q) if is_block else None)
     en = list(map(float, r["evals"]))
     totJs = None
     if r["status"] == _lib.OK and r["evecs"] is not None:

@@ -54,6 +54,8 @@ def lib():
         L.orc_trl.restype = C.c_int
         L.orc_trl.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
                               C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+        L.orc_trbl.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p,
+                               C.c_ulonglong, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_create_M.restype = vp
         L.orc_create_M.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
         L.orc_sym_eig.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -189,6 +191,23 @@ class OracleProblem:
         """<v|J^2|v>/<v|v> by the ladder operator (J^2 = J-J+ + M(M+1))."""
         v = np.ascontiguousarray(v, dtype=np.float64)
         return float(lib().orc_jj(self._h, _p(v)))
+
+    def trbl(self, q, num_ev, lm=300, ls=20, tol=1e-8, max_restart=10000, v1=None, seed=1234, want_vecs=False):
+        """Block thick-restart Lanczos (TRBL) with q vectors per block."""
+        L = lib()
+        k = min(num_ev, self.mdim)
+        ev = np.zeros(k)
+        vecs = np.zeros((k, self.mdim)) if want_vecs else None
+        stats = np.zeros(4, dtype=np.int32)
+        v1p = None
+        if v1 is not None:
+            v1 = np.ascontiguousarray(v1, dtype=np.float64)
+            v1p = _p(v1)
+        if L.orc_trbl(self._h, q, num_ev, lm, ls, tol, max_restart, v1p, seed, _p(ev),
+                      _p(vecs) if want_vecs else None, _p(stats)) != 0:
+            raise RuntimeError("oracle TRBL: " + L.orc_last_error().decode())
+        return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_hv=int(stats[1]), n_restart=int(stats[2]),
+                    converged=bool(stats[3]))
 
     def nnz(self) -> int:
         """Structural non-zeros of H (distinct (row, col) pairs, diagonal included)."""

@@ -1264,6 +1264,187 @@ sample_end:
   return R;
 }
 
+// ---------------------------------------------------------------------------
+// Block Lanczos: TRBL (lanczos_methods.jl:312-423), bl_ReORTH (:425-436),
+// bl_QR! (shellmodel_main.jl:1049-1066), add_bl_T! (:1201-1205),
+// bl_ThickRestart (lanczos_methods.jl:647-716) and the block Ritz vectors
+// (shellmodel_main.jl:208-224).  A block is q rows of mdim; the start block is
+// q hash draws (seeds seed..seed+q-1), orthonormalised as initialize_bl_wav
+// (:950-965) does and then QR-factorised.
+typedef std::vector<std::vector<double>> Block;  // q rows
+
+// bl_QR!: modified Gram-Schmidt over the rows; R upper triangular (q x q, R[j*q+k] = R(j,k))
+void bl_QR(Block& Q, std::vector<double>& R, i64 mdim) {
+  const int q = (int)Q.size();
+  std::fill(R.begin(), R.end(), 0.0);
+  for (int j = 0; j < q; ++j) {
+    const double t = std::sqrt(dotp(mdim, Q[j].data(), Q[j].data()));
+    R[(size_t)j * q + j] = t;
+    scal(mdim, 1.0 / t, Q[j].data());
+    for (int k = j + 1; k < q; ++k) {
+      double r = 0.0;
+      for (i64 i = 0; i < mdim; ++i) r += Q[j][i] * Q[k][i];
+      R[(size_t)j * q + k] = r;
+      axpy(mdim, -r, Q[j].data(), Q[k].data());
+    }
+  }
+}
+
+// HV -= (HV Vt^T) Vt for the blocks vks[it-2] .. vks[0]
+void bl_ReORTH(int it, Block& HV, std::vector<Block>& vks, i64 mdim) {
+  const int q = (int)HV.size();
+  for (int l = it - 1; l >= 1; --l) {
+    const Block& Vt = vks[l - 1];
+    std::vector<double> R((size_t)q * q);
+    for (int i = 0; i < q; ++i)
+      for (int j = 0; j < q; ++j) R[(size_t)i * q + j] = dotp(mdim, HV[i].data(), Vt[j].data());
+    for (int i = 0; i < q; ++i)
+      for (int j = 0; j < q; ++j) axpy(mdim, -R[(size_t)i * q + j], Vt[j].data(), HV[i].data());
+  }
+}
+
+TrlResult TRBL(const Problem& P, int q, int num_ev, int lm, int ls, double tol, int max_restart, const double* v1,
+               u64 seed, bool want_vecs, int num_history) {
+  const i64 mdim = P.mdim;
+  num_ev = (int)std::min<i64>(num_ev, mdim);
+  TrlResult R;
+  const int ls_sub = ls / q, itmax = lm / q - 1;
+  const int nblk = lm / q;
+  std::vector<Block> vks(nblk, Block(q, std::vector<double>(mdim, 0.0)));
+  std::vector<Block> uks(ls_sub, Block(q, std::vector<double>(mdim, 0.0)));
+  std::vector<double> T((size_t)lm * lm, 0.0);
+  auto Tm = [&](int i, int j) -> double& { return T[(size_t)(j - 1) * lm + (i - 1)]; };
+  std::vector<std::vector<double>> en(num_history, std::vector<double>(num_ev, 1.0e4));
+  std::vector<double> Beta((size_t)q * q, 0.0);
+  // start block (initialize_bl_wav + bl_QR!)
+  for (int i = 0; i < q; ++i) {
+    double* v = vks[0][i].data();
+    if (v1) std::memcpy(v, v1 + (size_t)i * mdim, sizeof(double) * mdim);
+    else
+      for (i64 x = 0; x < mdim; ++x) v[x] = start_elem(seed + (u64)i, x);
+    for (int k = i - 1; k >= 0; --k) axpy(mdim, -dotp(mdim, v, vks[0][k].data()), vks[0][k].data(), v);
+    scal(mdim, 1.0 / std::sqrt(dotp(mdim, v, v)), v);
+  }
+  bl_QR(vks[0], Beta, mdim);
+  bool TF = false;
+  int elit = 1, inow = 1, itmin = 1;
+  std::vector<double> wbuf;
+  while (!TF) {
+    for (int it = itmin; it <= itmax; ++it) {
+      inow = it;
+      Block& V = vks[it - 1];
+      Block& HV = vks[it];
+      for (int i = 0; i < q; ++i) {
+        std::fill(HV[i].begin(), HV[i].end(), 0.0);
+        operate_H(P, V[i].data(), HV[i].data());
+      }
+      R.n_hv += q;
+      std::vector<double> Rm((size_t)q * q);  // Rm[i*q+j] = V_i . HV_j
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j) Rm[(size_t)i * q + j] = dotp(mdim, V[i].data(), HV[j].data());
+      bool sym = true;
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j)
+          if (Rm[(size_t)i * q + j] != Rm[(size_t)j * q + i]) sym = false;
+      if (!sym)
+        for (int i = 0; i < q; ++i)
+          for (int j = i; j < q; ++j) Rm[(size_t)i * q + j] = Rm[(size_t)j * q + i];
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j) Tm(q * it - q + 1 + i, q * it - q + 1 + j) = Rm[(size_t)i * q + j];
+      // diagonalize_T!(it*q)
+      const int kk = it * q;
+      for (int ith = num_history - 1; ith >= 1; --ith) en[ith] = en[ith - 1];
+      std::vector<double> sub((size_t)kk * kk);
+      for (int j = 1; j <= kk; ++j)
+        for (int i = 1; i <= kk; ++i) sub[(size_t)(j - 1) * kk + (i - 1)] = Tm(i, j);
+      wbuf.assign(kk, 0.0);
+      sym_eig(kk, sub.data(), wbuf.data(), nullptr);
+      for (int i = 0; i < std::min(num_ev, kk); ++i) en[0][i] = wbuf[i];
+      bool all_ok = true;
+      for (int i = 0; i < num_ev; ++i)
+        if (!(en[1][i] - en[0][i] < tol)) all_ok = false;
+      if (all_ok) TF = true;
+      // HV -= R V
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j) axpy(mdim, -Rm[(size_t)i * q + j], V[j].data(), HV[i].data());
+      bl_ReORTH(it, HV, vks, mdim);
+      bl_QR(HV, Beta, mdim);
+      // add_bl_T!: T[block it+1, block it] = Beta, T[block it, block it+1] = Beta^T
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j) {
+          Tm(q * it + 1 + i, q * it - q + 1 + j) = Beta[(size_t)i * q + j];
+          Tm(q * it - q + 1 + j, q * it + 1 + i) = Beta[(size_t)i * q + j];
+        }
+      if (TF) { elit = it; break; }
+    }
+    if (!TF) {
+      if (R.n_restart >= max_restart) break;
+      R.n_restart++;
+      // bl_ThickRestart
+      const int lmq = q * inow, lsq = q * ls_sub;
+      std::vector<double> sub((size_t)lmq * lmq), vals(lmq), vecs((size_t)lmq * lmq);
+      for (int j = 1; j <= lmq; ++j)
+        for (int i = 1; i <= lmq; ++i) sub[(size_t)(j - 1) * lmq + (i - 1)] = Tm(i, j);
+      sym_eig(lmq, sub.data(), vals.data(), vecs.data());
+      auto VV = [&](int row, int col) { return vecs[(size_t)(col - 1) * lmq + (row - 1)]; };
+      std::fill(T.begin(), T.end(), 0.0);
+      for (int k = 1; k <= lsq; ++k) Tm(k, k) = vals[k - 1];
+      for (int a = 1; a <= q; ++a)
+        for (int k = 1; k <= lsq; ++k) {
+          double r = 0.0;
+          for (int b = 1; b <= q; ++b) r += Beta[(size_t)(a - 1) * q + (b - 1)] * VV(lmq - q + b, k);
+          Tm(lsq + a, k) = r;
+          Tm(k, lsq + a) = r;
+        }
+      for (int bi = 1; bi <= ls_sub; ++bi)
+        for (int b = 1; b <= q; ++b) {
+          std::vector<double>& u = uks[bi - 1][b - 1];
+          std::fill(u.begin(), u.end(), 0.0);
+          const int k = q * (bi - 1) + b;
+          for (int j = 1; j <= inow; ++j)
+            for (int bj = 1; bj <= q; ++bj) axpy(mdim, VV(q * (j - 1) + bj, k), vks[j - 1][bj - 1].data(), u.data());
+        }
+      for (int i = 0; i < ls_sub; ++i) vks[i] = uks[i];
+      vks[ls_sub] = vks[inow];
+      for (int i = ls_sub + 1; i < nblk; ++i)
+        for (auto& r : vks[i]) std::fill(r.begin(), r.end(), 0.0);
+      for (int i = 2; i <= ls_sub + 1; ++i) {
+        Block& V = vks[i - 1];
+        for (int j = i - 1; j >= 1; --j) {
+          const Block& Vt = vks[j - 1];
+          std::vector<double> Rm((size_t)q * q);
+          for (int a = 0; a < q; ++a)
+            for (int b = 0; b < q; ++b) Rm[(size_t)a * q + b] = dotp(mdim, V[a].data(), Vt[b].data());
+          for (int a = 0; a < q; ++a)
+            for (int b = 0; b < q; ++b) axpy(mdim, -Rm[(size_t)a * q + b], Vt[b].data(), V[a].data());
+        }
+        bl_QR(V, Beta, mdim);
+      }
+      itmin = ls_sub + 1;
+    }
+  }
+  R.converged = TF;
+  R.elit = elit;
+  R.en = en[0];
+  if (want_vecs) {
+    const int m = elit * q;
+    std::vector<double> sub((size_t)m * m), vals(m), vecs((size_t)m * m);
+    for (int j = 1; j <= m; ++j)
+      for (int i = 1; i <= m; ++i) sub[(size_t)(j - 1) * m + (i - 1)] = Tm(i, j);
+    sym_eig(m, sub.data(), vals.data(), vecs.data());
+    R.ritz.assign((size_t)num_ev * mdim, 0.0);
+    for (int nth = 0; nth < num_ev; ++nth) {
+      double* Rv = R.ritz.data() + (size_t)nth * mdim;
+      for (int k = 1; k <= m; ++k) {
+        const int it = (k - 1) / q, b = k - q * it;
+        axpy(mdim, vecs[(size_t)nth * m + (k - 1)], vks[it][b - 1].data(), Rv);
+      }
+      scal(mdim, 1.0 / std::sqrt(dotp(mdim, Rv, Rv)), Rv);
+    }
+  }
+  return R;
+}
+
 // shellmodel_main.jl:89-147 main_sm set-up (target_J = [], no truncation).
 Problem* build_problem(const std::string& sntf, const std::string& nuc, int nthreads_for_tasks, int mtot_override = -1) {
   Problem* P = new Problem();
@@ -1510,6 +1691,21 @@ long long orc_nnz(void* h) { return count_nnz(*(Problem*)h); }
 
 void orc_start_vector(long long mdim, unsigned long long seed, double* v) {
   for (i64 i = 0; i < mdim; ++i) v[i] = start_elem(seed, i);
+}
+
+// Block thick-restart Lanczos (TRBL, q vectors per block); v1: NULL or q x mdim.
+int orc_trbl(void* h, int q, int num_ev, int lm, int ls, double tol, int max_restart, const double* v1,
+             unsigned long long seed, double* evals, double* evecs, int* stats) {
+  try {
+    TrlResult R = TRBL(*(Problem*)h, q, num_ev, lm, ls, tol, max_restart, v1, seed, evecs != nullptr, 3);
+    for (size_t i = 0; i < R.en.size(); ++i) evals[i] = R.en[i];
+    if (evecs) std::memcpy(evecs, R.ritz.data(), sizeof(double) * R.ritz.size());
+    if (stats) { stats[0] = R.elit; stats[1] = R.n_hv; stats[2] = R.n_restart; stats[3] = R.converged ? 1 : 0; }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
 }
 
 // Full thick-restart Lanczos.  stats: [elit, n_hv, n_restart, converged]; times: [t_hv, t_reorth, t_total].

@@ -93,7 +93,7 @@ def test_main_sm_rejects_unsupported_paths():
     with pytest.raises(ValueError):
         main_sm("x.snt", "Be8", 1, [0, 2])  # one target J only (shellmodel_main.jl:109)
     with pytest.raises(NotImplementedError):
-        main_sm("x.snt", "Be8", 1, [], is_block=True)
+        main_sm("x.snt", "Be8", 1, [], calc_moment=True)
 
 
 def test_synthetic_recipe_counts():

@@ -297,3 +297,30 @@ def test_main_sm_target_j(lib, golden, capsys):
     ref = golden["ckpot_Be8"]["energies"]
     assert (en[0] - ref[0]) ** 2 < 1e-6 and (en[1] - ref[8]) ** 2 < 1e-6
     assert "2J= 0  En." in capsys.readouterr().out
+
+
+def test_block_lanczos_ckpot_known_answer(lib, golden):
+    """test/ShellModel_test.jl:8-15 runs main_sm(..., "Be8", 10, []; q=2,
+    is_block=true): the block Lanczos must reproduce the 10 levels."""
+    from smgpu import main_sm
+    en = main_sm(CKPOT, "Be8", 10, [], q=2, is_block=True, verbose=False)
+    for e, ref in zip(en, golden["ckpot_Be8"]["energies"]):
+        assert (e - ref) ** 2 < golden["ckpot_Be8"]["tolerance_sq"]
+
+
+@pytest.mark.parametrize("q", [2, 3])
+def test_block_lanczos_vs_oracle(lib, snt_dir, q):
+    """TRBL on the GPU against the oracle's restatement (sd 4p4n, lm=30,
+    ls=15), FP64, with Ritz vectors."""
+    snt, nuc = snt_dir["sd4p4n"]
+    O = _oracle(snt, nuc)
+    ro = O.trbl(q, 5, lm=30, ls=15, tol=1e-8)
+    assert ro["converged"]
+    G = _gpu(snt, nuc, 0)
+    r = G.solve(5, lm=30, ls=15, tol=1e-8, block=q, want_vecs=True)
+    assert r["converged"] and r["n_matvec"] > 0
+    assert np.allclose(r["evals"], ro["evals"], rtol=EIG_FP64_RTOL, atol=0), (r["evals"], ro["evals"])
+    for k in range(2):
+        x = r["evecs"][k]
+        assert abs(np.linalg.norm(x) - 1) < 1e-10
+        assert np.linalg.norm(O.operate_H(x) - r["evals"][k] * x) < 1e-3
