@@ -3,12 +3,14 @@
 
 Julia binding of libsmgpu.so for NuclearToolkit.jl's ShellModel path.
 
-`SMGPU.main_sm(sntf, target_nuc, num_ev, target_J; lm=300, ls=20, tol=1e-8,
-precision=:fp64)` has the arguments and the return value of
-`NuclearToolkit.main_sm` (src/ShellModel/shellmodel_main.jl:89-281) for
-`target_J = []`: it returns the lowest `num_ev` eigenvalues.  Parsing,
-basis, jump tables, H·v and the thick-restart Lanczos run inside the library
-(GPU); Julia only passes the file name and receives the energies.
+`SMGPU.main_sm(sntf, target_nuc, num_ev, target_J; q=1, is_block=false,
+lm=300, ls=20, tol=1e-8, precision=:fp64)` has the arguments and the return
+value of `NuclearToolkit.main_sm` (src/ShellModel/shellmodel_main.jl:89-281):
+it returns the lowest `num_ev` eigenvalues and prints the J labels as the
+reference does; `target_J = [2J]` runs the J-projected double Lanczos and
+`is_block = true` the block Lanczos with block size `q`.  Parsing, basis,
+jump tables, H·v and the Lanczos iterations run inside the library (GPU);
+Julia passes the file name and receives the energies.
 
 Set `ENV["SMGPU_LIB"]` to the path of libsmgpu.so before loading the module.
 """
@@ -27,11 +29,17 @@ function check(rc::Cint, h::Ptr{Cvoid})
     error("libsmgpu error $(rc): $(last_error(h))")
 end
 
-"""Create a problem handle (readsmsnt + basis + jump tables on the GPU)."""
-function create(sntf::AbstractString, target_nuc::AbstractString; precision::Symbol=:fp64)
+"""Create a problem handle (readsmsnt + basis + jump tables on the GPU);
+`twoJ >= 0` builds the basis of Mtot = twoJ (main_sm's target_J = [twoJ])."""
+function create(sntf::AbstractString, target_nuc::AbstractString; precision::Symbol=:fp64, twoJ::Int=-1)
     ref = Ref{Ptr{Cvoid}}(C_NULL)
-    rc = ccall((:smgpu_problem_create_from_snt, libsmgpu), Cint,
-               (Cstring, Cstring, Cint, Ref{Ptr{Cvoid}}), sntf, target_nuc, PRECISION[precision], ref)
+    if twoJ < 0
+        rc = ccall((:smgpu_problem_create_from_snt, libsmgpu), Cint,
+                   (Cstring, Cstring, Cint, Ref{Ptr{Cvoid}}), sntf, target_nuc, PRECISION[precision], ref)
+    else
+        rc = ccall((:smgpu_problem_create_from_snt_J, libsmgpu), Cint,
+                   (Cstring, Cstring, Cint, Cint, Ref{Ptr{Cvoid}}), sntf, target_nuc, twoJ, PRECISION[precision], ref)
+    end
     check(rc, C_NULL)
     return ref[]
 end
@@ -52,20 +60,60 @@ function operate_H!(h::Ptr{Cvoid}, wf::Vector{Float64}, twf::Vector{Float64})
     return nothing
 end
 
-function main_sm(sntf, target_nuc, num_ev, target_J; lm=300, ls=20, tol=1.e-8, max_restarts=10000,
-                 precision::Symbol=:fp64, is_show=false)
-    length(target_J) == 0 || error("SMGPU: target_J must be [] (J projection is not in the GPU library)")
-    h = create(sntf, target_nuc; precision=precision)
+"""<v|J^2|v> for the columns of a Vector of vectors (operate_J! + dot)."""
+function jj(h::Ptr{Cvoid}, vecs::Vector{Vector{Float64}})
+    m = mdim(h)
+    flat = Vector{Float64}(undef, m * length(vecs))
+    for (k, v) in enumerate(vecs); flat[(k-1)*m+1:k*m] .= v; end
+    out = zeros(Float64, length(vecs))
+    check(ccall((:smgpu_jj, libsmgpu), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}),
+                h, flat, length(vecs), out), h)
+    return out
+end
+
+# shellmodel_main.jl:1105-1113
+function J_from_JJ1(JJ, tol=1.e-6)
+    for J = 0:100
+        hJ = 0.5 * J
+        abs(hJ * (hJ + 1.0) - JJ) < tol && return hJ
+    end
+    return -1.0
+end
+
+function main_sm(sntf, target_nuc, num_ev, target_J; q=1, is_block=false, lm=300, ls=20, tol=1.e-8,
+                 max_restarts=10000, precision::Symbol=:fp64, is_show=false)
+    length(target_J) <= 1 || error("Invalid `target_J` Multiple J is not supported now.")
+    tJ = length(target_J) == 1 ? Int(target_J[1]) : -1
+    (is_block && tJ >= 0) && error("SMGPU: block Lanczos with target_J is not in the GPU library")
+    h = create(sntf, target_nuc; precision=precision, twoJ=tJ)
     try
-        n = min(num_ev, mdim(h))
+        m = mdim(h)
+        n = min(num_ev, m)
         en = zeros(Float64, n)
+        vecs = zeros(Float64, n * m)
         stats = zeros(Cint, 8)
-        rc = ccall((:smgpu_solve, libsmgpu), Cint,
-                   (Ptr{Cvoid}, Cint, Cint, Cint, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Cint}),
-                   h, num_ev, lm, ls, tol, max_restarts, C_NULL, en, C_NULL, stats)
+        argt = (Ptr{Cvoid}, Cint, Cint, Cint, Cint, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Cint})
+        if is_block
+            rc = ccall((:smgpu_solve_block, libsmgpu), Cint, argt,
+                       h, q, num_ev, lm, ls, tol, max_restarts, C_NULL, en, vecs, stats)
+        elseif tJ >= 0
+            rc = ccall((:smgpu_solve_J, libsmgpu), Cint, argt,
+                       h, tJ, num_ev, lm, ls, tol, max_restarts, C_NULL, en, vecs, stats)
+        else
+            rc = ccall((:smgpu_solve, libsmgpu), Cint,
+                       (Ptr{Cvoid}, Cint, Cint, Cint, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Cint}),
+                       h, num_ev, lm, ls, tol, max_restarts, C_NULL, en, vecs, stats)
+        end
         rc == SMGPU_ERR_NOCONV && @warn "Lanczos not converged after $(max_restarts) restarts"
         rc == SMGPU_ERR_NOCONV || check(rc, h)
-        print("En. "); foreach(x -> print(lpad(string(round(x, digits=4)), 10), " "), en); print("\n")
+        totJs = J_from_JJ1.(jj(h, [vecs[(k-1)*m+1:k*m] for k = 1:n]))
+        if tJ < 0
+            println("J $totJs")
+            print("En. "); foreach(x -> print(lpad(string(round(x, digits=4)), 10), " "), en); print("\n")
+        else
+            print("2J= $(Int(2*totJs[1]))  En."); foreach(x -> print(lpad(string(round(x, digits=5)), 12), " "), en)
+            print("\n")
+        end
         is_show && println("matvecs $(stats[2]) restarts $(stats[3])")
         return en
     finally
