@@ -137,6 +137,46 @@ int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int ma
  * J(J+1) - j_a(j_a+1) - j_b(j_b+1) per pair). */
 int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out);
 
+/* One-body electromagnetic operators of transit.jl. */
+enum { SMGPU_OBTR_M1 = 0, SMGPU_OBTR_E2 = 1 };
+
+/* out[a*nr + b] = <vl_a| O |vr_b> for the M1 (op = SMGPU_OBTR_M1) or E2
+ * (SMGPU_OBTR_E2) one-body operator, vl_a nl host vectors of hl's basis and
+ * vr_b nr host vectors of hr's basis (reference order).  symmetric != 0 is
+ * the expectation-value form of eval_moment (prep_obtr_diag / op_obtr_diag,
+ * src/ShellModel/transit.jl:82-284,702-765: orbit pairs f >= i applied with
+ * their transpose; hl and hr share one basis); symmetric == 0 is
+ * transit_main's (prep_obtr_nondiag / op_obtr_nondiag / calc_bifs,
+ * :286-531,561-700) with ΔM = (Mtot_l - Mtot_r)/2 (doubled Mtot of the
+ * handles; the reference takes Mtot_l >= Mtot_r).  gfactors = [g_l(p),
+ * g_l(n), g_s(p), g_s(n)] (NULL: 1.0, 0.0, 5.586, -3.826), effcharge =
+ * [e_p, e_n] (NULL: 1.5, 0.5); the oscillator length follows
+ * init_ho_by_mass (hwprm 2 for 16 <= A <= 40).  O·v and the overlaps run on
+ * the GPU in FP64; nl * nr <= 65535.  Both handles must describe one nucleus
+ * on one model space (SMGPU_ERR_ARG). */
+int smgpu_obtr(smgpu_problem* hl, smgpu_problem* hr, int op, int symmetric, const double* gfactors,
+               const double* effcharge, const double* vl, int nl, const double* vr, int nr, double* out);
+
+/* Transition densities of eigenvector continuation (prepEC mode "TD",
+ * src/ShellModel/eigenvector_continuation.jl:212-310; calcOBTD, prepTBTD,
+ * calcTBTD :1035-1380) for nvec sample vectors of h's basis (host, reference
+ * order, nvec <= 255): nmat_out[i*nvec + j] = <w_i|w_j>, and for each pair
+ * i <= j, in idx_from_ij order (shellmodel_main.jl:1297), ltd values
+ * td_out[pair*ltd + u]: the derivatives of <w_i|H|w_j> with respect to the
+ * proton SPEs (u < lp), the neutron SPEs, and the value of each TBME line of
+ * the snt file the handle was created from (hermitian partner included, no
+ * mass scaling) — the reference's OBTD and TBTD.  ltd = lp + ln + number of
+ * TBME lines (smgpu_ec_td_length).  Every unit's Hamiltonian is set up on
+ * the sample basis and applied on the GPU in FP64. */
+int smgpu_ec_td_length(const smgpu_problem* h, int* ltd);
+int smgpu_ec_td(smgpu_problem* h, const double* vecs, int nvec, double* nmat_out, double* td_out);
+
+/* Wigner 3j (j1 j2 j3; m1 m2 m3) and 6j {j1 j2 j3; j4 j5 j6} symbols with
+ * doubled arguments (the values of WignerSymbols.jl's wigner3j / wigner6j,
+ * used by eval_moment and transit_main; host code, no GPU needed). */
+double smgpu_wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3);
+double smgpu_wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
+
 /* J-projected ("double") Lanczos for the lowest num_ev states of total
  * angular momentum twoJ/2: TRL with doubleLanczos = true
  * (lanczos_methods.jl:1-91) — every new Krylov vector is projected onto J by

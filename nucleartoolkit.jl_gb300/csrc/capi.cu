@@ -1025,10 +1025,11 @@ int smgpu_problem_create(const smgpu_problem_desc* d, int precision, smgpu_probl
       else throw SetupError{SMGPU_ERR_ARG, "TBME with the proton index after the neutron index"};
       if (d->hermitian_partners) {
         bool same = (a == b) ? (c == dd && c == a) : (c != dd && a == c && b == dd);
-        if (!same) I.tb[kind].push_back({c, dd, a, b, l[4], d->tbme[k]});
+        if (!same) I.tb[kind].push_back({c, dd, a, b, l[4], d->tbme[k], k + 1});
       }
-      I.tb[kind].push_back({a, b, c, dd, l[4], d->tbme[k]});
+      I.tb[kind].push_back({a, b, c, dd, l[4], d->tbme[k], k + 1});
     }
+    I.nlines = d->ntbme;
     return create_common(I, d->vp, d->vn, d->mtot2, precision, out);
   });
 }

@@ -1,5 +1,6 @@
 // The problem handle behind the C ABI (shared by capi.cu and multi.cu).
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -203,6 +204,9 @@ struct smgpu_problem {
       c32.vtab = tables.upload(to_f32(vt2));
     }
     set_config(128, 4, 1);
+    // the synchronous uploads run on the legacy stream; the handle's streams
+    // are non-blocking, so finish them before any kernel reads the tables
+    SMGPU_CUDA_TRY(cudaDeviceSynchronize());
   }
 
   // FP64 coefficient tables for a handle created in the mixed form (the

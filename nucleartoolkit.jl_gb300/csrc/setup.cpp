@@ -124,9 +124,10 @@ Interaction read_snt(const std::string& path, int Anum) {
     if (massop == 1) v *= std::pow((double)Anum / Aref, pw);
     // readsmsnt adds (c,d,a,b) first when unique([a,b]) != unique([c,d]) (:354-357)
     bool same = (a == b) ? (c == d && c == a) : (c != d && a == c && b == d);
-    if (!same) I.tb[kind].push_back({c, d, a, b, J, v});
-    I.tb[kind].push_back({a, b, c, d, J, v});
+    if (!same) I.tb[kind].push_back({c, d, a, b, J, v, k + 1});
+    I.tb[kind].push_back({a, b, c, d, J, v, k + 1});
   }
+  I.nlines = ntbme;
   return I;
 }
 
@@ -230,11 +231,13 @@ double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
 }
 
 namespace {
-double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
-  if (tm1 + tm2 != tM) return 0.0;
-  if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return 0.0;
-  if (((tj1 + tm1) | (tj2 + tm2) | (tJ + tM)) & 1) return 0.0;
-  if (tJ > tj1 + tj2 || tJ < std::abs(tj1 - tj2) || ((tj1 + tj2 + tJ) & 1)) return 0.0;
+// ⟨j1 m1 j2 m2|J M⟩² as an exact reduced fraction num/den and its sign;
+// false when the coefficient vanishes.
+bool cg_square(int tj1, int tm1, int tj2, int tm2, int tJ, int tM, i128& num, i128& den, int& sign) {
+  if (tm1 + tm2 != tM) return false;
+  if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return false;
+  if (((tj1 + tm1) | (tj2 + tm2) | (tJ + tM)) & 1) return false;
+  if (tJ > tj1 + tj2 || tJ < std::abs(tj1 - tj2) || ((tj1 + tj2 + tJ) & 1)) return false;
   int n1 = (tj1 + tj2 - tJ) / 2, n2 = (tj1 - tj2 + tJ) / 2, n3 = (tj2 - tj1 + tJ) / 2;
   int j1mm1 = (tj1 - tm1) / 2, j2pm2 = (tj2 + tm2) / 2;
   i128 S = 0;
@@ -242,9 +245,10 @@ double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) 
     i128 t = binom(n1, k) * binom(n2, j1mm1 - k) * binom(n3, j2pm2 - k);
     S += (k & 1) ? -t : t;
   }
-  if (S == 0) return 0.0;
+  if (S == 0) return false;
   int s3 = (tj1 + tj2 + tJ) / 2;
-  i128 num = S * S, den = 1;
+  num = S * S;
+  den = 1;
   auto mul_num = [&](i128 x) { i128 g = gcd_(x, den); num *= x / g; den /= g; g = gcd_(num, den); num /= g; den /= g; };
   auto mul_den = [&](i128 x) { i128 g = gcd_(x, num); den *= x / g; num /= g; g = gcd_(num, den); num /= g; den /= g; };
   mul_num(binom(tj1, n1));
@@ -255,10 +259,95 @@ double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) 
   mul_den(binom(tj1, j1mm1));
   mul_den(binom(tj2, (tj2 - tm2) / 2));
   mul_den(binom(tJ, (tJ - tM) / 2));
+  sign = S < 0 ? -1 : 1;
+  return true;
+}
+
+double clebsch_gordan_exact(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
+  i128 num, den;
+  int sign;
+  if (!cg_square(tj1, tm1, tj2, tm2, tJ, tM, num, den, sign)) return 0.0;
   double v = std::sqrt((double)num / (double)den);
-  return S < 0 ? -v : v;
+  return sign < 0 ? -v : v;
+}
+
+// Exact fraction with 128-bit parts, reduced after every operation.
+struct Frac {
+  i128 n = 0, d = 1;
+  void reduce() {
+    if (d < 0) { d = -d; n = -n; }
+    i128 g = gcd_(n, d);
+    if (g > 1) { n /= g; d /= g; }
+  }
+};
+Frac fmul(Frac a, Frac b) {
+  i128 g1 = gcd_(a.n, b.d), g2 = gcd_(b.n, a.d);
+  if (g1 == 0) g1 = 1;
+  if (g2 == 0) g2 = 1;
+  Frac r{(a.n / g1) * (b.n / g2), (a.d / g2) * (b.d / g1)};
+  r.reduce();
+  return r;
+}
+Frac fadd(Frac a, Frac b) {
+  i128 g = gcd_(a.d, b.d);
+  if (g == 0) g = 1;
+  Frac r{a.n * (b.d / g) + b.n * (a.d / g), (a.d / g) * b.d};
+  r.reduce();
+  return r;
+}
+i128 factorial(int n) {
+  i128 r = 1;
+  for (int i = 2; i <= n; ++i) r *= i;
+  return r;
+}
+// Δ(abc)² = (a+b-c)!(a-b+c)!(-a+b+c)!/(a+b+c+1)! for doubled a, b, c; false
+// when the triad is not a triangle with an integer sum.
+bool triad(int ta, int tb, int tc, Frac& out) {
+  if (((ta + tb + tc) & 1) || tc > ta + tb || tc < std::abs(ta - tb)) return false;
+  out = Frac{factorial((ta + tb - tc) / 2) * factorial((ta - tb + tc) / 2), 1};
+  out = fmul(out, Frac{factorial((-ta + tb + tc) / 2), factorial((ta + tb + tc) / 2 + 1)});
+  return true;
 }
 }  // namespace
+
+// (j1 j2 j3; m1 m2 m3) = (-1)^(j1-j2-m3) ⟨j1 m1 j2 m2|j3 -m3⟩ / sqrt(2 j3 + 1),
+// squared exactly before the one final square root.
+double wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3) {
+  i128 num, den;
+  int sign;
+  if (!cg_square(tj1, tm1, tj2, tm2, tj3, -tm3, num, den, sign)) return 0.0;
+  Frac q = fmul(Frac{num, den}, Frac{1, (i128)(tj3 + 1)});
+  if (((tj1 - tj2 - tm3) / 2) & 1) sign = -sign;
+  const double v = std::sqrt((double)q.n / (double)q.d);
+  return sign < 0 ? -v : v;
+}
+
+// {j1 j2 j3; j4 j5 j6} by Racah's single sum:
+//   Δ(j1 j2 j3)Δ(j1 j5 j6)Δ(j4 j2 j6)Δ(j4 j5 j3) Σ_t (-1)^t (t+1)! /
+//   [Π_k (t-α_k)! Π_l (β_l-t)!],
+// α = the four triad sums, β = j1+j2+j4+j5, j2+j3+j5+j6, j3+j1+j6+j4;
+// the square is exact and rounded once.
+double wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6) {
+  Frac d1, d2, d3, d4;
+  if (!triad(tj1, tj2, tj3, d1) || !triad(tj1, tj5, tj6, d2) || !triad(tj4, tj2, tj6, d3) ||
+      !triad(tj4, tj5, tj3, d4))
+    return 0.0;
+  const int a[4] = {(tj1 + tj2 + tj3) / 2, (tj1 + tj5 + tj6) / 2, (tj4 + tj2 + tj6) / 2, (tj4 + tj5 + tj3) / 2};
+  const int b[3] = {(tj1 + tj2 + tj4 + tj5) / 2, (tj2 + tj3 + tj5 + tj6) / 2, (tj3 + tj1 + tj6 + tj4) / 2};
+  const int tmin = std::max(std::max(a[0], a[1]), std::max(a[2], a[3]));
+  const int tmax = std::min(std::min(b[0], b[1]), b[2]);
+  Frac S{0, 1};
+  for (int t = tmin; t <= tmax; ++t) {
+    i128 den = 1;
+    for (int k = 0; k < 4; ++k) den *= factorial(t - a[k]);
+    for (int l = 0; l < 3; ++l) den *= factorial(b[l] - t);
+    S = fadd(S, Frac{(t & 1) ? -factorial(t + 1) : factorial(t + 1), den});
+  }
+  if (S.n == 0) return 0.0;
+  Frac q = fmul(fmul(fmul(d1, d2), fmul(d3, d4)), fmul(S, S));
+  const double v = std::sqrt((double)q.n / (double)q.d);
+  return S.n < 0 ? -v : v;
+}
 
 // ------------------------------------------------------------- helpers
 namespace {

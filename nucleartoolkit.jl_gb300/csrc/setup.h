@@ -21,8 +21,10 @@ struct Interaction {
   struct TB {
     int a, b, c, d, J;
     double v;
+    int line = 0;  // 1-based TBME line of the snt file (readsmsnt's ith)
   };
   std::vector<TB> tb[3];
+  int nlines = 0;  // TBME lines of the snt file
 };
 
 struct SetupError {
@@ -44,6 +46,11 @@ void parse_nucleus(const std::string& nuc, int& A, int& Z);
 
 // Clebsch–Gordan coefficient with doubled arguments (exact, binomial form).
 double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM);
+// Wigner 3j (j1 j2 j3; m1 m2 m3) and 6j {j1 j2 j3; j4 j5 j6} symbols with
+// doubled arguments (exact squares, one final rounding), the values of
+// WignerSymbols.jl's wigner3j / wigner6j(Float64, ...).
+double wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3);
+double wigner6j(int tj1, int tj2, int tj3, int tj4, int tj5, int tj6);
 
 // One m-state of a species, in construct_msps order (shellmodel_main.jl:373-384).
 struct MState {

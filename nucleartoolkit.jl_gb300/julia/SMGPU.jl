@@ -71,6 +71,36 @@ function jj(h::Ptr{Cvoid}, vecs::Vector{Vector{Float64}})
     return out
 end
 
+"""<vl_a| O |vr_b> of the one-body M1 (op = 0) or E2 (op = 1) operator
+(smgpu_obtr): symmetric = true is eval_moment's form on one basis
+(transit.jl:82-284), false transit_main's from hr's basis to hl's
+(transit.jl:286-531).  Returns an nl x nr matrix."""
+function obtr(hl::Ptr{Cvoid}, hr::Ptr{Cvoid}, op::Integer, vl::Vector{Vector{Float64}},
+              vr::Vector{Vector{Float64}}; symmetric::Bool=true,
+              gfactors=[1.0, 0.0, 5.586, -3.826], effcharge=[1.5, 0.5])
+    fl = reduce(vcat, vl); fr = reduce(vcat, vr)
+    out = zeros(Float64, length(vr), length(vl))   # C row-major nl x nr
+    check(ccall((:smgpu_obtr, libsmgpu), Cint,
+                (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint,
+                 Ptr{Float64}, Cint, Ptr{Float64}),
+                hl, hr, op, symmetric ? 1 : 0, Vector{Float64}(gfactors), Vector{Float64}(effcharge),
+                fl, length(vl), fr, length(vr), out), hl)
+    return permutedims(out)
+end
+
+"""Nmat and the transition densities of prepEC mode "TD" (smgpu_ec_td,
+eigenvector_continuation.jl:212-310): TDs[:, Nij] = [OBTD_p; OBTD_n; TBTD]."""
+function ec_td(h::Ptr{Cvoid}, vecs::Vector{Vector{Float64}})
+    n = length(vecs)
+    ltd = Ref{Cint}(0)
+    check(ccall((:smgpu_ec_td_length, libsmgpu), Cint, (Ptr{Cvoid}, Ref{Cint}), h, ltd), h)
+    nmat = zeros(Float64, n, n)
+    tds = zeros(Float64, Int(ltd[]), div(n * (n + 1), 2))
+    check(ccall((:smgpu_ec_td, libsmgpu), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint, Ptr{Float64}, Ptr{Float64}),
+                h, reduce(vcat, vecs), n, nmat, tds), h)
+    return nmat, tds
+end
+
 # shellmodel_main.jl:1105-1113
 function J_from_JJ1(JJ, tol=1.e-6)
     for J = 0:100

@@ -2,6 +2,8 @@
 `main_sm` path) behind the C ABI of libsmgpu.so."""
 from ._lib import FP64, MIXED, SmgpuError, library_path, load
 from .shellmodel import BatchProblem, MultiSampleProblem, ShellModelProblem, main_sm
+from .transit import eval_moment, transit_main
+from .ec import prep_ec, solve_ec
 
-__all__ = ["FP64", "MIXED", "SmgpuError", "ShellModelProblem", "MultiSampleProblem", "BatchProblem", "main_sm", "load",
-           "library_path"]
+__all__ = ["FP64", "MIXED", "SmgpuError", "ShellModelProblem", "MultiSampleProblem", "BatchProblem", "main_sm",
+           "eval_moment", "transit_main", "prep_ec", "solve_ec", "load", "library_path"]

@@ -39,6 +39,11 @@ SIGNATURES = {
     "smgpu_matvec": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_int]),
     "smgpu_solve": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),
     "smgpu_jj": (C.c_int, [_vp, _vp, C.c_int, _vp]),
+    "smgpu_obtr": (C.c_int, [_vp, _vp, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp, C.c_int, _vp]),
+    "smgpu_ec_td_length": (C.c_int, [_vp, _vp]),
+    "smgpu_ec_td": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "smgpu_wigner3j": (C.c_double, [C.c_int] * 6),
+    "smgpu_wigner6j": (C.c_double, [C.c_int] * 6),
     "smgpu_solve_block": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp,
                                     _vp]),
     "smgpu_solve_J": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _vp, _vp]),

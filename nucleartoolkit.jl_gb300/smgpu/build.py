@@ -12,8 +12,8 @@ INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["hv.cu", "hv_multi.cu", "hv_batch.cu", "lanczos.cu", "multi_lanczos.cu", "batch_lanczos.cu", "enum.cu", "capi.cu",
-              "multi.cu", "batch.cu"]
-CXX_SOURCES = ["setup.cpp", "wavio.cpp"]
+              "multi.cu", "batch.cu", "obtr.cu", "ec.cu"]
+CXX_SOURCES = ["setup.cpp", "wavio.cpp", "obtr.cpp"]
 
 
 def _nvcc():

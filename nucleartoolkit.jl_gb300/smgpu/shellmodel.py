@@ -103,6 +103,39 @@ class ShellModelProblem:
         check(load().smgpu_jj(self._h, _p(v), n, _p(out)), self._h)
         return out
 
+    def obtr(self, op, vl, vr=None, right=None, symmetric=True, gfactors=None, effcharge=None):
+        """<vl_a| O |vr_b> for the one-body M1 (op 0) / E2 (op 1) operator on
+        the GPU.  symmetric: eval_moment's expectation-value form on this
+        basis (vr defaults to vl); otherwise transit_main's operator from the
+        basis of ``right`` (vr) to this one (vl), ΔM = (Mtot - right.Mtot)/2."""
+        R = self if right is None else right
+        vl = np.ascontiguousarray(np.atleast_2d(np.asarray(vl, dtype=np.float64)))
+        vr = vl if vr is None else np.ascontiguousarray(np.atleast_2d(np.asarray(vr, dtype=np.float64)))
+        if vl.shape[1] != self.mdim or vr.shape[1] != R.mdim:
+            raise ValueError("vector length does not match the basis dimension")
+        out = np.zeros((vl.shape[0], vr.shape[0]))
+        g = None if gfactors is None else np.ascontiguousarray(gfactors, dtype=np.float64)
+        e = None if effcharge is None else np.ascontiguousarray(effcharge, dtype=np.float64)
+        check(load().smgpu_obtr(self._h, R._h, int(op), 1 if symmetric else 0, _p(g), _p(e), _p(vl), vl.shape[0],
+                                _p(vr), vr.shape[0], _p(out)), self._h)
+        return out
+
+    def ec_td(self, vecs):
+        """Overlap matrix and transition densities of the sample vectors
+        (rows of vecs): prepEC mode "TD" (eigenvector_continuation.jl:212-310)
+        on the GPU.  Returns (Nmat, TDs) with TDs[pair] = [OBTD_p, OBTD_n,
+        TBTD per snt line] for the pairs i <= j in idx_from_ij order."""
+        v = np.ascontiguousarray(np.atleast_2d(np.asarray(vecs, dtype=np.float64)))
+        if v.shape[1] != self.mdim:
+            raise ValueError("vector length does not match the basis dimension")
+        n = v.shape[0]
+        ltd = C.c_int()
+        check(load().smgpu_ec_td_length(self._h, C.byref(ltd)), self._h)
+        nmat = np.zeros((n, n))
+        td = np.zeros((n * (n + 1) // 2, ltd.value))
+        check(load().smgpu_ec_td(self._h, _p(v), n, _p(nmat), _p(td)), self._h)
+        return nmat, td
+
     # --- compute
     def matvec(self, v, accumulate: bool = False, out=None):
         v = np.ascontiguousarray(v, dtype=np.float64)
@@ -328,8 +361,7 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
         if len(target_J) > 1:
             raise ValueError("Invalid `target_J` Multiple J is not supported now.")
         tJ = int(target_J[0])
-    unsupported = dict(block_with_target_J=is_block and tJ is not None, calc_moment=calc_moment,
-                       calc_entropy=calc_entropy,
+    unsupported = dict(block_with_target_J=is_block and tJ is not None, calc_entropy=calc_entropy,
                        visualize_occ=visualize_occ, print_evec=print_evec, truncation=bool(truncation_scheme),
                        debugmode=bool(debugmode))
     bad = [k for k, v in unsupported.items() if v]
@@ -355,13 +387,19 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
             v1 = np.array(vs[:q])
         else:
             v1 = vs[0]
-    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, v1=v1, want_vecs=verbose or save_wav,
+    r = P.solve(num_ev, lm=lm, ls=ls, tol=tol, max_restarts=max_restarts, v1=v1,
+                want_vecs=verbose or save_wav or calc_moment,
                 twoJ=tJ, block=int(q) if is_block else None)
     en = list(map(float, r["evals"]))
     totJs = None
     if r["status"] == _lib.OK and r["evecs"] is not None:
         # J labels of the Ritz vectors (shellmodel_main.jl:226-240)
         totJs = [J_from_JJ1(x) for x in P.jj(r["evecs"])]
+    tx_mom = ""
+    if calc_moment and totJs is not None:
+        # eval_moment (:242-246, transit.jl:702-765)
+        from .transit import eval_moment
+        tx_mom = eval_moment(P, r["evecs"], totJs, gfactors, effcharge)["text"]
     if save_wav and totJs is not None:
         # writeRitzvecs to ./<nucleus>_<interaction>.wav (:248-253)
         from .wav import write_wav
@@ -378,6 +416,8 @@ def main_sm(sntf, target_nuc, num_ev, target_J, save_wav=False, q=1, is_block=Fa
         print("Ex. " + " ".join(f"{x - en[0]:10.4f}" for x in en))
         if is_show:
             print(P.timings())
+    if verbose and tx_mom != "":
+        print(tx_mom)
     P.close()
     if r["status"] == _lib.ERR_NOCONV:
         raise RuntimeError(f"Lanczos did not converge within {max_restarts} restarts")

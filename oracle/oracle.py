@@ -63,6 +63,18 @@ def lib():
         L.orc_trl_sample.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_void_p]
         L.orc_clebsch.restype = C.c_double
         L.orc_clebsch.argtypes = [C.c_int] * 6
+        L.orc_obtr.restype = C.c_int
+        L.orc_obtr.argtypes = [vp, vp, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                               C.c_void_p, C.c_int, C.c_void_p]
+        for f in ("orc_wigner3j", "orc_wigner6j"):
+            getattr(L, f).restype = C.c_double
+            getattr(L, f).argtypes = [C.c_int] * 6
+        L.orc_radius_power.restype = C.c_double
+        L.orc_radius_power.argtypes = [C.c_int] * 5 + [C.c_double]
+        L.orc_ec_td_length.restype = C.c_int
+        L.orc_ec_td_length.argtypes = [vp]
+        L.orc_ec_td.restype = C.c_int
+        L.orc_ec_td.argtypes = [vp, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_get_threads.restype = C.c_int
         _lib = L
@@ -83,6 +95,18 @@ def get_threads() -> int:
 
 def clebsch(tj1, tm1, tj2, tm2, tJ, tM):
     return lib().orc_clebsch(tj1, tm1, tj2, tm2, tJ, tM)
+
+
+def wigner3j(*a):
+    return lib().orc_wigner3j(*map(int, a))
+
+
+def wigner6j(*a):
+    return lib().orc_wigner6j(*map(int, a))
+
+
+def radius_power(k, n1, l1, n2, l2, bpar):
+    return lib().orc_radius_power(int(k), int(n1), int(l1), int(n2), int(l2), float(bpar))
 
 
 def sym_eig(A):
@@ -253,3 +277,34 @@ class OracleProblem:
         return dict(evals=ev, evecs=vecs, elit=int(stats[0]), n_hv=int(stats[1]), n_restart=int(stats[2]),
                     converged=bool(stats[3]), t_hv=float(times[0]), t_reorth=float(times[1]),
                     t_total=float(times[2]))
+
+    def obtr(self, op, vl, vr=None, right=None, symmetric=True, gfactors=(1.0, 0.0, 5.586, -3.826),
+             effcharge=(1.5, 0.5)):
+        """<vl_a| O |vr_b> for op 0 (M1) / 1 (E2): symmetric -> eval_moment's
+        operator (transit.jl:82-284), else transit_main's between this basis
+        (left) and ``right`` (transit.jl:286-531)."""
+        R = right if right is not None else self
+        vl = np.ascontiguousarray(np.atleast_2d(np.asarray(vl, dtype=np.float64)))
+        vr = vl if vr is None else np.ascontiguousarray(np.atleast_2d(np.asarray(vr, dtype=np.float64)))
+        out = np.zeros((vl.shape[0], vr.shape[0]))
+        g = np.asarray(gfactors, dtype=np.float64)
+        e = np.asarray(effcharge, dtype=np.float64)
+        rc = lib().orc_obtr(self._h, R._h, int(op), 1 if symmetric else 0, _p(g), _p(e), _p(vl), vl.shape[0], _p(vr),
+                            vr.shape[0], _p(out))
+        if rc != 0:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return out
+
+    def ec_td(self, vecs):
+        """prepEC "TD" (eigenvector_continuation.jl:212-310): the overlap
+        matrix and, per pair i <= j (idx_from_ij order), [OBTD_p, OBTD_n,
+        TBTD per snt line] from the restatement of calcOBTD / prepTBTD /
+        calcTBTD (:1035-1380)."""
+        v = np.ascontiguousarray(np.atleast_2d(np.asarray(vecs, dtype=np.float64)))
+        n = v.shape[0]
+        ltd = lib().orc_ec_td_length(self._h)
+        nmat = np.zeros((n, n))
+        td = np.zeros((n * (n + 1) // 2, ltd))
+        if lib().orc_ec_td(self._h, _p(v), n, _p(nmat), _p(td)) != 0:
+            raise RuntimeError(lib().orc_last_error().decode())
+        return nmat, td

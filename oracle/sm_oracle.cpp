@@ -92,6 +92,7 @@ struct Snt {
   std::vector<double> SPEs[2];
   std::vector<std::array<int, 6>> labels[3];  // a,b,c,d,J,line  (pp, nn, pn)
   std::vector<double> TBMEs[3];
+  int ntbme = 0;  // TBME lines (length of oTBMEs)
 };
 
 int parse_int(const std::string& s) {
@@ -144,6 +145,7 @@ Snt readsmsnt(const std::string& path, int Anum) {
   }
   auto ht = fields(L(1 + s.ln + s.lp + 1 + nsp + 1));
   int ntbme = parse_int(ht[0]);
+  s.ntbme = ntbme;
   s.massop = parse_int(ht[1]);
   s.Aref = parse_dbl(ht[2]);
   if (ht.size() > 3) s.p = parse_dbl(ht[3]);
@@ -212,11 +214,12 @@ i128 fact(int n) {
   for (int i = 2; i <= n; ++i) r *= i;
   return r;
 }
-double clebsch(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
-  if (tm1 + tm2 != tM) return 0.0;
-  if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return 0.0;
-  if (((tj1 + tm1) & 1) || ((tj2 + tm2) & 1) || ((tJ + tM) & 1)) return 0.0;
-  if (tJ > tj1 + tj2 || tJ < std::abs(tj1 - tj2) || ((tj1 + tj2 + tJ) & 1)) return 0.0;
+// CG² as an exact fraction with the sign of CG; false when CG = 0.
+bool clebsch_sq(int tj1, int tm1, int tj2, int tm2, int tJ, int tM, Rat& c2, int& sign) {
+  if (tm1 + tm2 != tM) return false;
+  if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return false;
+  if (((tj1 + tm1) & 1) || ((tj2 + tm2) & 1) || ((tJ + tM) & 1)) return false;
+  if (tJ > tj1 + tj2 || tJ < std::abs(tj1 - tj2) || ((tj1 + tj2 + tJ) & 1)) return false;
   int a = (tj1 + tj2 - tJ) / 2, b = (tj1 - tj2 + tJ) / 2, c = (-tj1 + tj2 + tJ) / 2;
   int s = (tj1 + tj2 + tJ) / 2 + 1;
   // A = (2J+1) a! b! c! / s! * (j1+m1)!(j1-m1)!(j2+m2)!(j2-m2)!(J+M)!(J-M)!
@@ -238,9 +241,52 @@ double clebsch(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
     Rat t{(k & 1) ? -1 : 1, den};
     S = radd(S, t);
   }
-  if (S.n == 0) return 0.0;
-  Rat c2 = rmul(rmul(A, S), S);
+  if (S.n == 0) return false;
+  c2 = rmul(rmul(A, S), S);
+  sign = S.n < 0 ? -1 : 1;
+  return true;
+}
+double clebsch(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
+  Rat c2;
+  int sign;
+  if (!clebsch_sq(tj1, tm1, tj2, tm2, tJ, tM, c2, sign)) return 0.0;
   double v = std::sqrt((double)c2.n / (double)c2.d);
+  return sign < 0 ? -v : v;
+}
+// WignerSymbols.jl wigner3j(Float64, j1, j2, j3, m1, m2, m3) (doubled
+// arguments): (-1)^(j1-j2-m3) <j1 m1 j2 m2|j3 -m3> / sqrt(2 j3 + 1).
+double wigner3j(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3) {
+  Rat c2;
+  int sign;
+  if (!clebsch_sq(tj1, tm1, tj2, tm2, tj3, -tm3, c2, sign)) return 0.0;
+  c2 = rmul(c2, Rat{1, (i128)(tj3 + 1)});
+  if (((tj1 - tj2 - tm3) / 2) & 1) sign = -sign;
+  double v = std::sqrt((double)c2.n / (double)c2.d);
+  return sign < 0 ? -v : v;
+}
+// WignerSymbols.jl wigner6j(Float64, ...) (doubled arguments), Racah's formula
+// {a b c; d e f} = Δ(abc)Δ(aef)Δ(dbf)Δ(dec) Σ_t (-1)^t (t+1)! /
+// [(t-abc)!(t-aef)!(t-dbf)!(t-dec)!(a+b+d+e-t)!(b+c+e+f-t)!(c+a+f+d-t)!].
+double wigner6j(int a, int b, int c, int d, int e, int f) {
+  auto tri = [](int x, int y, int z, Rat& out) {
+    if (((x + y + z) & 1) || z > x + y || z < std::abs(x - y)) return false;
+    out = rmul(Rat{fact((x + y - z) / 2) * fact((x - y + z) / 2), 1},
+               Rat{fact((-x + y + z) / 2), fact((x + y + z) / 2 + 1)});
+    return true;
+  };
+  Rat d1, d2, d3, d4;
+  if (!tri(a, b, c, d1) || !tri(a, e, f, d2) || !tri(d, b, f, d3) || !tri(d, e, c, d4)) return 0.0;
+  int al[4] = {(a + b + c) / 2, (a + e + f) / 2, (d + b + f) / 2, (d + e + c) / 2};
+  int be[3] = {(a + b + d + e) / 2, (b + c + e + f) / 2, (c + a + f + d) / 2};
+  Rat S{0, 1};
+  for (int t = *std::max_element(al, al + 4); t <= *std::min_element(be, be + 3); ++t) {
+    i128 den = fact(t - al[0]) * fact(t - al[1]) * fact(t - al[2]) * fact(t - al[3]);
+    den *= fact(be[0] - t) * fact(be[1] - t) * fact(be[2] - t);
+    S = radd(S, Rat{(t & 1) ? -fact(t + 1) : fact(t + 1), den});
+  }
+  if (S.n == 0) return 0.0;
+  Rat q = rmul(rmul(rmul(d1, d2), rmul(d3, d4)), rmul(S, S));
+  double v = std::sqrt((double)q.n / (double)q.d);
   return S.n < 0 ? -v : v;
 }
 
@@ -1488,6 +1534,536 @@ Problem* build_problem(const std::string& sntf, const std::string& nuc, int nthr
   return P;
 }
 
+
+// ===========================================================================
+// One-body M1 / E2 operators (src/ShellModel/transit.jl).
+
+// transit.jl:49-60 init_ho_by_mass
+void init_ho_by_mass(int A, int hwprm, double& hw, double& bpar) {
+  const double nmass[2] = {938.27231, 939.56563};
+  const double amass = (nmass[0] + nmass[1]) / 2;
+  const double hc = 197.32696;
+  if (hwprm == 1) hw = 41.0 * std::pow((double)A, -1.0 / 3.0);
+  else hw = 45.0 * std::pow((double)A, -1.0 / 3.0) - 25.0 * std::pow((double)A, -2.0 / 3.0);
+  bpar = hc / std::sqrt(hw * amass);
+}
+
+// transit.jl:62-80 radius_power.  Julia evaluates the sum in BigInt/BigFloat
+// (Combinatorics.doublefactorial); here exact integers up to the two square
+// roots, which are taken in long double.
+long double jl_binomial(int n, int k) {
+  if (k < 0) return 0;
+  if (n < 0) return ((k & 1) ? -1 : 1) * jl_binomial(k - n - 1, k);
+  if (k > n) return 0;
+  long double r = 1;
+  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
+  return r;
+}
+long double doublefactorial(int n) {
+  long double r = 1;
+  for (int i = n; i >= 2; i -= 2) r *= i;
+  return r;
+}
+double radius_power(int k, int n1, int l1, int n2, int l2, double bpar) {
+  long double s = 0;
+  int ll = l1 + l2 + k, ll1 = l2 - l1 + k, ll2 = l1 - l2 + k;
+  ll1 = ll1 / 2;
+  ll2 = ll2 / 2;
+  int imin = std::max(std::max(0, n1 - ll1), n2 - ll2), imax = std::min(n1, n2);
+  for (int i = imin; i <= imax; ++i)
+    s += jl_binomial(ll1, n1 - i) * jl_binomial(ll2, n2 - i) * (doublefactorial(ll + 2 * i + 1) / doublefactorial(2 * i));
+  s *= std::sqrt(doublefactorial(2 * n1) / doublefactorial(2 * n1 + 2 * l1 + 1));
+  s *= std::sqrt(doublefactorial(2 * n2) / doublefactorial(2 * n2 + 2 * l2 + 1));
+  return (double)s * (1.0 / std::sqrt(std::pow(2.0, k))) * (((n1 - n2) & 1) ? -1.0 : 1.0) * std::pow(bpar, k);
+}
+
+inline double pm1(int e) { return (e & 1) ? -1.0 : 1.0; }
+
+// transit.jl:1-15 op_M1 / op_E2 (1-based block and SD numbers)
+struct OpD {
+  int bi, i, f;
+  bool phase;
+  double fac;
+};
+// transit.jl:17-31 op_M1_nd / op_E2_nd
+struct OpND {
+  int bl, Nl, br, Nr;
+  bool phase;
+  double fac;
+};
+struct Obtr {
+  std::vector<OpD> d[4];    // pjumps_mu, njumps_mu, pjumps_Q, njumps_Q
+  std::vector<OpND> nd[4];
+};
+
+// transit.jl:82-245 prep_obtr_diag
+void prep_obtr_diag(const Problem& P, double bpar, const double* gfactors, const double* eff_charge, Obtr& O) {
+  const double ec_p = eff_charge[0], ec_n = eff_charge[1];
+  const double c_mom_mu = std::sqrt(3.0 / (4.0 * M_PI)), c_mom_Q = std::sqrt(5.0 / (16.0 * M_PI));
+  const int lblock = (int)P.B.nbits.size();
+  for (int sp = 0; sp < 2; ++sp) {
+    const auto& sps = sp == 0 ? P.snt.p_sps : P.snt.n_sps;
+    const auto& msps = sp == 0 ? P.ms.p : P.ms.n;
+    const int L = (int)msps.size();
+    const auto& bits = sp == 0 ? P.B.pbits : P.B.nbits;
+    const int lsp = (int)sps.size();
+    for (int i = 1; i <= lsp; ++i) {
+      const int ni = sps[i - 1][0], li = sps[i - 1][1], ji = sps[i - 1][2];
+      for (int f = i; f <= lsp; ++f) {
+        const int nf = sps[f - 1][0], lf = sps[f - 1][1], jf = sps[f - 1][2];
+        const double ex_r2 = radius_power(2, ni, li, nf, lf, bpar);
+        const double l6j = wigner6j(2 * lf, 2 * li, 2, ji, jf, 1);
+        const double s6j = wigner6j(1, 1, 2, ji, jf, 2 * lf);
+        const double Q3j = wigner3j(ji, 4, jf, 1, 0, -1);
+        int jc, ja;
+        std::vector<int> mc_s, mc_idxs, ma_s, ma_idxs;
+        possible_mz(sps[i - 1], msps, jc, mc_s, mc_idxs);
+        possible_mz(sps[f - 1], msps, ja, ma_s, ma_idxs);
+        for (int mode = 0; mode < 2; ++mode) {  // "M1", "E2"
+          if (mode == 0 && (ni != nf || li != lf)) continue;
+          for (size_t ic = 0; ic < mc_s.size(); ++ic) {
+            const int mc = mc_s[ic];
+            const i64 bit_c = onehot(L, mc_idxs[ic]);
+            for (size_t ia = 0; ia < ma_s.size(); ++ia) {
+              const int ma = ma_s[ia];
+              if (ma != mc) continue;
+              const i64 bit_a = onehot(L, ma_idxs[ia]);
+              const double pfac = std::sqrt((double)((ji + 1) * (jf + 1)));
+              double coeff;
+              if (sp == 0) {
+                if (mode == 0) {
+                  const double sign1 = pm1((jf - ma) / 2 + lf + (ji + 3) / 2);
+                  const double sign2 = pm1((jf - ma) / 2 + lf + (jf + 3) / 2);
+                  const double fac1 = sign1 * l6j * std::sqrt((double)(lf * (lf + 1) * (2 * lf + 1)));
+                  const double fac2 = sign2 * s6j * std::sqrt(1.5);
+                  const double m3j = pfac * wigner3j(jf, 2, ji, -ma, 0, mc);
+                  coeff = m3j * (fac1 * gfactors[0] + fac2 * gfactors[2]) * c_mom_mu;
+                } else {
+                  const double signQ = pm1(jf + (1 - ma) / 2) * (1 + pm1(li + lf));
+                  if (signQ == 0) continue;
+                  const double m3j = wigner3j(jf, 4, ji, -ma, 0, mc);
+                  coeff = signQ * m3j * Q3j * pfac * ec_p * c_mom_Q * ex_r2;
+                }
+              } else {
+                const double sign1 = pm1((jf - ma) / 2 + lf + (ji + 3) / 2);
+                const double sign2 = pm1((jf - ma) / 2 + lf + (jf + 3) / 2);
+                if (mode == 0) {
+                  const double fac1 = sign1 * pfac * std::sqrt((double)(lf * (lf + 1) * (2 * lf + 1))) * l6j;
+                  const double fac2 = sign2 * pfac * std::sqrt(1.5) * s6j;
+                  const double m3j = wigner3j(jf, 2, ji, -ma, 0, mc);
+                  coeff = m3j * (fac1 * gfactors[1] + fac2 * gfactors[3]) * c_mom_mu;
+                } else {
+                  const double signQ = pm1(jf + (1 - ma) / 2) * (1 + pm1(li + lf));
+                  if (signQ == 0) continue;
+                  const double m3j = wigner3j(jf, 4, ji, -ma, 0, mc);
+                  coeff = signQ * m3j * Q3j * pfac * ec_n * c_mom_Q * ex_r2;
+                  if (coeff == 0.0) continue;
+                }
+              }
+              for (int bi = 1; bi <= lblock; ++bi) {
+                const auto& bl = bits[bi - 1];
+                for (size_t N = 0; N < bl.size(); ++N) {
+                  const i64 Phi = bl[N];
+                  if (!TF_connectable_1(Phi, bit_a, bit_c)) continue;
+                  int ph;
+                  i64 nPhi;
+                  calc_phase_1(Phi, bit_a, bit_c, ph, nPhi);
+                  const int Nf = bisearch_desc(bl, nPhi);
+                  if (Nf == 0) continue;
+                  const int Ni = (int)N + 1;
+                  O.d[2 * mode + sp].push_back(OpD{bi, Ni, Nf, ph == -1, coeff * (Ni == Nf ? 0.5 : 1.0)});
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// transit.jl:247-284 op_obtr_diag (twf accumulates)
+void op_obtr_diag(const Problem& P, const std::vector<OpD>& p_oprts, const std::vector<OpD>& n_oprts,
+                  const double* wf, double* twf) {
+  for (const OpD& t : p_oprts) {
+    const double coeff = t.phase ? -t.fac : t.fac;
+    const i64 idim = P.B.tdims[t.bi - 1];
+    const i64 l_Nn = (i64)P.B.nbits[t.bi - 1].size();
+    const i64 tMi = idim + (t.i - 1) * l_Nn, tMf = idim + (t.f - 1) * l_Nn;  // 0-based
+    for (i64 n = 0; n < l_Nn; ++n) {
+      twf[tMf + n] += coeff * wf[tMi + n];
+      twf[tMi + n] += coeff * wf[tMf + n];
+    }
+  }
+  for (const OpD& t : n_oprts) {
+    const double coeff = t.phase ? -t.fac : t.fac;
+    const i64 idim = P.B.tdims[t.bi - 1];
+    const i64 l_Nn = (i64)P.B.nbits[t.bi - 1].size(), l_Np = (i64)P.B.pbits[t.bi - 1].size();
+    for (i64 p = 0; p < l_Np; ++p) {
+      const i64 Mi = idim + p * l_Nn + (t.i - 1), Mf = idim + p * l_Nn + (t.f - 1);
+      twf[Mf] += coeff * wf[Mi];
+      twf[Mi] += coeff * wf[Mf];
+    }
+  }
+}
+
+// transit.jl:501-531 calc_bifs (1-based [il, ir] pairs)
+void calc_bifs(const Problem& L, const Problem& R, std::vector<std::array<int, 2>>& p_bifs,
+               std::vector<std::array<int, 2>>& n_bifs) {
+  std::vector<std::array<int, 2>> blocks_r, blocks_l;
+  for (int Mp : R.B.Mps)
+    for (int Mn : R.B.Mns)
+      if (Mp + Mn == R.Mtot) blocks_r.push_back({Mp, Mn});
+  for (int Mp : L.B.Mps)
+    for (int Mn : L.B.Mns)
+      if (Mp + Mn == L.Mtot) blocks_l.push_back({Mp, Mn});
+  for (size_t ir = 0; ir < blocks_r.size(); ++ir)
+    for (size_t il = 0; il < blocks_l.size(); ++il) {
+      if (blocks_r[ir][1] == blocks_l[il][1]) p_bifs.push_back({(int)il + 1, (int)ir + 1});
+      if (blocks_r[ir][0] == blocks_l[il][0]) n_bifs.push_back({(int)il + 1, (int)ir + 1});
+    }
+}
+
+// transit.jl:286-445 prep_obtr_nondiag (Mtot_l = jl2, Mtot_r = jr2)
+void prep_obtr_nondiag(const Problem& L, const Problem& R, double bpar, const double* gfactors,
+                       const double* eff_charge, Obtr& O) {
+  const int jl2 = L.Mtot, jr2 = R.Mtot;
+  const int omu = (jl2 - jr2) / 2;  // Julia div truncates toward zero
+  std::vector<std::array<int, 2>> bifs[2];
+  calc_bifs(L, R, bifs[0], bifs[1]);
+  const double ec_p = eff_charge[0], ec_n = eff_charge[1];
+  const double c_mom_mu = std::sqrt(3.0 / (4.0 * M_PI)), c_mom_Q = std::sqrt(5.0 / (16.0 * M_PI));
+  for (int sp = 0; sp < 2; ++sp) {
+    const auto& sps = sp == 0 ? L.snt.p_sps : L.snt.n_sps;
+    const auto& msps = sp == 0 ? L.ms.p : L.ms.n;
+    const int Lm = (int)msps.size();
+    const auto& bits_l = sp == 0 ? L.B.pbits : L.B.nbits;
+    const auto& bits_r = sp == 0 ? R.B.pbits : R.B.nbits;
+    const int lsp = (int)sps.size();
+    for (int i = 1; i <= lsp; ++i) {
+      const int ni = sps[i - 1][0], li = sps[i - 1][1], ji = sps[i - 1][2];
+      for (int f = 1; f <= lsp; ++f) {
+        const int nf = sps[f - 1][0], lf = sps[f - 1][1], jf = sps[f - 1][2];
+        const double ex_r2 = radius_power(2, ni, li, nf, lf, bpar);
+        const double l6j = wigner6j(2 * lf, 2 * li, 2, ji, jf, 1);
+        const double s6j = wigner6j(1, 1, 2, ji, jf, 2 * lf);
+        const double Q3j = wigner3j(ji, 4, jf, 1, 0, -1);
+        int jc, ja;
+        std::vector<int> mc_s, mc_idxs, ma_s, ma_idxs;
+        possible_mz(sps[i - 1], msps, jc, mc_s, mc_idxs);
+        possible_mz(sps[f - 1], msps, ja, ma_s, ma_idxs);
+        for (int mode = 0; mode < 2; ++mode) {
+          if (mode == 0) {
+            if (ni != nf || li != lf) continue;
+            if ((jl2 - jr2) / 2 > 1) continue;
+          } else if ((jl2 - jr2) / 2 > 2) {
+            continue;
+          }
+          for (size_t ic = 0; ic < mc_s.size(); ++ic) {
+            const int mc = mc_s[ic];
+            const i64 bit_c = onehot(Lm, mc_idxs[ic]);
+            for (size_t ia = 0; ia < ma_s.size(); ++ia) {
+              const int ma = ma_s[ia];
+              if ((ma - mc) / 2 != omu) continue;
+              const i64 bit_a = onehot(Lm, ma_idxs[ia]);
+              const double pfac = std::sqrt((double)((ji + 1) * (jf + 1)));
+              double coeff;
+              const double sign1 = pm1((jf - ma) / 2 + lf + (ji + 3) / 2);
+              const double sign2 = pm1((jf - ma) / 2 + lf + (jf + 3) / 2);
+              if (mode == 0) {
+                if (sp == 0) {
+                  const double fac1 = sign1 * l6j * std::sqrt((double)(lf * (lf + 1) * (2 * lf + 1)));
+                  const double fac2 = sign2 * s6j * std::sqrt(1.5);
+                  const double m3j = pfac * wigner3j(jf, 2, ji, -ma, 2 * omu, mc);
+                  coeff = m3j * (fac1 * gfactors[0] + fac2 * gfactors[2]) * c_mom_mu;
+                } else {
+                  const double fac1 = sign1 * pfac * std::sqrt((double)(lf * (lf + 1) * (2 * lf + 1))) * l6j;
+                  const double fac2 = sign2 * pfac * std::sqrt(1.5) * s6j;
+                  const double m3j = wigner3j(jf, 2, ji, -ma, 2 * omu, mc);
+                  coeff = m3j * (fac1 * gfactors[1] + fac2 * gfactors[3]) * c_mom_mu;
+                }
+              } else {
+                const double signQ = pm1(jf + (1 - ma) / 2) * (1 + pm1(li + lf));
+                if (signQ == 0) continue;
+                const double m3j = wigner3j(jf, 4, ji, -ma, 2 * omu, mc);
+                coeff = signQ * m3j * Q3j * pfac * (sp == 0 ? ec_p : ec_n) * c_mom_Q * ex_r2;
+              }
+              for (const auto& lr : bifs[sp]) {
+                const int bl = lr[0], br = lr[1];
+                const auto& rb = bits_r[br - 1];
+                for (size_t N = 0; N < rb.size(); ++N) {
+                  const i64 Phi = rb[N];
+                  if (!TF_connectable_1(Phi, bit_a, bit_c)) continue;
+                  int ph;
+                  i64 nPhi;
+                  calc_phase_1(Phi, bit_a, bit_c, ph, nPhi);
+                  const int Nf = bisearch_desc(bits_l[bl - 1], nPhi);
+                  if (Nf == 0) continue;
+                  O.nd[2 * mode + sp].push_back(OpND{bl, Nf, br, (int)N + 1, ph == -1, coeff});
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+// transit.jl:447-499 op_obtr_nondiag (twf accumulates, left basis)
+void op_obtr_nondiag(const Problem& L, const Problem& R, const std::vector<OpND>& p_oprts,
+                     const std::vector<OpND>& n_oprts, const double* wf, double* twf) {
+  for (const OpND& t : p_oprts) {
+    const double coeff = t.phase ? -t.fac : t.fac;
+    const auto& nbit_r = R.B.nbits[t.br - 1];
+    const auto& nbit_l = L.B.nbits[t.bl - 1];
+    const i64 tMi = R.B.tdims[t.br - 1] + (i64)(t.Nr - 1) * (i64)nbit_r.size();
+    const i64 tMf = L.B.tdims[t.bl - 1] + (i64)(t.Nl - 1) * (i64)nbit_l.size();
+    for (size_t r = 0; r < nbit_r.size(); ++r)
+      for (size_t l = 0; l < nbit_l.size(); ++l) {
+        if (nbit_r[r] != nbit_l[l]) continue;
+        twf[tMf + (i64)l] += coeff * wf[tMi + (i64)r];
+      }
+  }
+  for (const OpND& t : n_oprts) {
+    const double coeff = t.phase ? -t.fac : t.fac;
+    const auto& pbit_r = R.B.pbits[t.br - 1];
+    const auto& pbit_l = L.B.pbits[t.bl - 1];
+    const i64 lNr = (i64)R.B.nbits[t.br - 1].size(), lNl = (i64)L.B.nbits[t.bl - 1].size();
+    for (size_t r = 0; r < pbit_r.size(); ++r)
+      for (size_t l = 0; l < pbit_l.size(); ++l) {
+        if (pbit_r[r] != pbit_l[l]) continue;
+        const i64 Mi = R.B.tdims[t.br - 1] + (i64)r * lNr + (t.Nr - 1);
+        const i64 Mf = L.B.tdims[t.bl - 1] + (i64)l * lNl + (t.Nl - 1);
+        twf[Mf] += coeff * wf[Mi];
+      }
+  }
+}
+
+
+// ===========================================================================
+// Eigenvector-continuation transition densities
+// (src/ShellModel/eigenvector_continuation.jl).
+
+// shellmodel_main.jl:1297-1299 idx_from_ij (1-based)
+i64 idx_from_ij(i64 i, i64 j, i64 Dim) { return (Dim + 1) * (i - 1) - (i * (i - 1)) / 2 + j - i + 1; }
+
+// eigenvector_continuation.jl:1035-1099 calcOBTD: per pair, Σ_M w_i[M] w_j[M] jocc.
+void calcOBTD(const Problem& P, const std::vector<const double*>& wfs, std::vector<std::vector<double>>& OBTDs) {
+  const int lps = (int)P.snt.p_sps.size(), lns = (int)P.snt.n_sps.size();
+  const int Dim = (int)wfs.size();
+  for (int i = 1; i <= Dim; ++i)
+    for (int j = i; j <= Dim; ++j) {
+      std::vector<double>& T = OBTDs[idx_from_ij(i, j, Dim) - 1];
+      const double* wi = wfs[i - 1];
+      const double* wj = wfs[j - 1];
+      for (size_t bi = 0; bi < P.B.pbits.size(); ++bi) {
+        const i64 l_Nn = (i64)P.B.nbits[bi].size();
+        for (size_t p = 0; p < P.B.jocc_p[bi].size(); ++p)
+          for (i64 n = 0; n < l_Nn; ++n) {
+            const i64 M = P.B.tdims[bi] + (i64)p * l_Nn + n;
+            const double wfprod = wi[M] * wj[M];
+            for (int o = 0; o < lps; ++o) T[o] += wfprod * P.B.jocc_p[bi][p][o];
+            for (int o = 0; o < lns; ++o) T[lps + o] += wfprod * P.B.jocc_n[bi][n][o];
+          }
+      }
+    }
+}
+
+// eigenvector_continuation.jl:1085-1100 T1ifc / T0ifc
+struct T1ifc {
+  int nth, bi, i, f;
+  double fac;
+};
+struct T0ifc {
+  int i, f;
+  double fac;
+};
+
+// eigenvector_continuation.jl:1101-1304 prepTBTD + :1306-1380 calcTBTD,
+// accumulated into TBTDs[pair][line-1].
+void calcTBTD(const Problem& P, const std::vector<const double*>& wfs, std::vector<std::vector<double>>& TBTDs,
+              int off) {
+  const int lblock = (int)P.B.pbits.size();
+  const int lp = (int)P.ms.p.size(), ln = (int)P.ms.n.size();
+  const int Dim = (int)wfs.size();
+  const int loffs[2] = {0, (int)P.snt.p_sps.size()};
+  // pp / nn
+  std::vector<T1ifc> TBTD1[2];
+  for (int vrank = 0; vrank < 2; ++vrank) {
+    const int loff = loffs[vrank];
+    const auto& sps = vrank == 0 ? P.snt.p_sps : P.snt.n_sps;
+    const auto& ms = vrank == 0 ? P.ms.p : P.ms.n;
+    const auto& bits = vrank == 0 ? P.B.pbits : P.B.nbits;
+    const int L = vrank == 0 ? lp : ln;
+    for (size_t nth = 0; nth < P.snt.labels[vrank].size(); ++nth) {
+      const auto& lab = P.snt.labels[vrank][nth];
+      const int a = lab[0], b = lab[1], c = lab[2], d = lab[3], J2 = 2 * lab[4];
+      int ja, jb, jc, jd;
+      std::vector<int> ma_s, ma_i, mb_s, mb_i, mc_s, mc_i, md_s, md_i;
+      possible_mz(sps[a - loff - 1], ms, ja, ma_s, ma_i);
+      possible_mz(sps[b - loff - 1], ms, jb, mb_s, mb_i);
+      possible_mz(sps[c - loff - 1], ms, jc, mc_s, mc_i);
+      possible_mz(sps[d - loff - 1], ms, jd, md_s, md_i);
+      for (size_t ic = 0; ic < mc_s.size(); ++ic)
+        for (size_t id = 0; id < md_s.size(); ++id) {
+          const int mc = mc_s[ic], md = md_s[id];
+          if (c == d && mc >= md) continue;
+          if (std::abs(mc + md) > J2) continue;
+          const int M_ani = mc + md;
+          const i64 bit_c = onehot(L, mc_i[ic]), bit_d = onehot(L, md_i[id]);
+          for (size_t ia = 0; ia < ma_s.size(); ++ia)
+            for (size_t ib = 0; ib < mb_s.size(); ++ib) {
+              const int ma = ma_s[ia], mb = mb_s[ib];
+              if (a == b && ma >= mb) continue;
+              if (ma + mb != M_ani) continue;
+              const i64 bit_a = onehot(L, ma_i[ia]), bit_b = onehot(L, mb_i[ib]);
+              const double CG1 = clebsch(ja, ma, jb, mb, J2, M_ani);
+              const double CG2 = clebsch(jc, mc, jd, md, J2, M_ani);
+              const Key4 bl{bit_a, bit_b, bit_c, bit_d};
+              const double coeff = std::sqrt((1.0 + (a == b)) * (1.0 + (c == d))) * CG1 * CG2;
+              for (int bi = 1; bi <= lblock; ++bi) {
+                const auto& lst = bits[bi - 1];
+                for (size_t N = 0; N < lst.size(); ++N) {
+                  if (!TF_connectable(lst[N], bl)) continue;
+                  int ph;
+                  i64 nPhi;
+                  calc_phase(lst[N], bl, ph, nPhi);
+                  const int Nf = bisearch_desc(lst, nPhi);
+                  TBTD1[vrank].push_back(T1ifc{(int)nth, bi, (int)N + 1, Nf, coeff * ph});
+                }
+              }
+            }
+        }
+    }
+  }
+  // pn jumps: delMs over proton m-state pairs (descending), blocks bi <= bf
+  std::vector<int> delMs;
+  for (int j = 0; j < lp; ++j)
+    for (int i = 0; i < lp; ++i) delMs.push_back(P.ms.p[i][4] - P.ms.p[j][4]);
+  std::sort(delMs.begin(), delMs.end(), std::greater<int>());
+  delMs.erase(std::unique(delMs.begin(), delMs.end()), delMs.end());
+  auto inDel = [&](int dm) { return std::find(delMs.begin(), delMs.end(), dm) != delMs.end(); };
+  std::vector<std::vector<int>> bfs(lblock);
+  for (int i = 1; i <= lblock; ++i)
+    for (int j = i; j <= lblock; ++j)
+      if (inDel(P.B.Mps[j - 1] - P.B.Mps[i - 1])) bfs[i - 1].push_back(j);
+  const int nbif = lblock * (lblock + 1) / 2;
+  struct PnOp {
+    int nth;
+    std::vector<std::vector<T0ifc>> pj, nj;  // per bif_idx
+  };
+  std::vector<PnOp> pnops;
+  const auto& lab3 = P.snt.labels[2];
+  for (size_t nth = 0; nth < lab3.size(); ++nth) {
+    const int a = lab3[nth][0], b = lab3[nth][1], c = lab3[nth][2], d = lab3[nth][3], J2 = 2 * lab3[nth][4];
+    const int loff = loffs[1];
+    int ja, jb, jc, jd;
+    std::vector<int> ma_s, ma_i, mb_s, mb_i, mc_s, mc_i, md_s, md_i;
+    possible_mz(P.snt.p_sps[a - 1], P.ms.p, ja, ma_s, ma_i);
+    possible_mz(P.snt.p_sps[c - 1], P.ms.p, jc, mc_s, mc_i);
+    possible_mz(P.snt.n_sps[b - loff - 1], P.ms.n, jb, mb_s, mb_i);
+    possible_mz(P.snt.n_sps[d - loff - 1], P.ms.n, jd, md_s, md_i);
+    for (size_t ic = 0; ic < mc_s.size(); ++ic) {
+      const int mc = mc_s[ic];
+      const i64 bit_c = onehot(lp, mc_i[ic]);
+      for (size_t ia = 0; ia < ma_s.size(); ++ia) {
+        const int ma = ma_s[ia];
+        const i64 bit_a = onehot(lp, ma_i[ia]);
+        const int Mp = ma - mc;
+        for (size_t id = 0; id < md_s.size(); ++id) {
+          const int md = md_s[id];
+          if (std::abs(mc + md) > J2) continue;
+          const i64 bit_d = onehot(ln, md_i[id]);
+          for (size_t ib = 0; ib < mb_s.size(); ++ib) {
+            const int mb = mb_s[ib];
+            if (mb - md + Mp != 0) continue;
+            const i64 bit_b = onehot(ln, mb_i[ib]);
+            const double CG1 = clebsch(ja, ma, jb, mb, J2, ma + mb);
+            const double CG2 = clebsch(jc, mc, jd, md, J2, mc + md);
+            const double fac = CG1 * CG2;
+            PnOp op;
+            op.nth = (int)nth;
+            op.pj.assign(nbif, {});
+            op.nj.assign(nbif, {});
+            for (int bi = 1; bi <= lblock; ++bi)
+              for (int bf : bfs[bi - 1]) {
+                const int deltaM = P.B.Mps[bf - 1] - P.B.Mps[bi - 1];
+                const double tfac = fac * (bi == bf ? 0.5 : 1.0);
+                if (!inDel(deltaM)) continue;
+                const int bif = (int)idx_from_ij(bi, bf, lblock) - 1;
+                const auto& pb = P.B.pbits[bi - 1];
+                for (size_t N = 0; N < pb.size(); ++N) {
+                  if (!TF_connectable_1(pb[N], bit_a, bit_c)) continue;
+                  int ph;
+                  i64 f;
+                  calc_phase_1(pb[N], bit_a, bit_c, ph, f);
+                  const int Nf = bisearch_desc(P.B.pbits[bf - 1], f);
+                  if (Nf == 0) continue;
+                  op.pj[bif].push_back(T0ifc{(int)N + 1, Nf, tfac * ph});
+                }
+                const auto& nb = P.B.nbits[bi - 1];
+                for (size_t N = 0; N < nb.size(); ++N) {
+                  if (!TF_connectable_1(nb[N], bit_b, bit_d)) continue;
+                  int ph;
+                  i64 f;
+                  calc_phase_1(nb[N], bit_b, bit_d, ph, f);
+                  const int Nf = bisearch_desc(P.B.nbits[bf - 1], f);
+                  if (Nf == 0) continue;
+                  op.nj[bif].push_back(T0ifc{(int)N + 1, Nf, 1.0 * ph});
+                }
+              }
+            pnops.push_back(std::move(op));
+          }
+        }
+      }
+    }
+  }
+  std::vector<std::array<int, 2>> bif_idxs;
+  for (int i = 1; i <= lblock; ++i)
+    for (int j = i; j <= lblock; ++j) bif_idxs.push_back({i, j});
+  // calcTBTD
+  for (int i = 1; i <= Dim; ++i)
+    for (int j = i; j <= Dim; ++j) {
+      const double* w_i = wfs[i - 1];
+      const double* w_j = wfs[j - 1];
+      std::vector<double>& T = TBTDs[idx_from_ij(i, j, Dim) - 1];
+      for (int vrank = 0; vrank < 2; ++vrank)
+        for (const T1ifc& t : TBTD1[vrank]) {
+          const int vidx = P.snt.labels[vrank][t.nth][5];
+          const i64 lN = (i64)P.B.nbits[t.bi - 1].size(), lP = (i64)P.B.pbits[t.bi - 1].size();
+          const i64 td = P.B.tdims[t.bi - 1];
+          if (vrank == 0) {
+            for (i64 n = 0; n < lN; ++n) {
+              const i64 Mi = td + (t.i - 1) * lN + n, Mf = td + (t.f - 1) * lN + n;
+              T[off + vidx - 1] += t.fac * (w_i[Mf] * w_j[Mi]);
+            }
+          } else {
+            for (i64 p = 0; p < lP; ++p) {
+              const i64 Mi = td + p * lN + (t.i - 1), Mf = td + p * lN + (t.f - 1);
+              T[off + vidx - 1] += t.fac * (w_i[Mf] * w_j[Mi]);
+            }
+          }
+        }
+      for (const PnOp& op : pnops) {
+        const int vidx = lab3[op.nth][5];
+        for (size_t bidx = 0; bidx < bif_idxs.size(); ++bidx) {
+          const int bi = bif_idxs[bidx][0], bf = bif_idxs[bidx][1];
+          const i64 idim = P.B.tdims[bi - 1], fdim = P.B.tdims[bf - 1];
+          const i64 lNi = (i64)P.B.nbits[bi - 1].size(), lNf = (i64)P.B.nbits[bf - 1].size();
+          for (const T0ifc& pj : op.pj[bidx]) {
+            const i64 tMi = idim + (pj.i - 1) * lNi, tMf = fdim + (pj.f - 1) * lNf;
+            for (const T0ifc& nj : op.nj[bidx]) {
+              const i64 Mi = tMi + nj.i - 1, Mf = tMf + nj.f - 1;
+              T[off + vidx - 1] += pj.fac * nj.fac * (w_i[Mf] * w_j[Mi]);
+              T[off + vidx - 1] += pj.fac * nj.fac * (w_i[Mi] * w_j[Mf]);
+            }
+          }
+        }
+      }
+    }
+}
+
 thread_local std::string g_err;
 }  // namespace
 
@@ -1743,5 +2319,69 @@ int orc_trl_sample(void* h, int num_ev, int lm, int ls, double tol, int max_hv, 
 // Dense eigen-solver exposed for tests.
 void orc_sym_eig(int n, const double* A, double* w, double* Z) { sym_eig(n, A, w, Z); }
 double orc_clebsch(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) { return clebsch(tj1, tm1, tj2, tm2, tJ, tM); }
+
+// <vl_a| O |vr_b> for the M1 (op 0) or E2 (op 1) operator: symmetric = 1 is
+// eval_moment's form (prep_obtr_diag / op_obtr_diag, one basis), 0 is
+// transit_main's (prep_obtr_nondiag / op_obtr_nondiag).  The oscillator
+// length follows main_sm / transit_main (hwprm 2 for 16 <= A <= 40).
+int orc_obtr(void* hl, void* hr, int op, int symmetric, const double* gfactors, const double* eff_charge,
+             const double* vl, int nl, const double* vr, int nr, double* out) {
+  try {
+    const Problem& L = *(Problem*)hl;
+    const Problem& R = *(Problem*)hr;
+    double hw, bpar;
+    init_ho_by_mass(L.Anum, (16 <= L.Anum && L.Anum <= 40) ? 2 : 1, hw, bpar);
+    Obtr O;
+    if (symmetric) prep_obtr_diag(L, bpar, gfactors, eff_charge, O);
+    else prep_obtr_nondiag(L, R, bpar, gfactors, eff_charge, O);
+    std::vector<double> twf(L.mdim);
+    for (int b = 0; b < nr; ++b) {
+      std::fill(twf.begin(), twf.end(), 0.0);
+      const double* wf = vr + (size_t)b * R.mdim;
+      if (symmetric) op_obtr_diag(L, O.d[2 * op], O.d[2 * op + 1], wf, twf.data());
+      else op_obtr_nondiag(L, R, O.nd[2 * op], O.nd[2 * op + 1], wf, twf.data());
+      for (int a = 0; a < nl; ++a) out[(size_t)a * nr + b] = dotp(L.mdim, vl + (size_t)a * L.mdim, twf.data());
+    }
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+double orc_wigner3j(int a, int b, int c, int d, int e, int f) { return wigner3j(a, b, c, d, e, f); }
+double orc_wigner6j(int a, int b, int c, int d, int e, int f) { return wigner6j(a, b, c, d, e, f); }
+double orc_radius_power(int k, int n1, int l1, int n2, int l2, double bpar) { return radius_power(k, n1, l1, n2, l2, bpar); }
+
+// prepEC mode "TD" (eigenvector_continuation.jl:212-310): Nmat (Dim x Dim)
+// and, per pair i <= j in idx_from_ij order, the TD vector [OBTD_p, OBTD_n,
+// TBTD per snt line].  ltd() gives its length.
+int orc_ec_td_length(void* h) {
+  const Problem& P = *(Problem*)h;
+  return (int)(P.snt.p_sps.size() + P.snt.n_sps.size()) + P.snt.ntbme;
+}
+int orc_ec_td(void* h, const double* vecs, int nvec, double* nmat, double* td) {
+  try {
+    const Problem& P = *(Problem*)h;
+    const int ltd = orc_ec_td_length(h);
+    std::vector<const double*> wfs(nvec);
+    for (int k = 0; k < nvec; ++k) wfs[k] = vecs + (size_t)k * P.mdim;
+    for (int j = 0; j < nvec; ++j)
+      for (int i = 0; i <= j; ++i) {
+        const double tN = dotp(P.mdim, wfs[i], wfs[j]);
+        nmat[(size_t)i * nvec + j] = tN;
+        nmat[(size_t)j * nvec + i] = tN;
+      }
+    const int npair = nvec * (nvec + 1) / 2;
+    std::vector<std::vector<double>> T(npair, std::vector<double>(ltd, 0.0));
+    calcOBTD(P, wfs, T);
+    calcTBTD(P, wfs, T, (int)(P.snt.p_sps.size() + P.snt.n_sps.size()));
+    for (int p = 0; p < npair; ++p)
+      for (int u = 0; u < ltd; ++u) td[(size_t)p * ltd + u] = T[p][u];
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
 
 }  // extern "C"

@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "smgpu.h")
 
 def declared_symbols():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(smgpu_\w+)\s*\(", txt, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|double|const char\*)\s+(smgpu_\w+)\s*\(", txt, re.M)))
 
 
 def test_library_builds_and_exports_every_declared_symbol():
@@ -93,7 +93,7 @@ def test_main_sm_rejects_unsupported_paths():
     with pytest.raises(ValueError):
         main_sm("x.snt", "Be8", 1, [0, 2])  # one target J only (shellmodel_main.jl:109)
     with pytest.raises(NotImplementedError):
-        main_sm("x.snt", "Be8", 1, [], calc_moment=True)
+        main_sm("x.snt", "Be8", 1, [], calc_entropy=True)
 
 
 def test_synthetic_recipe_counts():
@@ -150,3 +150,19 @@ def test_wav_round_trip_and_layout(tmp_path):
     with pytest.raises(SmgpuError) as ei:
         read_wav(str(tmp_path / "missing.wav"), mdim, 1)
     assert ei.value.code == _lib.ERR_IO
+
+
+def test_wigner_symbols_of_the_library_equal_the_oracle():
+    """smgpu_wigner3j / smgpu_wigner6j (host code) against the oracle's
+    restatement: both square exactly and round once, so they agree bit for
+    bit."""
+    import itertools
+    from smgpu import _lib
+    from oracle.oracle import wigner3j, wigner6j
+    L = _lib.load()
+    for js in itertools.product(range(0, 7), repeat=6):
+        assert L.smgpu_wigner6j(*js) == wigner6j(*js)
+    for a, b, c in itertools.product(range(0, 9), range(0, 5), range(0, 9)):
+        for ma in range(-a, a + 1, 2):
+            for mb in range(-b, b + 1, 2):
+                assert L.smgpu_wigner3j(a, b, c, ma, mb, -ma - mb) == wigner3j(a, b, c, ma, mb, -ma - mb)

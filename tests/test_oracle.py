@@ -162,3 +162,131 @@ def test_jj_two_body_form_matches_ladder_operator(tmp_path, vp, vn):
         a, b = x @ Jop.operate_H(x), ref.jj(x)
         assert abs(a - b) < 1e-8
         assert abs(np.sqrt(1 + 4 * b) - np.round(np.sqrt(1 + 4 * b))) < 1e-6
+
+
+# --------------------------------------------------------------- moments
+def one_orbit_snt(path, n, l, j2, core=(8, 8)):
+    """A model space of one orbit (n, l, j) per species and no two-body
+    interaction: one valence nucleon is a pure single-particle state."""
+    with open(path, "w") as f:
+        f.write(f"! one orbit\n 1 1 {core[0]} {core[1]}\n 1 {n} {l} {j2} -1\n 2 {n} {l} {j2} 1\n 2 0\n"
+                f" 1 1 0.0\n 2 2 0.0\n 0 0 {sum(core) + 2} -0.3\n")
+    return str(path)
+
+
+def schmidt_mu(l, j2, g_l, g_s):
+    """Schmidt value of one nucleon in j = l ± 1/2 (units of mu_N)."""
+    j = j2 / 2
+    if j2 == 2 * l + 1:
+        return g_l * l + g_s / 2
+    return j / (j + 1) * ((j + 1.5) * g_l - g_s / 2)
+
+
+def single_particle_q(n, l, j2, e, A):
+    """Q = -(2j-1)/(2j+2) <r^2> e, <r^2> = b^2 (2n + l + 3/2), b from the
+    mass formula the reference uses for 16 <= A <= 40."""
+    hw = 45.0 * A ** (-1 / 3) - 25.0 * A ** (-2 / 3)
+    b2 = 197.32696 ** 2 / (hw * (938.27231 + 939.56563) / 2)
+    j = j2 / 2
+    return -(2 * j - 1) / (2 * j + 2) * b2 * (2 * n + l + 1.5) * e
+
+
+@pytest.mark.parametrize("orb", [(0, 2, 5), (0, 2, 3), (1, 0, 1)])
+@pytest.mark.parametrize("nuc,species", [("F17", 0), ("O17", 1)])
+def test_moment_operators_give_schmidt_values(tmp_path, orb, nuc, species):
+    """Known answer for the restatement of prep_obtr_diag / op_obtr_diag /
+    eval_moment (transit.jl:82-284,702-765): one nucleon in one orbit has the
+    Schmidt magnetic moment and the single-particle quadrupole moment."""
+    from oracle.oracle import wigner3j
+    import math
+    n, l, j2 = orb
+    snt = one_orbit_snt(tmp_path / "one.snt", n, l, j2)
+    O = OracleProblem(snt, nuc, mtot2=j2)
+    assert O.mdim == 1
+    v = np.ones((1, 1))
+    g = (1.0, 0.0, 5.586, -3.826)
+    ec = (1.5, 0.5)
+    mu = O.obtr(0, v, gfactors=g, effcharge=ec)[0, 0]
+    q = O.obtr(1, v, gfactors=g, effcharge=ec)[0, 0]
+    gm = mu * wigner3j(j2, 2, j2, -j2, 0, j2) / wigner3j(j2, 2, j2, -j2, 0, j2) * math.sqrt(4 * math.pi / 3)
+    assert abs(gm - schmidt_mu(l, j2, g[species], g[2 + species])) < 1e-12
+    if j2 > 1:
+        Q = q * math.sqrt(16 * math.pi / 5)
+        assert abs(Q - single_particle_q(n, l, j2, ec[species], 17)) < 1e-12
+    else:
+        assert abs(q) < 1e-14
+
+
+def test_wigner_symbols_match_sympy():
+    """The oracle's 3j / 6j (WignerSymbols.jl stand-ins) against sympy."""
+    wig = pytest.importorskip("sympy.physics.wigner")
+    from sympy import Rational as R
+    from oracle.oracle import wigner3j, wigner6j
+    import itertools
+    for a, b, c in itertools.product(range(0, 8), range(0, 5), range(0, 8)):
+        for ma in range(-a, a + 1, 2):
+            for mb in range(-b, b + 1, 2):
+                mc = -ma - mb
+                ref = float(wig.wigner_3j(R(a, 2), R(b, 2), R(c, 2), R(ma, 2), R(mb, 2), R(mc, 2)))
+                assert abs(wigner3j(a, b, c, ma, mb, mc) - ref) < 1e-15
+    rng = np.random.default_rng(5)
+    for js in rng.integers(0, 9, size=(3000, 6)):
+        try:
+            ref = float(wig.wigner_6j(*[R(int(j), 2) for j in js]))
+        except ValueError:
+            ref = 0.0
+        assert abs(wigner6j(*js) - ref) < 1e-15
+
+
+def test_radius_power_is_the_oscillator_r2():
+    """radius_power(2, n, l, n, l, b) = b^2 (2n + l + 3/2) (transit.jl:62-80)."""
+    from oracle.oracle import radius_power
+    for n in range(3):
+        for l in range(5):
+            assert abs(radius_power(2, n, l, n, l, 1.7) - 1.7 ** 2 * (2 * n + l + 1.5)) < 1e-12
+
+
+# ------------------------------------------------- eigenvector continuation
+def _snt_parts(path):
+    L = [x.strip() for x in open(path) if x.strip() and not x.strip().startswith(("!", "#"))]
+    lp, ln = map(int, L[0].split()[:2])
+    nsp = int(L[1 + lp + ln].split()[0])
+    hdr = L[2 + lp + ln + nsp].split()
+    nt = int(hdr[0])
+    return L[0], L[1:1 + lp + ln], hdr, L[3 + lp + ln + nsp:3 + lp + ln + nsp + nt], lp, ln
+
+
+def unit_snt(path, u, out):
+    """The interaction whose only non-zero entry is unit u: the SPE of orbit
+    u (u < lp + ln) or TBME line u - lp - ln, set to 1 without mass scaling."""
+    head, orbs, hdr, tb, lp, ln = _snt_parts(path)
+    s = [head] + orbs
+    if u < lp + ln:
+        s += [" 1 0", f" {u + 1} {u + 1} 1.0", f" 0 0 {hdr[2]}"]
+    else:
+        s += [" 0 0", f" 1 0 {hdr[2]}", " ".join(tb[u - lp - ln].split()[:5] + ["1.0"])]
+    with open(out, "w") as f:
+        f.write("\n".join(s) + "\n")
+    return str(out)
+
+
+@pytest.mark.parametrize("snt,nuc,mtot2", [("ckpot.snt", "Be8", 0), ("ckpot.snt", "Li7", 1),
+                                           ("usdb.snt", "Ne20", 0)])
+def test_ec_transition_densities_are_derivatives_of_h(tmp_path, snt, nuc, mtot2):
+    """The restated calcOBTD / prepTBTD / calcTBTD (eigenvector_continuation.jl:
+    1035-1380) equal <w_i|H_u|w_j> with H_u the Hamiltonian of the unit
+    interaction of each orbit SPE and snt line (hermitian partner included):
+    the identity the GPU's transition densities are computed from."""
+    snt = os.path.join(GOLDEN, snt)
+    O = OracleProblem(snt, nuc, mtot2=mtot2)
+    V = np.random.default_rng(3).standard_normal((2, O.mdim))
+    N, td = O.ec_td(V)
+    assert np.allclose(N, V @ V.T, rtol=1e-14, atol=0)
+    _, _, _, tb, lp, ln = _snt_parts(snt)
+    assert td.shape == (3, lp + ln + len(tb))
+    for u in range(td.shape[1]):
+        U = OracleProblem(unit_snt(snt, u, tmp_path / "unit.snt"), nuc, mtot2=mtot2)
+        W = np.array([U.operate_H(v) for v in V])
+        M = V @ W.T
+        got = np.array([M[0, 0], M[0, 1], M[1, 1]])
+        assert np.abs(got - td[:, u]).max() <= 1e-12 * max(1.0, np.abs(td[:, u]).max()), u
