@@ -262,6 +262,7 @@ struct BatchSolve {
     B.jacZ = A.alloc<double>((size_t)np * lm * lm);
     B.evals = A.alloc<double>((size_t)np * lm);
     B.Yf = A.alloc<float>((size_t)np * (lm - 1) * ls);
+    B.wsplit = A.alloc<float>(2 * (size_t)B.LEN);
     B.X = A.alloc<double>((size_t)np * ls * ls);
     B.Xf = A.alloc<float>((size_t)np * (ls * ls + ls));
     B.cvec = A.alloc<double>((size_t)np * ls);

@@ -50,6 +50,7 @@ struct BatchDev {
   double* jacZ;
   double* evals;      // nprob x lm
   float* Yf;          // nprob x (lm-1) x ls
+  float* wsplit;      // 2 x LEN: FP32 (hi, lo) split of w' (first re-orthogonalisation pass)
   double* X;          // nprob x ls x ls
   float* Xf;          // nprob x (ls*ls + ls)
   double* cvec;       // nprob x ls

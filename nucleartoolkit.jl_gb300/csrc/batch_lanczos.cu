@@ -119,38 +119,54 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
   const float* __restrict__ vk = Vb + (int64_t)it0 * B.LEN;
   double* wb = w + P.voff;
   const int m = it0 + 1;
+  // w' = w - α v_k in FP64 once per element, split into an FP32 pair (kept
+  // in wsplit for the later column blocks); the dots accumulate exact FP32
+  // products in double-float on the FP32 pipe.
+  float* __restrict__ wh = B.wsplit + P.voff;
+  float* __restrict__ wl = B.wsplit + B.LEN + P.voff;
   for (int j0 = 0; j0 <= m; j0 += 8) {
-    double acc[8];
+    DFAcc acc[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int q = 0; q < 8; ++q) acc[q].init();
     for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
-      double wv[4];
-      load4(wb + i, wv);
+      float h[4], l[4];
       if (j0 == 0) {
-        double x[4];
+        double wv[4], x[4];
+        load4(wb + i, wv);
         load4(vk + i, x);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
+        for (int u = 0; u < 4; ++u) {
+          wv[u] = fma(-alpha, x[u], wv[u]);
+          df_split(wv[u], h[u], l[u]);
+        }
         store4(wb + i, wv);
+        *reinterpret_cast<float4*>(wh + i) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
+      } else {
+        const float4 a = *reinterpret_cast<const float4*>(wh + i);
+        const float4 b = *reinterpret_cast<const float4*>(wl + i);
+        h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+        l[0] = b.x; l[1] = b.y; l[2] = b.z; l[3] = b.w;
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int j = j0 + q;
         if (j < m) {
-          double x[4];
-          load4(Vb + (int64_t)j * B.LEN + i, x);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+          const float4 x = *reinterpret_cast<const float4*>(Vb + (int64_t)j * B.LEN + i);
+          acc[q].add_prod2(x.x, h[0], l[0]);
+          acc[q].add_prod2(x.y, h[1], l[1]);
+          acc[q].add_prod2(x.z, h[2], l[2]);
+          acc[q].add_prod2(x.w, h[3], l[3]);
         } else if (j == m) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
+          for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
         }
       }
     }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       if (j0 + q > m) break;
-      const double s = block_sum_all<kNT>(acc[q], red);
+      const double s = block_sum_all<kNT>(acc[q].get(), red);
       if (threadIdx.x == 0) B.pdot[(int64_t)(j0 + q) * B.nchunks + c] = s;
     }
   }
@@ -172,19 +188,32 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
   const float* __restrict__ Vb = V + P.voff;
   double* wb = w + P.voff;
   double nrm = 0.0;
+  // Σ_j h_j V_j in double-float (h_j split once per CTA), one FP64
+  // subtraction per element
+  float* hh = reinterpret_cast<float*>(hs + m);
+  float* hl = hh + m;
+  for (int j = threadIdx.x; j < m; j += kNT) df_split(hs[j], hh[j], hl[j]);
+  __syncthreads();
   for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+    DFAcc s4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s4[u].init();
+    for (int j = 0; j < m; ++j) {
+      const float4 x = *reinterpret_cast<const float4*>(Vb + (int64_t)j * B.LEN + i);
+      const float a = hh[j], b = hl[j];
+      s4[0].add_prod2(x.x, a, b);
+      s4[1].add_prod2(x.y, a, b);
+      s4[2].add_prod2(x.z, a, b);
+      s4[3].add_prod2(x.w, a, b);
+    }
     double t[4];
     load4(wb + i, t);
-    for (int j = 0; j < m; ++j) {
-      double x[4];
-      load4(Vb + (int64_t)j * B.LEN + i, x);
-      const double hj = hs[j];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+    for (int u = 0; u < 4; ++u) {
+      t[u] -= s4[u].get();
+      nrm = fma(t[u], t[u], nrm);
     }
     store4(wb + i, t);
-#pragma unroll
-    for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
   }
   const double s = block_sum_all<kNT>(nrm, red);
   if (threadIdx.x == 0) pout[blockIdx.x] = s;
@@ -542,10 +571,7 @@ __global__ void __launch_bounds__(kNT) k_b_ritz(const BatchDev B, const float* _
   }
 }
 
-size_t jacobi_smem(int n) {
-  const int N = n + (n & 1);
-  return sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
-}
+size_t jacobi_smem(int n) { return jacobi_smem_bytes(n); }
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
@@ -575,7 +601,7 @@ void launch_b_sturm(const BatchDev& B, int k, int lock, cudaStream_t st) {
   k_b_sturm<<<B.nprob, threads, shm, st>>>(B, k, lock);
 }
 void launch_b_orth(const BatchDev& B, float* V, double* w, int it0, cudaStream_t st) {
-  const size_t hsh = sizeof(double) * (size_t)(it0 + 1);
+  const size_t hsh = 2 * sizeof(double) * (size_t)(it0 + 1);  // h_j and their FP32 splits
   k_b_orth_dot<<<B.nchunks, kNT, 0, st>>>(B, V, w, it0);
   k_b_orth_axpy<<<B.nchunks, kNT, hsh, st>>>(B, V, w, it0);
   k_b_orth_dot2<<<B.nchunks, kNT, 0, st>>>(B, V, w, it0);

@@ -259,6 +259,7 @@ struct Solve {
     L.jacZ = A.alloc<double>((size_t)lm * lm);
     L.evals = A.alloc<double>(lm);
     L.Yf = A.alloc<float>((size_t)lm * ls);
+    L.wsplit = sizeof(TX) == 4 ? A.alloc<float>(2 * (size_t)L.len) : nullptr;
     L.gram = A.alloc<double>(P_gram);
     L.X = A.alloc<double>((size_t)ls * ls);
     L.cvec = A.alloc<double>(ls);

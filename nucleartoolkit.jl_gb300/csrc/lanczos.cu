@@ -128,7 +128,8 @@ __global__ void __launch_bounds__(kNT) k_scale_store(const double* __restrict__ 
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                   const double* __restrict__ alpha_part, int nalpha,
-                                                  double* __restrict__ pdot, int G, const LanczosFlags* fl) {
+                                                  double* __restrict__ pdot, int G, const LanczosFlags* fl,
+                                                  float* __restrict__ wsplit) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
   const double alpha = sum_partials<kNT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
@@ -136,39 +137,93 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
   const int m = it0 + 1;
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
-  for (int j0 = 0; j0 <= m; j0 += 8) {
-    double acc[8];
+  if constexpr (sizeof(TX) == 4) {
+    // FP32 basis: w' = w - α v_k in FP64 once per element, split into an FP32
+    // pair (kept in wsplit for the later column blocks); the dot products
+    // accumulate exact FP32 products in double-float on the FP32 pipe.
+    float* __restrict__ wh = wsplit;
+    float* __restrict__ wl = wsplit + ld;
+    for (int j0 = 0; j0 <= m; j0 += 8) {
+      DFAcc acc[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-      double wv[4];
-      load4(w + i, wv);
-      if (j0 == 0) {
-        double x[4];
-        load4(vk + i, x);
+      for (int q = 0; q < 8; ++q) acc[q].init();
+      for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+        float h[4], l[4];
+        if (j0 == 0) {
+          double wv[4], x[4];
+          load4(w + i, wv);
+          load4(vk + i, x);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
-        store4(w + i, wv);
+          for (int u = 0; u < 4; ++u) {
+            wv[u] = fma(-alpha, x[u], wv[u]);
+            df_split(wv[u], h[u], l[u]);
+          }
+          store4(w + i, wv);
+          *reinterpret_cast<float4*>(wh + i) = make_float4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
+        } else {
+          const float4 a = *reinterpret_cast<const float4*>(wh + i);
+          const float4 b = *reinterpret_cast<const float4*>(wl + i);
+          h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+          l[0] = b.x; l[1] = b.y; l[2] = b.z; l[3] = b.w;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int j = j0 + q;
+          if (j < m) {
+            const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
+            acc[q].add_prod2(x.x, h[0], l[0]);
+            acc[q].add_prod2(x.y, h[1], l[1]);
+            acc[q].add_prod2(x.z, h[2], l[2]);
+            acc[q].add_prod2(x.w, h[3], l[3]);
+          } else if (j == m) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
+          }
+        }
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        const int j = j0 + q;
-        if (j < m) {
-          double x[4];
-          load4(V + (int64_t)j * ld + i, x);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
-        } else if (j == m) {
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
-        }
+        if (j0 + q > m) break;
+        double s = block_sum_all<kNT>(acc[q].get(), red);
+        if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
       }
     }
+  } else {
+    for (int j0 = 0; j0 <= m; j0 += 8) {
+      double acc[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q > m) break;
-      double s = block_sum_all<kNT>(acc[q], red);
-      if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+      for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+        double wv[4];
+        load4(w + i, wv);
+        if (j0 == 0) {
+          double x[4];
+          load4(vk + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
+          store4(w + i, wv);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int j = j0 + q;
+          if (j < m) {
+            double x[4];
+            load4(V + (int64_t)j * ld + i, x);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+          } else if (j == m) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        if (j0 + q > m) break;
+        double s = block_sum_all<kNT>(acc[q], red);
+        if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+      }
     }
   }
 }
@@ -189,22 +244,54 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
   double nrm = 0.0;
-  for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-    double t[4];
-    load4(w + i, t);
-    for (int j = 0; j < m; ++j) {
-      double x[4];
-      load4(V + (int64_t)j * ld + i, x);
-      const double hj = hs[j];
+  if constexpr (sizeof(TX) == 4) {
+    // FP32 basis: Σ_j h_j V_j in double-float (h_j split once per CTA), one
+    // FP64 subtraction per element.
+    float* hh = reinterpret_cast<float*>(hs + m);
+    float* hl = hh + m;
+    for (int j = threadIdx.x; j < m; j += kNT) df_split(hs[j], hh[j], hl[j]);
+    __syncthreads();
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+      DFAcc s4[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+      for (int u = 0; u < 4; ++u) s4[u].init();
+      for (int j = 0; j < m; ++j) {
+        const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
+        const float a = hh[j], b = hl[j];
+        s4[0].add_prod2(x.x, a, b);
+        s4[1].add_prod2(x.y, a, b);
+        s4[2].add_prod2(x.z, a, b);
+        s4[3].add_prod2(x.w, a, b);
+      }
+      double t[4];
+      load4(w + i, t);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        t[u] -= s4[u].get();
+        nrm = fma(t[u], t[u], nrm);
+      }
+      store4(w + i, t);
     }
-    store4(w + i, t);
+    double s = block_sum_all<kNT>(nrm, red);
+    if (threadIdx.x == 0) pout[blockIdx.x] = s;
+  } else {
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+      double t[4];
+      load4(w + i, t);
+      for (int j = 0; j < m; ++j) {
+        double x[4];
+        load4(V + (int64_t)j * ld + i, x);
+        const double hj = hs[j];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
+        for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+      }
+      store4(w + i, t);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
+    }
+    double s = block_sum_all<kNT>(nrm, red);
+    if (threadIdx.x == 0) pout[blockIdx.x] = s;
   }
-  double s = block_sum_all<kNT>(nrm, red);
-  if (threadIdx.x == 0) pout[blockIdx.x] = s;
 }
 
 template <class TX>
@@ -633,8 +720,8 @@ void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const dou
 template <class TX>
 void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaStream_t st) {
   const int m = it0 + 1;
-  const size_t hsh = sizeof(double) * (size_t)m;
-  k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl);
+  const size_t hsh = 2 * sizeof(double) * (size_t)m;  // h_j and, for an FP32 basis, their FP32 splits
+  k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl, L.wsplit);
   k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, L.fl);
   k_orth_dot2<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.G, L.fl);
   k_orth_axpy2<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.pn2, L.G, L.fl);
@@ -650,8 +737,7 @@ void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
                                    L.fl);
 }
 void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st) {
-  int N = n + (n & 1);
-  size_t shm = sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+  const size_t shm = jacobi_smem_bytes(n);
   k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
 }
 void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
@@ -700,8 +786,7 @@ void launch_combine(const double* Q, int64_t ld, int m, const double* c, double*
   k_combine<<<grid_for(len), kNT, 0, st>>>(Q, ld, m, c, out, len);
 }
 void launch_small_eig(const double* T, int n, double* A, double* Z, double* evals, cudaStream_t st) {
-  const int N = n + (n & 1);
-  const size_t shm = sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+  const size_t shm = jacobi_smem_bytes(n);
   k_small_eig<<<1, 256, shm, st>>>(T, n, A, Z, evals);
 }
 

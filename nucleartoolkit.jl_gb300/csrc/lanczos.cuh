@@ -33,6 +33,7 @@ struct LanczosDev {
   double* jacZ;         // lm x lm
   double* evals;        // lm
   float* Yf;            // (lm-1) x ls: FP32 copy of the restart rotation
+  float* wsplit;        // 2 x len: FP32 (hi, lo) split of w' (FP32 basis only)
   double* gram;         // ls*(ls+1)/2 + ls (restart Gram matrix, packed)
   double* X;            // ls x ls (restart: inverse Cholesky factor)
   double* cvec;         // ls

@@ -237,6 +237,16 @@ __device__ inline void sturm_step(double* __restrict__ T, int lm, int k, int loc
 // (round-robin pairing, n/2 disjoint rotations per round) in one CTA.
 // Output: evals ascending, A = eigenvectors (column-major, ld n).  Dynamic
 // shared memory: see the launchers.
+// Matrices up to this order are rotated in shared memory by jacobi_eig.
+constexpr int kJacobiSmemN = 48;
+// Dynamic shared memory of jacobi_eig for order n.
+__host__ __device__ inline size_t jacobi_smem_bytes(int n) {
+  const int N = n + (n & 1);
+  size_t b = sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
+  if (n <= kJacobiSmemN) b += 2 * sizeof(double) * (size_t)n * n;
+  return b;
+}
+
 template <int NT>
 __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, double* A, double* Z,
                                   double* evals) {
@@ -245,7 +255,11 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
   extern __shared__ double shj[];
   const int N = n + (n & 1);
   const int npair = N / 2;
-  double* cc = shj;
+  // small matrices rotate in shared memory, larger ones in the global A / Z
+  const bool in_smem = n <= kJacobiSmemN;
+  double* A_ = in_smem ? shj : A;
+  double* Z_ = in_smem ? shj + n * n : Z;
+  double* cc = shj + (in_smem ? 2 * n * n : 0);
   double* ss = cc + npair;
   double* dg = ss + npair;
   int* pp = (int*)(dg + N);
@@ -253,18 +267,18 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
   const int tid = threadIdx.x;
   for (int idx = tid; idx < n * n; idx += NT) {
     int i = idx % n, j = idx / n;
-    A[idx] = T[(int64_t)j * ldt + i];
-    Z[idx] = (i == j) ? 1.0 : 0.0;
+    A_[idx] = T[(int64_t)j * ldt + i];
+    Z_[idx] = (i == j) ? 1.0 : 0.0;
   }
   __syncthreads();
   double fro = 0.0;
-  for (int idx = tid; idx < n * n; idx += NT) fro += A[idx] * A[idx];
+  for (int idx = tid; idx < n * n; idx += NT) fro += A_[idx] * A_[idx];
   fro = block_sum_all<NT>(fro, red);
   for (int sweep = 0; sweep < 64; ++sweep) {
     double off = 0.0;
     for (int idx = tid; idx < n * n; idx += NT) {
       int i = idx % n, j = idx / n;
-      if (i < j) off += A[idx] * A[idx];
+      if (i < j) off += A_[idx] * A_[idx];
     }
     off = block_sum_all<NT>(off, red);
     if (tid == 0) s_stop = (off <= 1e-34 * fro || off == 0.0) ? 1 : 0;
@@ -278,9 +292,9 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
         if (p > q) { int x = p; p = q; q = x; }
         double c = 1.0, s = 0.0;
         if (q < n) {
-          double apq = A[(int64_t)q * n + p];
+          double apq = A_[(int64_t)q * n + p];
           if (apq != 0.0) {
-            double app = A[(int64_t)p * n + p], aqq = A[(int64_t)q * n + q];
+            double app = A_[(int64_t)p * n + p], aqq = A_[(int64_t)q * n + q];
             double theta = (aqq - app) / (2.0 * apq);
             double t = (fabs(theta) > 1e150) ? 0.5 / theta
                                               : (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(1.0 + theta * theta));
@@ -296,9 +310,9 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
         if (ss[k] == 0.0) continue;
         int p = pp[k], q = qq[k];
         double c = cc[k], s = ss[k];
-        double aip = A[(int64_t)p * n + i], aiq = A[(int64_t)q * n + i];
-        A[(int64_t)p * n + i] = c * aip - s * aiq;
-        A[(int64_t)q * n + i] = s * aip + c * aiq;
+        double aip = A_[(int64_t)p * n + i], aiq = A_[(int64_t)q * n + i];
+        A_[(int64_t)p * n + i] = c * aip - s * aiq;
+        A_[(int64_t)q * n + i] = s * aip + c * aiq;
       }
       __syncthreads();
       for (int idx = tid; idx < npair * n; idx += NT) {
@@ -306,29 +320,29 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
         if (ss[k] == 0.0) continue;
         int p = pp[k], q = qq[k];
         double c = cc[k], s = ss[k];
-        double apj = A[(int64_t)j * n + p], aqj = A[(int64_t)j * n + q];
-        A[(int64_t)j * n + p] = c * apj - s * aqj;
-        A[(int64_t)j * n + q] = s * apj + c * aqj;
+        double apj = A_[(int64_t)j * n + p], aqj = A_[(int64_t)j * n + q];
+        A_[(int64_t)j * n + p] = c * apj - s * aqj;
+        A_[(int64_t)j * n + q] = s * apj + c * aqj;
       }
       __syncthreads();
       for (int k = tid; k < npair; k += NT)
         if (ss[k] != 0.0) {
-          A[(int64_t)qq[k] * n + pp[k]] = 0.0;
-          A[(int64_t)pp[k] * n + qq[k]] = 0.0;
+          A_[(int64_t)qq[k] * n + pp[k]] = 0.0;
+          A_[(int64_t)pp[k] * n + qq[k]] = 0.0;
         }
       for (int idx = tid; idx < npair * n; idx += NT) {
         int k = idx / n, i = idx % n;
         if (ss[k] == 0.0) continue;
         int p = pp[k], q = qq[k];
         double c = cc[k], s = ss[k];
-        double zip = Z[(int64_t)p * n + i], ziq = Z[(int64_t)q * n + i];
-        Z[(int64_t)p * n + i] = c * zip - s * ziq;
-        Z[(int64_t)q * n + i] = s * zip + c * ziq;
+        double zip = Z_[(int64_t)p * n + i], ziq = Z_[(int64_t)q * n + i];
+        Z_[(int64_t)p * n + i] = c * zip - s * ziq;
+        Z_[(int64_t)q * n + i] = s * zip + c * ziq;
       }
       __syncthreads();
     }
   }
-  for (int i = tid; i < n; i += NT) dg[i] = A[(int64_t)i * n + i];
+  for (int i = tid; i < n; i += NT) dg[i] = A_[(int64_t)i * n + i];
   __syncthreads();
   for (int i = tid; i < n; i += NT) {
     double d = dg[i];
@@ -336,7 +350,7 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
     for (int j = 0; j < n; ++j)
       if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
     evals[rank] = d;
-    for (int r = 0; r < n; ++r) A[(int64_t)rank * n + r] = Z[(int64_t)i * n + r];
+    for (int r = 0; r < n; ++r) A[(int64_t)rank * n + r] = Z_[(int64_t)i * n + r];
   }
 }
 
@@ -355,8 +369,25 @@ struct DFAcc {
     hi = s;
     lo = __fadd_rn(lo, __fadd_rn(err, e));
   }
+  // += a·(bh + bl): a·bh exactly (two-product), a·bl rounded — the product
+  // of an FP32 value with a double-float pair.
+  __device__ __forceinline__ void add_prod2(float a, float bh, float bl) {
+    const float p = __fmul_rn(a, bh);
+    const float e = __fmaf_rn(a, bh, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, __fmaf_rn(a, bl, e)));
+  }
   __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
+
+// x = hi + lo with hi = x rounded to FP32 and lo the FP32 rounding of the rest.
+__device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(x - (double)hi);
+}
 
 __device__ __forceinline__ void gram_pair(int pr, int ls, int& k, int& l) {
   if (pr < ls * (ls + 1) / 2) {

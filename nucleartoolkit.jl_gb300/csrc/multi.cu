@@ -246,6 +246,7 @@ struct MultiSolve {
     M.jacZ = A.alloc<double>((size_t)S * lm * lm);
     M.evals = A.alloc<double>((size_t)S * lm);
     M.Yf = A.alloc<float>((size_t)S * (lm - 1) * ls);
+    M.wsplit = A.alloc<float>(2 * LSz);
     M.gram = A.alloc<double>((size_t)P * S);
     M.X = A.alloc<double>((size_t)S * ls * ls);
     M.Xf = A.alloc<float>((size_t)S * (ls * ls + ls));

@@ -38,6 +38,7 @@ struct MultiDev {
   double* jacZ;        // S x lm x lm
   double* evals;       // S x lm
   float* Yf;           // S x (lm-1) x ls (restart rotation, FP32)
+  float* wsplit;       // 2 x len x S: FP32 (hi, lo) split of w' (first re-orthogonalisation pass)
   double* gram;        // P x S (packed Gram matrices, sample innermost)
   double* X;           // S x ls x ls
   float* Xf;           // S x (ls*ls + ls): X then c, FP32

@@ -189,7 +189,8 @@ __global__ void k_m_sturm(double* T, int lm, int k, int lock, int num_ev, double
 template <int S>
 __global__ void __launch_bounds__(kNT) k_m_dot(const float* __restrict__ V, int64_t len, int it0, double* w,
                                                const double* __restrict__ T, int lm, double* __restrict__ part, int G,
-                                               const LanczosFlags* fl, const MultiCtl* ctl, int first) {
+                                               const LanczosFlags* fl, const MultiCtl* ctl, int first,
+                                               float* __restrict__ wsplit) {
   if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (!first && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
   __shared__ double red[(kNT / 32) * 8 * S];
@@ -204,6 +205,63 @@ __global__ void __launch_bounds__(kNT) k_m_dot(const float* __restrict__ V, int6
   const float* __restrict__ vk = V + (int64_t)it0 * LS;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
+  if (first) {
+    // w' = w - α v_k in FP64 once per element, split into an FP32 pair (kept
+    // in wsplit for the later column blocks); the dots accumulate exact FP32
+    // products in double-float on the FP32 pipe.
+    float* __restrict__ wh = wsplit;
+    float* __restrict__ wl = wsplit + LS;
+    for (int j0 = 0; j0 < mt; j0 += 8) {
+      DFAcc acc[8][4];
+#pragma unroll
+      for (int q8 = 0; q8 < 8; ++q8)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[q8][u].init();
+      for (int64_t i = cb + r; i < ce; i += RPP) {
+        const int64_t e = i * S + s0;
+        float h[4], l[4];
+        if (j0 == 0) {
+          double wv[4], x[4];
+          load4(w + e, wv);
+          load4(vk + e, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            wv[u] = fma(-alpha[u], x[u], wv[u]);
+            df_split(wv[u], h[u], l[u]);
+          }
+          store4(w + e, wv);
+          *reinterpret_cast<float4*>(wh + e) = make_float4(h[0], h[1], h[2], h[3]);
+          *reinterpret_cast<float4*>(wl + e) = make_float4(l[0], l[1], l[2], l[3]);
+        } else {
+          const float4 a = *reinterpret_cast<const float4*>(wh + e);
+          const float4 b = *reinterpret_cast<const float4*>(wl + e);
+          h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
+          l[0] = b.x; l[1] = b.y; l[2] = b.z; l[3] = b.w;
+        }
+#pragma unroll
+        for (int q8 = 0; q8 < 8; ++q8) {
+          const int j = j0 + q8;
+          if (j < m) {
+            const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
+            acc[q8][0].add_prod2(x.x, h[0], l[0]);
+            acc[q8][1].add_prod2(x.y, h[1], l[1]);
+            acc[q8][2].add_prod2(x.z, h[2], l[2]);
+            acc[q8][3].add_prod2(x.w, h[3], l[3]);
+          } else if (j == m) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[q8][u].add_prod2(h[u], h[u], 2.0f * l[u]);
+          }
+        }
+      }
+      double accd[8][4];
+#pragma unroll
+      for (int q8 = 0; q8 < 8; ++q8)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) accd[q8][u] = acc[q8][u].get();
+      reduce_slots<S, 8>(accd, min(8, mt - j0), red, part, j0, G);
+    }
+    return;
+  }
   for (int j0 = 0; j0 < mt; j0 += 8) {
     double acc[8][4];
 #pragma unroll
@@ -245,15 +303,18 @@ template <int S>
 __global__ void __launch_bounds__(kNT) k_m_axpy(const float* __restrict__ V, int64_t len, int m, double* w,
                                                 const double* __restrict__ h, double* __restrict__ part, int G,
                                                 const LanczosFlags* fl, const MultiCtl* ctl,
-                                                const int* __restrict__ sec) {
+                                                const int* __restrict__ sec, int df) {
   if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (sec != nullptr && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
-  extern __shared__ double hs[];  // m*S
+  extern __shared__ double hs[];  // m*S doubles, then (df) m*S FP32 high and m*S FP32 low parts
   __shared__ double red[(kNT / 32) * S];
+  float* hh = reinterpret_cast<float*>(hs + (int64_t)m * S);
+  float* hl = hh + (int64_t)m * S;
   for (int c = threadIdx.x; c < m * S; c += kNT) {
     const int s = c % S;
     const bool use = !lane_stopped(fl, s) && (sec == nullptr || sec[s] != 0);
     hs[c] = use ? h[c] : 0.0;
+    if (df) df_split(hs[c], hh[c], hl[c]);
   }
   __syncthreads();
   const int q = threadIdx.x % Q, r = threadIdx.x / Q, s0 = 4 * q;
@@ -261,6 +322,33 @@ __global__ void __launch_bounds__(kNT) k_m_axpy(const float* __restrict__ V, int
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
   double nrm[1][4] = {{0.0, 0.0, 0.0, 0.0}};
+  if (df) {
+    // Σ_j h_j V_j in double-float on the FP32 pipe, one FP64 subtraction per element
+    for (int64_t i = cb + r; i < ce; i += RPP) {
+      const int64_t e = i * S + s0;
+      DFAcc s4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s4[u].init();
+      for (int j = 0; j < m; ++j) {
+        const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
+        const int c = j * S + s0;
+        s4[0].add_prod2(x.x, hh[c], hl[c]);
+        s4[1].add_prod2(x.y, hh[c + 1], hl[c + 1]);
+        s4[2].add_prod2(x.z, hh[c + 2], hl[c + 2]);
+        s4[3].add_prod2(x.w, hh[c + 3], hl[c + 3]);
+      }
+      double t[4];
+      load4(w + e, t);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        t[u] -= s4[u].get();
+        nrm[0][u] = fma(t[u], t[u], nrm[0][u]);
+      }
+      store4(w + e, t);
+    }
+    reduce_slots<S, 1>(nrm, 1, red, part, 0, G);
+    return;
+  }
   for (int64_t i = cb + r; i < ce; i += RPP) {
     const int64_t e = i * S + s0;
     double t[4];
@@ -566,10 +654,7 @@ __global__ void __launch_bounds__(kNT) k_m_ritz(const float* __restrict__ V, int
   }
 }
 
-size_t jacobi_smem(int n) {
-  const int N = n + (n & 1);
-  return sizeof(double) * (N / 2) * 2 + sizeof(double) * N + sizeof(int) * (N / 2) * 2 + 16;
-}
+size_t jacobi_smem(int n) { return jacobi_smem_bytes(n); }
 
 int gram_tile(int ls, int S) {
   int t = (int)(48 * 1024 / ((size_t)(ls + 1) * S * sizeof(float)));
@@ -622,15 +707,23 @@ static int reduce_grid(int count) { return (count * 32 + kNT - 1) / kNT; }
 
 void launch_m_orth(const MultiDev& M, float* V, double* w, int it0, cudaStream_t st) {
   const int m = it0 + 1, S = M.S, G = M.G;
+  // h_j (FP64) plus, when they fit the default 48 KB, their FP32 splits for
+  // the double-float update
   const size_t hsh = sizeof(double) * (size_t)m * S;
-  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 1)));
+  const int df = 2 * hsh <= 48 * 1024 ? 1 : 0;
+  const size_t hshx = df ? 2 * hsh : hsh;
+  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 1,
+                                                     M.wsplit)));
   k_m_reduce<<<reduce_grid((m + 1) * S), kNT, 0, st>>>(M.part, G, (m + 1) * S, M.h1, M.ctl, 1);
-  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hsh, st>>>(V, M.len, m, w, M.h1, M.part, G, M.fl, M.ctl, nullptr)));
+  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hshx, st>>>(V, M.len, m, w, M.h1, M.part, G, M.fl, M.ctl, nullptr,
+                                                          df)));
   k_m_reduce<<<reduce_grid(S), kNT, 0, st>>>(M.part, G, S, M.nrm1, M.ctl, 1);
   k_m_decide<<<1, 32, 0, st>>>(M.h1, M.nrm1, m, M.sec, M.fl, M.ctl, S);
-  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 0)));
+  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 0,
+                                                     M.wsplit)));
   k_m_reduce<<<reduce_grid(m * S), kNT, 0, st>>>(M.part, G, m * S, M.h2, M.ctl, 2);
-  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hsh, st>>>(V, M.len, m, w, M.h2, M.part, G, M.fl, M.ctl, M.sec)));
+  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hshx, st>>>(V, M.len, m, w, M.h2, M.part, G, M.fl, M.ctl, M.sec,
+                                                          df)));
   k_m_reduce<<<reduce_grid(S), kNT, 0, st>>>(M.part, G, S, M.nrm2, M.ctl, 2);
   k_m_beta<<<1, 32, 0, st>>>(M.T, M.lm, it0, M.nrm1, M.nrm2, M.sec, M.invb, M.fl, M.ctl, S);
   SMGPU_S_DISPATCH(S, (k_m_scale<SS><<<grid_for(M.len * S / 4), kNT, 0, st>>>(
