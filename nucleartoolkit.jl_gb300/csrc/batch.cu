@@ -274,6 +274,7 @@ struct BatchSolve {
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(float) * (size_t)lm * B.LEN, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(U, 0, sizeof(float) * (size_t)ls * B.LEN, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * B.LEN, st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(B.wsplit, 0, sizeof(float) * 2 * B.LEN, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(B.T, 0, sizeof(double) * (size_t)np * lm * lm, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(B.fl, 0, sizeof(LanczosFlags) * np, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(B.ctl, 0, sizeof(BatchCtl), st));
@@ -471,8 +472,10 @@ int smgpu_batch_create_from_snt(const char* const* snt_paths, const char* const*
     smgpu_batch* h = new smgpu_batch();
     try {
       h->nprob = nprob;
+      int prio_lo = 0, prio_hi = 0;
+      SMGPU_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
       SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
-      SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking));
+      SMGPU_CUDA_TRY(cudaStreamCreateWithPriority(&h->st2, cudaStreamNonBlocking, prio_hi));
       int dev = 0;
       SMGPU_CUDA_TRY(cudaGetDevice(&dev));
       SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev));

@@ -267,6 +267,8 @@ struct Solve {
     L.fl = A.alloc<LanczosFlags>(1);
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(TX) * (size_t)lm * L.len, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * L.len, P->st));
+    // the padding slots of the double-float residual are never written by H·v
+    if (L.wsplit) SMGPU_CUDA_TRY(cudaMemsetAsync(L.wsplit, 0, sizeof(float) * 2 * L.len, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(L.T, 0, sizeof(double) * (size_t)lm * lm, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(L.sc, 0, sizeof(LanczosScalars), P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(L.fl, 0, sizeof(LanczosFlags), P->st));
@@ -295,11 +297,20 @@ struct Solve {
       epi.vprev = V + (size_t)(it0 - 1) * L.len;
       epi.beta = L.T + (size_t)(it0 - 1) * L.lm + it0;
     }
-    P->hv(vk, w, epi, s);
+    if constexpr (sizeof(TX) == 4) {
+      // FP32 basis: the residual w stays a double-float pair (wsplit)
+      P->hv_df(vk, L.wsplit, L.wsplit + L.len, epi, s);
+    } else {
+      P->hv(vk, w, epi, s);
+    }
     SMGPU_CUDA_TRY(cudaEventRecord(ev_fork, s));
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
     launch_sturm(L, it, lock, s2);
-    launch_orth_iteration<TX>(L, V, w, it0, s);
+    if constexpr (sizeof(TX) == 4) {
+      launch_orth_iteration_df(L, V, L.wsplit, L.wsplit + L.len, it0, s);
+    } else {
+      launch_orth_iteration<TX>(L, V, w, it0, s);
+    }
   }
 
   void restart(cudaStream_t s) {

@@ -39,6 +39,42 @@ struct DevTables {
   const uint32_t* ppn_meta;  // link<<16 | ia<<1 | sign
 };
 
+// Double-float arithmetic on the FP32 pipe: a value is an unevaluated pair
+// hi + lo of FP32 numbers (about 48 significant bits).  GB300 runs FP64 at a
+// small fraction of the FP32 rate, so the FP32-mixed solver keeps its
+// long vectors of residuals in this form.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (h, l) += x (bh + bl), renormalised; x·bh exact by a fused two-product.
+__device__ __forceinline__ void df_fma(float& h, float& l, float x, float bh, float bl) {
+  const float p = __fmul_rn(x, bh);
+  const float pe = __fmaf_rn(x, bh, -p);
+  float s, e;
+  two_sum(h, p, s, e);
+  const float t = __fadd_rn(__fadd_rn(l, e), __fmaf_rn(x, bl, pe));
+  fast_two_sum(s, t, h, l);
+}
+// (h, l) += (bh + bl), renormalised.
+__device__ __forceinline__ void df_add(float& h, float& l, float bh, float bl) {
+  float s, e;
+  two_sum(h, bh, s, e);
+  const float t = __fadd_rn(__fadd_rn(l, bl), e);
+  fast_two_sum(s, t, h, l);
+}
+// x = hi + lo: hi the FP32 rounding of x, lo that of the remainder.
+__host__ __device__ __forceinline__ void df_from_double(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
 // Row-tile schedule of the H·v kernel.
 struct TileTables {
   const int* task_b;       // block of each CTA
@@ -63,7 +99,8 @@ struct LanczosScalars {
   double nrm;
   double beta;
   double inv_beta;
-  double pad[4];
+  double w_norm2;  // ||w - α v_k||² of the current iteration (second-pass test of the double-float solve)
+  double pad[3];
 };
 struct LanczosFlags {
   int done;       // converged (set by the eigenvalue test)
@@ -157,6 +194,11 @@ void launch_hv_fp64(const DevTables& t, const TileTables& tt, const HvConfig& cf
 void launch_hv_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
                      const double* en, const CoefTables<float>& c, const float* v, double* w,
                      const HvEpilogue<float>& epi, cudaStream_t st);
+// FP32-mixed H·v with the Lanczos epilogue in double-float: w = wh + wl;
+// ep2/en2 the one-body diagonals as (hi, lo) FP32 pairs.
+void launch_hv_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
+                        const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
+                        const HvEpilogue<float>& epi, cudaStream_t st);
 // Multi-sample H·V (hv_multi.cu).  S in {4, 8, 16}; tt1 = one-row tasks
 // (ntasks of them); v/w interleaved; cand = index into hv_multi_candidates().
 struct MultiHvConfig {

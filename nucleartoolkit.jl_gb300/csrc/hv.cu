@@ -35,22 +35,22 @@
 
 namespace smgpu {
 
-template <class TV, class TC, class Acc, int NT, int R, int MINB>
+template <class TV, class TC, class Acc, int NT, int R, int MINB, bool DF>
 __global__ void __launch_bounds__(NT, MINB) hv_tile_kernel(const HvArgs<TV, TC> a) {
   if (a.fl != nullptr && cta_gate(threadIdx.x == 0 && (a.fl->done || a.fl->exhausted))) return;
   const int task = blockIdx.x;
   const double beta = (a.vprev != nullptr) ? *a.beta : 0.0;
-  hv_tile_rows<TV, TC, Acc, NT, R>(a, a.v, a.w, a.vprev, a.tt.task_b[task], a.tt.task_p0[task], beta,
-                                   a.alpha_part != nullptr ? a.alpha_part + task : nullptr);
+  hv_tile_rows<TV, TC, Acc, NT, R, DF>(a, a.v, a.w, a.vprev, a.tt.task_b[task], a.tt.task_p0[task], beta,
+                                       a.alpha_part != nullptr ? a.alpha_part + task : nullptr);
 }
 
 // ---------------------------------------------------------------- dispatch
-template <class TV, class TC, class Acc>
+template <class TV, class TC, class Acc, bool DF>
 static void launch_cfg(const HvConfig& cfg, const HvArgs<TV, TC>& a, cudaStream_t st) {
   const int grid = cfg.ntasks;
 #define SMGPU_HV_CASE(NT_, R_, MB_)                                           \
   if (cfg.nt == NT_ && cfg.rows == R_ && cfg.minb == MB_) {                   \
-    hv_tile_kernel<TV, TC, Acc, NT_, R_, MB_><<<grid, NT_, 0, st>>>(a);       \
+    hv_tile_kernel<TV, TC, Acc, NT_, R_, MB_, DF><<<grid, NT_, 0, st>>>(a);   \
     return;                                                                   \
   }
   SMGPU_HV_CASE(128, 1, 1)
@@ -81,15 +81,25 @@ const HvConfig* hv_candidates(int* count) {
 void launch_hv_fp64(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
                     const double* en, const CoefTables<double>& c, const double* v, double* w,
                     const HvEpilogue<double>& epi, cudaStream_t st) {
-  HvArgs<double, double> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part};
-  launch_cfg<double, double, AccF64>(cfg, a, st);
+  HvArgs<double, double> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
+                           nullptr, nullptr, nullptr, nullptr};
+  launch_cfg<double, double, AccF64, false>(cfg, a, st);
 }
 
 void launch_hv_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
                      const double* en, const CoefTables<float>& c, const float* v, double* w,
                      const HvEpilogue<float>& epi, cudaStream_t st) {
-  HvArgs<float, float> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part};
-  launch_cfg<float, float, AccKahan>(cfg, a, st);
+  HvArgs<float, float> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
+                         nullptr, nullptr, nullptr, nullptr};
+  launch_cfg<float, float, AccKahan, false>(cfg, a, st);
+}
+
+void launch_hv_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
+                        const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
+                        const HvEpilogue<float>& epi, cudaStream_t st) {
+  HvArgs<float, float> a{t, tt, c, nullptr, nullptr, v, nullptr, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
+                         wh, wl, ep2, en2};
+  launch_cfg<float, float, AccKahan, true>(cfg, a, st);
 }
 
 }  // namespace smgpu

@@ -39,6 +39,12 @@ struct HvArgs {
   const TV* vprev;         // three-term correction (may be null)
   const double* beta;      // β of the previous iteration
   double* alpha_part;      // per-CTA partial of v·Hv (may be null)
+  // double-float output (the DF kernels): w = wh + wl, one-body diagonals as
+  // (hi, lo) pairs
+  float* wh;
+  float* wl;
+  const float2* ep2;
+  const float2* en2;
 };
 
 constexpr int KMAX = 16;
@@ -47,7 +53,9 @@ constexpr int KMAX = 16;
 // the tables of `a` (its v/w/vprev fields are not read; the vectors are the
 // explicit arguments).  vprev: three-term correction w -= beta*vprev (null:
 // none); alpha_out: where the CTA's partial of v·Hv goes (null: none).
-template <class TV, class TC, class Acc, int NT, int R>
+// DF = true (FP32 v, Kahan accumulation): the epilogue runs in double-float
+// and writes w as the pair (a.wh, a.wl); the α partial is returned in FP64.
+template <class TV, class TC, class Acc, int NT, int R, bool DF = false>
 __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* __restrict__ v, double* w,
                                              const TV* vprev, const int b, const int p0, const double beta,
                                              double* alpha_out) {
@@ -62,6 +70,9 @@ __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* 
   const int nl = a.tt.link_begin[b + 1] - lb;
   const int64_t rlb = a.tt.rl_base[b] + (int64_t)p0 * (nl + 1);
   double apart = 0.0;
+  float ah = 0.f, al = 0.f;  // DF: α partial
+  float bh = 0.f, bl = 0.f;  // DF: β
+  if constexpr (DF) df_from_double(beta, bh, bl);
 
   for (int n0 = 0; n0 < nn; n0 += NT) {
     const int n = n0 + threadIdx.x;
@@ -167,7 +178,35 @@ __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* 
       }
     }
     // one-body term, Lanczos epilogue, store
-    if (act) {
+    if constexpr (DF) {
+      if (act) {
+        const float2 en2 = a.en2[nst + n];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r >= nr) break;
+          const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
+          const float x = (float)v[o];
+          float hh, hl;
+          fast_two_sum(acc[r].s, -acc[r].c, hh, hl);  // the Kahan pair as a double-float value
+          const float2 ep2 = a.ep2[pst + p0 + r];
+          float dh = ep2.x, dl = ep2.y;
+          df_add(dh, dl, en2.x, en2.y);
+          df_fma(hh, hl, x, dh, dl);
+          // α partial: x·hv
+          {
+            const float p = __fmul_rn(x, hh);
+            const float pe = __fmaf_rn(x, hh, -p);
+            float s, e;
+            two_sum(ah, p, s, e);
+            ah = s;
+            al = __fadd_rn(al, __fadd_rn(e, __fmaf_rn(x, hl, pe)));
+          }
+          if (vprev != nullptr) df_fma(hh, hl, (float)vprev[o], -bh, -bl);
+          a.wh[o] = hh;
+          a.wl[o] = hl;
+        }
+      }
+    } else if (act) {
       const double enn = a.en[nst + n];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -183,8 +222,19 @@ __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* 
   }
   if (alpha_out != nullptr) {
     __shared__ double red[NT / 32];
+    if constexpr (DF) {
+      // warp sums in double-float (FP32 pipe), one FP64 value per warp
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) apart += __shfl_down_sync(0xffffffffu, apart, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, ah, o);
+        const float ol = __shfl_down_sync(0xffffffffu, al, o);
+        df_add(ah, al, oh, ol);
+      }
+      apart = (double)ah + (double)al;
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) apart += __shfl_down_sync(0xffffffffu, apart, o);
+    }
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = apart;
     __syncthreads();
     if (threadIdx.x == 0) {

@@ -128,8 +128,7 @@ __global__ void __launch_bounds__(kNT) k_scale_store(const double* __restrict__ 
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                   const double* __restrict__ alpha_part, int nalpha,
-                                                  double* __restrict__ pdot, int G, const LanczosFlags* fl,
-                                                  float* __restrict__ wsplit) {
+                                                  double* __restrict__ pdot, int G, const LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
   const double alpha = sum_partials<kNT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
@@ -137,93 +136,39 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
   const int m = it0 + 1;
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
-  if constexpr (sizeof(TX) == 4) {
-    // FP32 basis: w' = w - α v_k in FP64 once per element, split into an FP32
-    // pair (kept in wsplit for the later column blocks); the dot products
-    // accumulate exact FP32 products in double-float on the FP32 pipe.
-    float* __restrict__ wh = wsplit;
-    float* __restrict__ wl = wsplit + ld;
-    for (int j0 = 0; j0 <= m; j0 += 8) {
-      DFAcc acc[8];
+  for (int j0 = 0; j0 <= m; j0 += 8) {
+    double acc[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q].init();
-      for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-        float h[4], l[4];
-        if (j0 == 0) {
-          double wv[4], x[4];
-          load4(w + i, wv);
-          load4(vk + i, x);
+    for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+      double wv[4];
+      load4(w + i, wv);
+      if (j0 == 0) {
+        double x[4];
+        load4(vk + i, x);
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            wv[u] = fma(-alpha, x[u], wv[u]);
-            df_split(wv[u], h[u], l[u]);
-          }
-          store4(w + i, wv);
-          *reinterpret_cast<float4*>(wh + i) = make_float4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
-        } else {
-          const float4 a = *reinterpret_cast<const float4*>(wh + i);
-          const float4 b = *reinterpret_cast<const float4*>(wl + i);
-          h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
-          l[0] = b.x; l[1] = b.y; l[2] = b.z; l[3] = b.w;
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int j = j0 + q;
-          if (j < m) {
-            const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
-            acc[q].add_prod2(x.x, h[0], l[0]);
-            acc[q].add_prod2(x.y, h[1], l[1]);
-            acc[q].add_prod2(x.z, h[2], l[2]);
-            acc[q].add_prod2(x.w, h[3], l[3]);
-          } else if (j == m) {
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
-          }
-        }
+        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
+        store4(w + i, wv);
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
-        if (j0 + q > m) break;
-        double s = block_sum_all<kNT>(acc[q].get(), red);
-        if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
+        const int j = j0 + q;
+        if (j < m) {
+          double x[4];
+          load4(V + (int64_t)j * ld + i, x);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
+        } else if (j == m) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
+        }
       }
     }
-  } else {
-    for (int j0 = 0; j0 <= m; j0 += 8) {
-      double acc[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-      for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-        double wv[4];
-        load4(w + i, wv);
-        if (j0 == 0) {
-          double x[4];
-          load4(vk + i, x);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha, x[u], wv[u]);
-          store4(w + i, wv);
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int j = j0 + q;
-          if (j < m) {
-            double x[4];
-            load4(V + (int64_t)j * ld + i, x);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
-          } else if (j == m) {
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q] = fma(wv[u], wv[u], acc[q]);
-          }
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        if (j0 + q > m) break;
-        double s = block_sum_all<kNT>(acc[q], red);
-        if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
-      }
+    for (int q = 0; q < 8; ++q) {
+      if (j0 + q > m) break;
+      double s = block_sum_all<kNT>(acc[q], red);
+      if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
     }
   }
 }
@@ -244,54 +189,22 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
   double nrm = 0.0;
-  if constexpr (sizeof(TX) == 4) {
-    // FP32 basis: Σ_j h_j V_j in double-float (h_j split once per CTA), one
-    // FP64 subtraction per element.
-    float* hh = reinterpret_cast<float*>(hs + m);
-    float* hl = hh + m;
-    for (int j = threadIdx.x; j < m; j += kNT) df_split(hs[j], hh[j], hl[j]);
-    __syncthreads();
-    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-      DFAcc s4[4];
+  for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+    double t[4];
+    load4(w + i, t);
+    for (int j = 0; j < m; ++j) {
+      double x[4];
+      load4(V + (int64_t)j * ld + i, x);
+      const double hj = hs[j];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) s4[u].init();
-      for (int j = 0; j < m; ++j) {
-        const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
-        const float a = hh[j], b = hl[j];
-        s4[0].add_prod2(x.x, a, b);
-        s4[1].add_prod2(x.y, a, b);
-        s4[2].add_prod2(x.z, a, b);
-        s4[3].add_prod2(x.w, a, b);
-      }
-      double t[4];
-      load4(w + i, t);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        t[u] -= s4[u].get();
-        nrm = fma(t[u], t[u], nrm);
-      }
-      store4(w + i, t);
+      for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
     }
-    double s = block_sum_all<kNT>(nrm, red);
-    if (threadIdx.x == 0) pout[blockIdx.x] = s;
-  } else {
-    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
-      double t[4];
-      load4(w + i, t);
-      for (int j = 0; j < m; ++j) {
-        double x[4];
-        load4(V + (int64_t)j * ld + i, x);
-        const double hj = hs[j];
+    store4(w + i, t);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
-      }
-      store4(w + i, t);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
-    }
-    double s = block_sum_all<kNT>(nrm, red);
-    if (threadIdx.x == 0) pout[blockIdx.x] = s;
+    for (int u = 0; u < 4; ++u) nrm = fma(t[u], t[u], nrm);
   }
+  double s = block_sum_all<kNT>(nrm, red);
+  if (threadIdx.x == 0) pout[blockIdx.x] = s;
 }
 
 template <class TX>
@@ -387,6 +300,219 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
   for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT)
     vnext[i] = (TX)(w[i] * inv);
 }
+
+// ---------------------------------------- FP32 basis, double-float residual
+// The FP32-mixed solve keeps w = wh + wl as a double-float pair: every
+// vector-length operation below runs on the FP32 pipe (exact FP32 products
+// by fused two-products, sums in double-float); only per-CTA scalars are FP64.
+// 512-thread CTAs, two per SM: the streams need the memory-level parallelism.
+constexpr int kONT = 512;
+
+// α (from the H·v partials), w' = w − α v_k, partials of v_j·w' (j <= it0)
+// and of ||w'||² (slot it0+1).
+__global__ void __launch_bounds__(kONT, 2) k_orth_dot_df(const float* __restrict__ V, int64_t ld, int it0,
+                                                         float* __restrict__ wh, float* __restrict__ wl,
+                                                         const double* __restrict__ alpha_part, int nalpha,
+                                                         double* __restrict__ pdot, int G, const LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  __shared__ double red[kONT / 32];
+  __shared__ double red8[(kONT / 32) * 8];
+  const double alpha = sum_partials<kONT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
+  float aH, aL;
+  df_from_double(-alpha, aH, aL);
+  const float* __restrict__ vk = V + (int64_t)it0 * ld;
+  const int m = it0 + 1;
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  for (int j0 = 0; j0 <= m; j0 += 8) {
+    DFAcc acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q].init();
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kONT) {
+      const float4 a = *reinterpret_cast<const float4*>(wh + i);
+      const float4 b = *reinterpret_cast<const float4*>(wl + i);
+      float h[4] = {a.x, a.y, a.z, a.w}, l[4] = {b.x, b.y, b.z, b.w};
+      if (j0 == 0) {
+        const float4 x = *reinterpret_cast<const float4*>(vk + i);
+        df_fma(h[0], l[0], x.x, aH, aL);
+        df_fma(h[1], l[1], x.y, aH, aL);
+        df_fma(h[2], l[2], x.z, aH, aL);
+        df_fma(h[3], l[3], x.w, aH, aL);
+        *reinterpret_cast<float4*>(wh + i) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int j = j0 + q;
+        if (j < m) {
+          const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
+          acc[q].add_prod2(x.x, h[0], l[0]);
+          acc[q].add_prod2(x.y, h[1], l[1]);
+          acc[q].add_prod2(x.z, h[2], l[2]);
+          acc[q].add_prod2(x.w, h[3], l[3]);
+        } else if (j == m) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
+        }
+      }
+    }
+    double s;
+    block_sum_df<kONT, 8>(acc, red8, s);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m) pdot[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
+  }
+}
+
+// w -= Σ_j h_j V_j (h_j = Σ_g ph[j*G+g], split once per CTA); pout[cta] = ||w chunk||².
+__device__ __forceinline__ void orth_subtract_df(const float* __restrict__ V, int64_t ld, int m,
+                                                 float* __restrict__ wh, float* __restrict__ wl,
+                                                 const double* __restrict__ ph, double* __restrict__ pout, int G,
+                                                 double* hs, double* red) {
+  sum_partials_many<kONT>(ph, G, m, hs);
+  float* hh = reinterpret_cast<float*>(hs + m + 2);
+  float* hl = hh + m;
+  for (int j = threadIdx.x; j < m; j += kONT) df_from_double(hs[j], hh[j], hl[j]);
+  __syncthreads();
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  DFAcc nrm;
+  nrm.init();
+  for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kONT) {
+    DFAcc s4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s4[u].init();
+    for (int j = 0; j < m; ++j) {
+      const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
+      const float a = hh[j], b = hl[j];
+      s4[0].add_prod2(x.x, a, b);
+      s4[1].add_prod2(x.y, a, b);
+      s4[2].add_prod2(x.z, a, b);
+      s4[3].add_prod2(x.w, a, b);
+    }
+    const float4 a = *reinterpret_cast<const float4*>(wh + i);
+    const float4 b = *reinterpret_cast<const float4*>(wl + i);
+    float h[4] = {a.x, a.y, a.z, a.w}, l[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      df_add(h[u], l[u], -s4[u].hi, -s4[u].lo);
+      nrm.add_prod2(h[u], h[u], 2.0f * l[u]);
+    }
+    *reinterpret_cast<float4*>(wh + i) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  DFAcc n1[1] = {nrm};
+  double s;
+  block_sum_df<kONT, 1>(n1, red, s);
+  if (threadIdx.x == 0) pout[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kONT, 2) k_orth_axpy_df(const float* __restrict__ V, int64_t ld, int it0, float* wh,
+                                                      float* wl, const double* __restrict__ pdot,
+                                                      double* __restrict__ pn1, int G, LanczosScalars* sc,
+                                                      const LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  extern __shared__ double hs[];
+  __shared__ double red[kONT / 32];
+  const int m = it0 + 1;
+  if (blockIdx.x == 0) {
+    // ||w − α v_k||² (slot m of the first-pass partials), for the second-pass test
+    const double n0 = sum_partials<kONT>(pdot + (int64_t)m * G, G, red);
+    if (threadIdx.x == 0) sc->w_norm2 = n0;
+  }
+  orth_subtract_df(V, ld, m, wh, wl, pdot, pn1, G, hs, red);
+}
+
+// Second-pass decision of the double-float solve: ||w''||² < ||w'||² / 2.
+__device__ __forceinline__ bool need_second_df(const LanczosScalars* sc, const double* pn1, int G, double* red) {
+  const double n1 = sum_partials<kONT>(pn1, G, red);
+  return n1 < 0.5 * sc->w_norm2;
+}
+
+__global__ void __launch_bounds__(kONT, 2) k_orth_dot2_df(const float* __restrict__ V, int64_t ld, int it0,
+                                                      const float* __restrict__ wh, const float* __restrict__ wl,
+                                                      const LanczosScalars* sc,
+                                                      const double* __restrict__ pn1, double* __restrict__ pdot2,
+                                                      int G, const LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  __shared__ double red[kONT / 32];
+  const int m = it0 + 1;
+  if (!need_second_df(sc, pn1, G, red)) return;
+  __shared__ double red8[(kONT / 32) * 8];
+  int64_t cb, ce;
+  chunk_of(ld, G, cb, ce);
+  for (int j0 = 0; j0 < m; j0 += 8) {
+    DFAcc acc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) acc[q].init();
+    for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kONT) {
+      const float4 a = *reinterpret_cast<const float4*>(wh + i);
+      const float4 b = *reinterpret_cast<const float4*>(wl + i);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (j0 + q < m) {
+          const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)(j0 + q) * ld + i);
+          acc[q].add_prod2(x.x, a.x, b.x);
+          acc[q].add_prod2(x.y, a.y, b.y);
+          acc[q].add_prod2(x.z, a.z, b.z);
+          acc[q].add_prod2(x.w, a.w, b.w);
+        }
+    }
+    double s;
+    block_sum_df<kONT, 8>(acc, red8, s);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m) pdot2[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kONT, 2) k_orth_axpy2_df(const float* __restrict__ V, int64_t ld, int it0, float* wh,
+                                                       float* wl, const LanczosScalars* sc,
+                                                       const double* __restrict__ pn1,
+                                                       const double* __restrict__ pdot2, double* __restrict__ pn2,
+                                                       int G, const LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  extern __shared__ double hs[];
+  __shared__ double red[kONT / 32];
+  const int m = it0 + 1;
+  if (!need_second_df(sc, pn1, G, red)) return;
+  orth_subtract_df(V, ld, m, wh, wl, pdot2, pn2, G, hs, red);
+}
+
+// β = ||w||, T entries, v_{it0+1} = w/β rounded to FP32 (as k_orth_scale).
+__global__ void __launch_bounds__(kONT, 2) k_orth_scale_df(const float* __restrict__ wh, const float* __restrict__ wl,
+                                                       float* __restrict__ vnext, const double* __restrict__ pn1,
+                                                       const double* __restrict__ pn2, int G, int it0, double* T,
+                                                       int lm, int64_t len, LanczosScalars* sc, LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  __shared__ double red[kONT / 32];
+  const bool second = need_second_df(sc, pn1, G, red);
+  const double nrm = sum_partials<kONT>(second ? pn2 : pn1, G, red);
+  const double beta = sqrt(nrm);
+  const bool ok = (beta > 0.0) && (beta < INFINITY);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (ok) {
+      T[(int64_t)it0 * lm + it0 + 1] = beta;
+      T[(int64_t)(it0 + 1) * lm + it0] = beta;
+      sc->beta = beta;
+      sc->inv_beta = 1.0 / beta;
+      fl->second = second ? 1 : 0;
+      if (second) fl->n_second += 1;
+    } else {
+      fl->exh_k = it0 + 1;
+      fl->exhausted = 1;
+    }
+  }
+  if (!ok) return;
+  float ih, il;
+  df_from_double(1.0 / beta, ih, il);
+  for (int64_t i = 4 * (blockIdx.x * (int64_t)kONT + threadIdx.x); i < len; i += 4 * (int64_t)gridDim.x * kONT) {
+    const float4 h = *reinterpret_cast<const float4*>(wh + i);
+    const float4 l = *reinterpret_cast<const float4*>(wl + i);
+    *reinterpret_cast<float4*>(vnext + i) =
+        make_float4(__fmaf_rn(h.x, ih, __fmaf_rn(l.x, ih, __fmul_rn(h.x, il))),
+                    __fmaf_rn(h.y, ih, __fmaf_rn(l.y, ih, __fmul_rn(h.y, il))),
+                    __fmaf_rn(h.z, ih, __fmaf_rn(l.z, ih, __fmul_rn(h.z, il))),
+                    __fmaf_rn(h.w, ih, __fmaf_rn(l.w, ih, __fmul_rn(h.w, il))));
+  }
+}
+
 
 // Lowest eigenvalues (diagonalize_T!, lanczos_methods.jl:250-258): α from the
 // H·v epilogue partials, then sturm_step.
@@ -720,13 +846,26 @@ void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const dou
 template <class TX>
 void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaStream_t st) {
   const int m = it0 + 1;
-  const size_t hsh = 2 * sizeof(double) * (size_t)m;  // h_j and, for an FP32 basis, their FP32 splits
-  k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl, L.wsplit);
+  const size_t hsh = sizeof(double) * (size_t)m;
+  k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl);
   k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, L.fl);
   k_orth_dot2<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.G, L.fl);
   k_orth_axpy2<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.pn2, L.G, L.fl);
   k_orth_scale<TX><<<L.G, kNT, 0, st>>>(w, V + (int64_t)(it0 + 1) * L.len, L.pdot, L.pn1, L.pn2, L.G, it0, L.T,
                                         L.lm, L.len, L.sc, L.fl);
+}
+void launch_orth_iteration_df(const LanczosDev& L, float* V, float* wh, float* wl, int it0, cudaStream_t st) {
+  const int m = it0 + 1;
+  const size_t hsh = sizeof(double) * (size_t)(m + 2) + 2 * sizeof(float) * (size_t)m;  // h_j, their FP32 splits
+  // one wave of two CTAs per SM, less one SM: the eigenvalue test running
+  // beside them finds room without delaying a CTA to a second wave
+  const int G = L.G > 4 ? L.G - 2 : L.G;
+  k_orth_dot_df<<<G, kONT, 0, st>>>(V, L.len, it0, wh, wl, L.alpha_part, L.nalpha, L.pdot, G, L.fl);
+  k_orth_axpy_df<<<G, kONT, hsh, st>>>(V, L.len, it0, wh, wl, L.pdot, L.pn1, G, L.sc, L.fl);
+  k_orth_dot2_df<<<G, kONT, 0, st>>>(V, L.len, it0, wh, wl, L.sc, L.pn1, L.pdot2, G, L.fl);
+  k_orth_axpy2_df<<<G, kONT, hsh, st>>>(V, L.len, it0, wh, wl, L.sc, L.pn1, L.pdot2, L.pn2, G, L.fl);
+  k_orth_scale_df<<<G, kONT, 0, st>>>(wh, wl, V + (int64_t)(it0 + 1) * L.len, L.pn1, L.pn2, G, it0, L.T, L.lm,
+                                      L.len, L.sc, L.fl);
 }
 void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
   int threads = ((L.num_ev * kLPE + 31) / 32) * 32;

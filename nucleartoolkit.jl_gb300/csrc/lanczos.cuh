@@ -33,7 +33,7 @@ struct LanczosDev {
   double* jacZ;         // lm x lm
   double* evals;        // lm
   float* Yf;            // (lm-1) x ls: FP32 copy of the restart rotation
-  float* wsplit;        // 2 x len: FP32 (hi, lo) split of w' (FP32 basis only)
+  float* wsplit;        // 2 x len: the residual w = hi + lo in double-float (FP32 basis only)
   double* gram;         // ls*(ls+1)/2 + ls (restart Gram matrix, packed)
   double* X;            // ls x ls (restart: inverse Cholesky factor)
   double* cvec;         // ls
@@ -53,6 +53,8 @@ void launch_scale_store(const LanczosDev& L, const double* w, TX* out, const dou
 // w' = w - alpha v_it0, first CGS pass, conditional second pass, beta and v_{it0+1}.
 template <class TX>
 void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaStream_t st);
+// The same for an FP32 basis with the residual kept in double-float, w = wh + wl.
+void launch_orth_iteration_df(const LanczosDev& L, float* V, float* wh, float* wl, int it0, cudaStream_t st);
 void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st);
 void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st);
 void launch_restart_small(const LanczosDev& L, cudaStream_t st);

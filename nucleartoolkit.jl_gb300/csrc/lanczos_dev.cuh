@@ -383,6 +383,36 @@ struct DFAcc {
   __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
 
+// Sums of NQ double-float accumulators over a CTA: warp shuffles in
+// double-float on the FP32 pipe, one FP64 sum of the warp totals per value
+// (GB300 runs FP64 adds at a small fraction of the FP32 rate).  Thread q < NQ
+// gets value q in *out; red holds (NT/32)*NQ doubles.
+template <int NT, int NQ>
+__device__ __forceinline__ void block_sum_df(DFAcc (&acc)[NQ], double* red, double& out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    float h = acc[q].hi, l = acc[q].lo;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+      df_add(h, l, oh, ol);
+    }
+    acc[q].hi = h;
+    acc[q].lo = l;
+  }
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) red[wid * NQ + q] = (double)acc[q].hi + (double)acc[q].lo;
+  }
+  __syncthreads();
+  out = 0.0;
+  if (threadIdx.x < NQ)
+    for (int k = 0; k < NT / 32; ++k) out += red[k * NQ + threadIdx.x];
+}
+
 // x = hi + lo with hi = x rounded to FP32 and lo the FP32 rounding of the rest.
 __device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
   hi = __double2float_rn(x);

@@ -258,6 +258,7 @@ struct MultiSolve {
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(float) * (size_t)lm * LSz, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(U, 0, sizeof(float) * (size_t)ls * LSz, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * LSz, st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(M.wsplit, 0, sizeof(float) * 2 * LSz, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(M.T, 0, sizeof(double) * (size_t)S * lm * lm, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(M.sec, 0, sizeof(int) * S, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(hv_count, 0, sizeof(int), st));

@@ -39,6 +39,16 @@ struct DeviceArena {
   }
 };
 
+// (hi, lo) FP32 pairs with hi + lo = x to about 48 bits.
+inline std::vector<float2> to_df(const std::vector<double>& v) {
+  std::vector<float2> r(v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    const float hi = (float)v[i];
+    r[i] = make_float2(hi, (float)(v[i] - (double)hi));
+  }
+  return r;
+}
+
 template <class T>
 std::vector<float> to_f32(const std::vector<T>& v) {
   std::vector<float> r(v.size());
@@ -75,6 +85,8 @@ struct smgpu_problem {
   CoefTables<float> c32{};
   const double* d_ep = nullptr;
   const double* d_en = nullptr;
+  const float2* d_ep2 = nullptr;  // one-body diagonals as double-float pairs (FP32-mixed solve)
+  const float2* d_en2 = nullptr;
   HvConfig cfg{128, 4, 0, 1};
   std::map<int, std::pair<const int*, const int*>> task_arrays;  // rows -> (task_b, task_p0)
   std::map<int, int> task_count;
@@ -127,8 +139,12 @@ struct smgpu_problem {
   // on a batch's streams.
   void upload(bool with_streams = true) {
     if (with_streams) {
+      // the eigenvalue test runs beside the main chain on st2: highest
+      // priority, so its single CTA is scheduled as soon as an SM frees
+      int prio_lo = 0, prio_hi = 0;
+      SMGPU_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
       SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-      SMGPU_CUDA_TRY(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+      SMGPU_CUDA_TRY(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, prio_hi));
     }
     int dev = 0;
     SMGPU_CUDA_TRY(cudaGetDevice(&dev));
@@ -202,6 +218,8 @@ struct smgpu_problem {
       c32.pp_val = tables.upload(to_f32(T.pp_val));
       c32.nn_val = tables.upload(to_f32(T.nn_val));
       c32.vtab = tables.upload(to_f32(vt2));
+      d_ep2 = tables.upload(to_df(T.ep));
+      d_en2 = tables.upload(to_df(T.en));
     }
     set_config(128, 4, 1);
     // the synchronous uploads run on the legacy stream; the handle's streams
@@ -223,6 +241,10 @@ struct smgpu_problem {
   }
   void hv(const float* v, double* w, const HvEpilogue<float>& epi, cudaStream_t s) {
     launch_hv_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
+  }
+  // FP32-mixed H·v with the Lanczos epilogue in double-float (w = wh + wl)
+  void hv_df(const float* v, float* wh, float* wl, const HvEpilogue<float>& epi, cudaStream_t s) {
+    launch_hv_mixed_df(dt, tt, cfg, d_ep2, d_en2, c32, v, wh, wl, epi, s);
   }
 
   // Time every candidate launch shape on a device vector and keep the fastest
