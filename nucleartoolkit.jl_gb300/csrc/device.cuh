@@ -130,6 +130,8 @@ struct MultiCoef {
   const float* vtab;
   const double* ep;
   const double* en;
+  const float2* ep2;  // the one-body diagonals as double-float pairs, same layout
+  const float2* en2;
 };
 
 struct MultiEpilogue {
@@ -139,6 +141,9 @@ struct MultiEpilogue {
   int beta_stride;
   double* alpha_part;       // [s * ntasks + task] partial sums of v_s·(Hv)_s (null: none)
   int* count;               // incremented once per executed launch (null: none)
+  float* wh;                // non-null: w written as the double-float pair (wh, wl) instead of FP64
+  float* wl;
+  const float2* beta2;      // double-float form: beta_s as (hi, lo) at [s]
 };
 
 #ifdef __CUDACC__

@@ -56,7 +56,7 @@ __device__ __forceinline__ void ld4(const float* __restrict__ p, float (&o)[4]) 
   o[3] = f.w;
 }
 
-template <int S, int NT, int MINB, int KM>
+template <int S, int NT, int MINB, int KM, bool DF>
 __global__ void __launch_bounds__(NT, MINB) hv_multi_kernel(const MultiHvArgs<S> a) {
   if (a.epi.all_done != nullptr && cta_gate(threadIdx.x == 0 && *a.epi.all_done)) return;
   if (a.epi.count != nullptr && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.epi.count, 1);
@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(NT, MINB) hv_multi_kernel(const MultiHvArgs<S>
   const int s0 = 4 * q;
   const float* __restrict__ v = a.v + s0;
   double apart[4] = {0.0, 0.0, 0.0, 0.0};
+  float aH[4] = {0.f, 0.f, 0.f, 0.f}, aL[4] = {0.f, 0.f, 0.f, 0.f};  // DF: α partials
 
   for (int n0 = 0; n0 < nn; n0 += CP) {
     const int n = n0 + (int)(threadIdx.x / Q);
@@ -158,7 +159,37 @@ __global__ void __launch_bounds__(NT, MINB) hv_multi_kernel(const MultiHvArgs<S>
 #pragma unroll
       for (int u = 0; u < 4; ++u) acc[u].add(part[u]);
     }
-    if (act) {
+    if (DF && act) {
+      // epilogue in double-float on the FP32 pipe: w = wh + wl
+      const int64_t o = (rowoff + n) * S;
+      const int gn = nst + n;
+      ld4(v + o, x);
+      float xp[4] = {0.f, 0.f, 0.f, 0.f};
+      if (a.epi.vprev != nullptr) ld4(a.epi.vprev + s0 + o, xp);
+      float hh[4], hl[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        fast_two_sum(acc[u].s, -acc[u].c, hh[u], hl[u]);
+        const float2 ep = a.c.ep2[(int64_t)g * S + s0 + u], en = a.c.en2[(int64_t)gn * S + s0 + u];
+        float dh = ep.x, dl = ep.y;
+        df_add(dh, dl, en.x, en.y);
+        df_fma(hh[u], hl[u], x[u], dh, dl);
+        {  // α partial x·hv in double-float
+          const float pp = __fmul_rn(x[u], hh[u]);
+          const float pe = __fmaf_rn(x[u], hh[u], -pp);
+          float t, e;
+          two_sum(aH[u], pp, t, e);
+          aH[u] = t;
+          aL[u] = __fadd_rn(aL[u], __fadd_rn(e, __fmaf_rn(x[u], hl[u], pe)));
+        }
+        if (a.epi.vprev != nullptr) {
+          const float2 b = a.epi.beta2[s0 + u];
+          df_fma(hh[u], hl[u], xp[u], -b.x, -b.y);
+        }
+      }
+      *reinterpret_cast<float4*>(a.epi.wh + o + s0) = make_float4(hh[0], hh[1], hh[2], hh[3]);
+      *reinterpret_cast<float4*>(a.epi.wl + o + s0) = make_float4(hl[0], hl[1], hl[2], hl[3]);
+    } else if (!DF && act) {
       const int64_t o = (rowoff + n) * S;
       const int gn = nst + n;
       ld4(v + o, x);
@@ -177,6 +208,10 @@ __global__ void __launch_bounds__(NT, MINB) hv_multi_kernel(const MultiHvArgs<S>
       *reinterpret_cast<double2*>(wo) = make_double2(hv[0], hv[1]);
       *reinterpret_cast<double2*>(wo + 2) = make_double2(hv[2], hv[3]);
     }
+  }
+  if constexpr (DF) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) apart[u] = (double)aH[u] + (double)aL[u];
   }
   if (a.epi.alpha_part != nullptr) {
     // sum over the threads of each sample group, fixed order
@@ -213,7 +248,8 @@ template <int S, int NT, int MINB, int KM>
 static void launch_one(const DevTables& t, const TileTables& tt1, int ntasks, const MultiCoef& c, const float* v,
                        double* w, const MultiEpilogue& epi, cudaStream_t st) {
   const MultiHvArgs<S> a{t, tt1, c, v, w, epi};
-  hv_multi_kernel<S, NT, MINB, KM><<<ntasks, NT, 0, st>>>(a);
+  if (epi.wh != nullptr) hv_multi_kernel<S, NT, MINB, KM, true><<<ntasks, NT, 0, st>>>(a);
+  else hv_multi_kernel<S, NT, MINB, KM, false><<<ntasks, NT, 0, st>>>(a);
 }
 
 template <int S>

@@ -247,6 +247,7 @@ struct MultiSolve {
     M.evals = A.alloc<double>((size_t)S * lm);
     M.Yf = A.alloc<float>((size_t)S * (lm - 1) * ls);
     M.wsplit = A.alloc<float>(2 * LSz);
+    M.beta2 = A.alloc<float2>(S);
     M.gram = A.alloc<double>((size_t)P * S);
     M.X = A.alloc<double>((size_t)S * ls * ls);
     M.Xf = A.alloc<float>((size_t)S * (ls * ls + ls));
@@ -259,6 +260,7 @@ struct MultiSolve {
     SMGPU_CUDA_TRY(cudaMemsetAsync(U, 0, sizeof(float) * (size_t)ls * LSz, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * LSz, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(M.wsplit, 0, sizeof(float) * 2 * LSz, st));
+    SMGPU_CUDA_TRY(cudaMemsetAsync(M.beta2, 0, sizeof(float2) * S, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(M.T, 0, sizeof(double) * (size_t)S * lm * lm, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(M.sec, 0, sizeof(int) * S, st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(hv_count, 0, sizeof(int), st));
@@ -288,12 +290,16 @@ struct MultiSolve {
       epi.beta_base = M.T + (size_t)(it0 - 1) * M.lm + it0;
       epi.beta_stride = M.lm * M.lm;
     }
-    H->hv(V + (size_t)it0 * LS(), w, epi, s);
+    // the residual of the iterations is a double-float pair (wsplit)
+    epi.wh = M.wsplit;
+    epi.wl = M.wsplit + LS();
+    epi.beta2 = M.beta2;
+    H->hv(V + (size_t)it0 * LS(), nullptr, epi, s);
     launch_m_alpha(M, it0, s);
     SMGPU_CUDA_TRY(cudaEventRecord(ev_fork, s));
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
     launch_m_sturm(M, it, lock, s2);
-    launch_m_orth(M, V, w, it0, s);
+    launch_m_orth(M, V, M.wsplit, M.wsplit + LS(), it0, s);
   }
 
   cudaGraphExec_t capture_cycle(int kstart, int lock, long long* nkernels) {
@@ -511,6 +517,8 @@ int smgpu_multi_create_from_snt(const char* const* snt_paths, int nsamples, cons
       h->mc.vtab = h->coef.upload(interleave<float>(vt, S));
       h->mc.ep = h->coef.upload(interleave<double>(ep, S));
       h->mc.en = h->coef.upload(interleave<double>(en, S));
+      h->mc.ep2 = h->coef.upload(to_df(interleave<double>(ep, S)));
+      h->mc.en2 = h->coef.upload(to_df(interleave<double>(en, S)));
       h->autotune();
       SMGPU_CUDA_TRY(cudaStreamSynchronize(B.st));
       h->times[0] = now_s() - t0;

@@ -38,7 +38,8 @@ struct MultiDev {
   double* jacZ;        // S x lm x lm
   double* evals;       // S x lm
   float* Yf;           // S x (lm-1) x ls (restart rotation, FP32)
-  float* wsplit;       // 2 x len x S: FP32 (hi, lo) split of w' (first re-orthogonalisation pass)
+  float* wsplit;       // 2 x len x S: the residual w = hi + lo in double-float (the iterations' w)
+  float2* beta2;       // S: β of each sample as a double-float pair (H·V epilogue)
   double* gram;        // P x S (packed Gram matrices, sample innermost)
   double* X;           // S x ls x ls
   float* Xf;           // S x (ls*ls + ls): X then c, FP32
@@ -56,7 +57,7 @@ void launch_m_init(const MultiDev& M, const double* w, float* V0, cudaStream_t s
 void launch_m_alpha(const MultiDev& M, int it0, cudaStream_t st);
 void launch_m_sturm(const MultiDev& M, int k, int lock, cudaStream_t st);
 // orthogonalisation, β and v_{it0+1} after the H·V and α of iteration it0
-void launch_m_orth(const MultiDev& M, float* V, double* w, int it0, cudaStream_t st);
+void launch_m_orth(const MultiDev& M, float* V, float* wh, float* wl, int it0, cudaStream_t st);
 void launch_m_cycle_end(const MultiDev& M, cudaStream_t st);
 void launch_m_restart(const MultiDev& M, float* V, float* U, cudaStream_t st);
 // Ritz vectors of sample s: R (nev x len, FP64, padded) from jacA of that sample

@@ -70,6 +70,43 @@ __device__ __forceinline__ void reduce_slots(double (&acc)[NQ][4], int nq, doubl
   }
 }
 
+// reduce_slots for double-float accumulators: shuffles in double-float on the
+// FP32 pipe, FP64 only for the per-warp totals.
+template <int S, int NQ>
+__device__ __forceinline__ void reduce_slots_df(DFAcc (&acc)[NQ][4], int nq, double* red, double* __restrict__ part,
+                                                int slot0, int G) {
+  constexpr int Q = S / 4;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float h = acc[q][u].hi, l = acc[q][u].lo;
+#pragma unroll
+      for (int o = Q; o < 32; o <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+        df_add(h, l, oh, ol);
+      }
+      acc[q][u].hi = h;
+      acc[q][u].lo = l;
+    }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane < Q) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) red[(wid * NQ + q) * S + 4 * lane + u] = acc[q][u].get();
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nq * S; c += kNT) {
+    const int q = c / S, s = c % S;
+    double x = 0.0;
+    for (int w = 0; w < kNT / 32; ++w) x += red[(w * NQ + q) * S + s];
+    part[((int64_t)(slot0 + q) * S + s) * G + blockIdx.x] = x;
+  }
+}
+
 // ------------------------------------------------------------------ vectors
 __global__ void k_m_start(DevTables t, int S, uint64_t seed, double* __restrict__ w) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < t.len_pad;
@@ -184,186 +221,123 @@ __global__ void k_m_sturm(double* T, int lm, int k, int lock, int num_ev, double
   if (threadIdx.x == 0 && f->done) lane_finished(ctl, S);
 }
 
-// first = 1: w' = w − α_s v_it0, partials of v_j·w' (j <= it0) and ||w'||²
-// first = 0: partials of v_j·w (second pass; only when some sample takes it)
+// First pass (first = 1): α_s (T diagonal), w' = w − α v_k, partials of
+// V_j·w' (j <= it0) and of ||w'||² (slot it0+1); second pass (first = 0):
+// partials of V_j·w (j <= it0).  w = wh + wl in double-float, interleaved as V;
+// all vector arithmetic on the FP32 pipe.
 template <int S>
-__global__ void __launch_bounds__(kNT) k_m_dot(const float* __restrict__ V, int64_t len, int it0, double* w,
-                                               const double* __restrict__ T, int lm, double* __restrict__ part, int G,
-                                               const LanczosFlags* fl, const MultiCtl* ctl, int first,
-                                               float* __restrict__ wsplit) {
+__global__ void __launch_bounds__(kNT) k_m_dot_df(const float* __restrict__ V, int64_t len, int it0,
+                                                  float* __restrict__ wh, float* __restrict__ wl,
+                                                  const double* __restrict__ T, int lm, double* __restrict__ part,
+                                                  int G, const LanczosFlags* fl, const MultiCtl* ctl, int first) {
   if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (!first && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
   __shared__ double red[(kNT / 32) * 8 * S];
   const int q = threadIdx.x % Q, r = threadIdx.x / Q, s0 = 4 * q;
   const int64_t LS = len * S;
-  double alpha[4];
+  float aH[4], aL[4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
-    alpha[u] = (first && !lane_stopped(fl, s0 + u)) ? T[(int64_t)(s0 + u) * lm * lm + (int64_t)it0 * lm + it0] : 0.0;
+  for (int u = 0; u < 4; ++u) {
+    const double al = (first && !lane_stopped(fl, s0 + u)) ? T[(int64_t)(s0 + u) * lm * lm + (int64_t)it0 * lm + it0] : 0.0;
+    df_from_double(-al, aH[u], aL[u]);
+  }
   const int m = it0 + 1;
   const int mt = first ? m + 1 : m;
   const float* __restrict__ vk = V + (int64_t)it0 * LS;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
-  if (first) {
-    // w' = w - α v_k in FP64 once per element, split into an FP32 pair (kept
-    // in wsplit for the later column blocks); the dots accumulate exact FP32
-    // products in double-float on the FP32 pipe.
-    float* __restrict__ wh = wsplit;
-    float* __restrict__ wl = wsplit + LS;
-    for (int j0 = 0; j0 < mt; j0 += 8) {
-      DFAcc acc[8][4];
-#pragma unroll
-      for (int q8 = 0; q8 < 8; ++q8)
-#pragma unroll
-        for (int u = 0; u < 4; ++u) acc[q8][u].init();
-      for (int64_t i = cb + r; i < ce; i += RPP) {
-        const int64_t e = i * S + s0;
-        float h[4], l[4];
-        if (j0 == 0) {
-          double wv[4], x[4];
-          load4(w + e, wv);
-          load4(vk + e, x);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            wv[u] = fma(-alpha[u], x[u], wv[u]);
-            df_split(wv[u], h[u], l[u]);
-          }
-          store4(w + e, wv);
-          *reinterpret_cast<float4*>(wh + e) = make_float4(h[0], h[1], h[2], h[3]);
-          *reinterpret_cast<float4*>(wl + e) = make_float4(l[0], l[1], l[2], l[3]);
-        } else {
-          const float4 a = *reinterpret_cast<const float4*>(wh + e);
-          const float4 b = *reinterpret_cast<const float4*>(wl + e);
-          h[0] = a.x; h[1] = a.y; h[2] = a.z; h[3] = a.w;
-          l[0] = b.x; l[1] = b.y; l[2] = b.z; l[3] = b.w;
-        }
-#pragma unroll
-        for (int q8 = 0; q8 < 8; ++q8) {
-          const int j = j0 + q8;
-          if (j < m) {
-            const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
-            acc[q8][0].add_prod2(x.x, h[0], l[0]);
-            acc[q8][1].add_prod2(x.y, h[1], l[1]);
-            acc[q8][2].add_prod2(x.z, h[2], l[2]);
-            acc[q8][3].add_prod2(x.w, h[3], l[3]);
-          } else if (j == m) {
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q8][u].add_prod2(h[u], h[u], 2.0f * l[u]);
-          }
-        }
-      }
-      double accd[8][4];
-#pragma unroll
-      for (int q8 = 0; q8 < 8; ++q8)
-#pragma unroll
-        for (int u = 0; u < 4; ++u) accd[q8][u] = acc[q8][u].get();
-      reduce_slots<S, 8>(accd, min(8, mt - j0), red, part, j0, G);
-    }
-    return;
-  }
   for (int j0 = 0; j0 < mt; j0 += 8) {
-    double acc[8][4];
+    DFAcc acc[8][4];
 #pragma unroll
     for (int q8 = 0; q8 < 8; ++q8)
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc[q8][u] = 0.0;
+      for (int u = 0; u < 4; ++u) acc[q8][u].init();
     for (int64_t i = cb + r; i < ce; i += RPP) {
       const int64_t e = i * S + s0;
-      double wv[4];
-      load4(w + e, wv);
+      const float4 a4 = *reinterpret_cast<const float4*>(wh + e);
+      const float4 b4 = *reinterpret_cast<const float4*>(wl + e);
+      float h[4] = {a4.x, a4.y, a4.z, a4.w}, l[4] = {b4.x, b4.y, b4.z, b4.w};
       if (first && j0 == 0) {
-        double x[4];
-        load4(vk + e, x);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) wv[u] = fma(-alpha[u], x[u], wv[u]);
-        store4(w + e, wv);
+        const float4 x = *reinterpret_cast<const float4*>(vk + e);
+        df_fma(h[0], l[0], x.x, aH[0], aL[0]);
+        df_fma(h[1], l[1], x.y, aH[1], aL[1]);
+        df_fma(h[2], l[2], x.z, aH[2], aL[2]);
+        df_fma(h[3], l[3], x.w, aH[3], aL[3]);
+        *reinterpret_cast<float4*>(wh + e) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(wl + e) = make_float4(l[0], l[1], l[2], l[3]);
       }
 #pragma unroll
       for (int q8 = 0; q8 < 8; ++q8) {
         const int j = j0 + q8;
         if (j < m) {
-          double x[4];
-          load4(V + (int64_t)j * LS + e, x);
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q8][u] = fma(x[u], wv[u], acc[q8][u]);
+          const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
+          acc[q8][0].add_prod2(x.x, h[0], l[0]);
+          acc[q8][1].add_prod2(x.y, h[1], l[1]);
+          acc[q8][2].add_prod2(x.z, h[2], l[2]);
+          acc[q8][3].add_prod2(x.w, h[3], l[3]);
         } else if (first && j == m) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q8][u] = fma(wv[u], wv[u], acc[q8][u]);
+          for (int u = 0; u < 4; ++u) acc[q8][u].add_prod2(h[u], h[u], 2.0f * l[u]);
         }
       }
     }
-    reduce_slots<S, 8>(acc, min(8, mt - j0), red, part, j0, G);
+    reduce_slots_df<S, 8>(acc, min(8, mt - j0), red, part, j0, G);
   }
 }
 
 // w_s -= Σ_j h[j*S+s] V_j,s for the live samples (second pass: only those
-// with sec[s]); part[s*G + cta] = ||w_s chunk||².
+// with sec[s]); part[s*G + cta] = ||w_s chunk||².  Double-float w, the h_j
+// split once per CTA into FP32 pairs (dynamic shared memory: 2·m·S floats).
 template <int S>
-__global__ void __launch_bounds__(kNT) k_m_axpy(const float* __restrict__ V, int64_t len, int m, double* w,
-                                                const double* __restrict__ h, double* __restrict__ part, int G,
-                                                const LanczosFlags* fl, const MultiCtl* ctl,
-                                                const int* __restrict__ sec, int df) {
+__global__ void __launch_bounds__(kNT) k_m_axpy_df(const float* __restrict__ V, int64_t len, int m,
+                                                   float* __restrict__ wh, float* __restrict__ wl,
+                                                   const double* __restrict__ h, double* __restrict__ part, int G,
+                                                   const LanczosFlags* fl, const MultiCtl* ctl,
+                                                   const int* __restrict__ sec) {
   if (cta_gate(threadIdx.x == 0 && (ctl->all_done || (sec != nullptr && !ctl->any_second)))) return;
   constexpr int Q = S / 4, RPP = kNT / Q;
-  extern __shared__ double hs[];  // m*S doubles, then (df) m*S FP32 high and m*S FP32 low parts
+  extern __shared__ float hsf[];  // m*S high parts, then m*S low parts
   __shared__ double red[(kNT / 32) * S];
-  float* hh = reinterpret_cast<float*>(hs + (int64_t)m * S);
-  float* hl = hh + (int64_t)m * S;
+  float* hh = hsf;
+  float* hl = hsf + m * S;
   for (int c = threadIdx.x; c < m * S; c += kNT) {
     const int s = c % S;
     const bool use = !lane_stopped(fl, s) && (sec == nullptr || sec[s] != 0);
-    hs[c] = use ? h[c] : 0.0;
-    if (df) df_split(hs[c], hh[c], hl[c]);
+    df_from_double(use ? h[c] : 0.0, hh[c], hl[c]);
   }
   __syncthreads();
   const int q = threadIdx.x % Q, r = threadIdx.x / Q, s0 = 4 * q;
   const int64_t LS = len * S;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
-  double nrm[1][4] = {{0.0, 0.0, 0.0, 0.0}};
-  if (df) {
-    // Σ_j h_j V_j in double-float on the FP32 pipe, one FP64 subtraction per element
-    for (int64_t i = cb + r; i < ce; i += RPP) {
-      const int64_t e = i * S + s0;
-      DFAcc s4[4];
+  DFAcc nrm[1][4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) s4[u].init();
-      for (int j = 0; j < m; ++j) {
-        const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
-        const int c = j * S + s0;
-        s4[0].add_prod2(x.x, hh[c], hl[c]);
-        s4[1].add_prod2(x.y, hh[c + 1], hl[c + 1]);
-        s4[2].add_prod2(x.z, hh[c + 2], hl[c + 2]);
-        s4[3].add_prod2(x.w, hh[c + 3], hl[c + 3]);
-      }
-      double t[4];
-      load4(w + e, t);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        t[u] -= s4[u].get();
-        nrm[0][u] = fma(t[u], t[u], nrm[0][u]);
-      }
-      store4(w + e, t);
-    }
-    reduce_slots<S, 1>(nrm, 1, red, part, 0, G);
-    return;
-  }
+  for (int u = 0; u < 4; ++u) nrm[0][u].init();
   for (int64_t i = cb + r; i < ce; i += RPP) {
     const int64_t e = i * S + s0;
-    double t[4];
-    load4(w + e, t);
+    DFAcc s4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s4[u].init();
     for (int j = 0; j < m; ++j) {
-      double x[4];
-      load4(V + (int64_t)j * LS + e, x);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) t[u] = fma(-hs[j * S + s0 + u], x[u], t[u]);
+      const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
+      const int c = j * S + s0;
+      s4[0].add_prod2(x.x, hh[c], hl[c]);
+      s4[1].add_prod2(x.y, hh[c + 1], hl[c + 1]);
+      s4[2].add_prod2(x.z, hh[c + 2], hl[c + 2]);
+      s4[3].add_prod2(x.w, hh[c + 3], hl[c + 3]);
     }
-    store4(w + e, t);
+    const float4 a4 = *reinterpret_cast<const float4*>(wh + e);
+    const float4 b4 = *reinterpret_cast<const float4*>(wl + e);
+    float hv[4] = {a4.x, a4.y, a4.z, a4.w}, lv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-    for (int u = 0; u < 4; ++u) nrm[0][u] = fma(t[u], t[u], nrm[0][u]);
+    for (int u = 0; u < 4; ++u) {
+      df_add(hv[u], lv[u], -s4[u].hi, -s4[u].lo);
+      nrm[0][u].add_prod2(hv[u], hv[u], 2.0f * lv[u]);
+    }
+    *reinterpret_cast<float4*>(wh + e) = make_float4(hv[0], hv[1], hv[2], hv[3]);
+    *reinterpret_cast<float4*>(wl + e) = make_float4(lv[0], lv[1], lv[2], lv[3]);
   }
-  reduce_slots<S, 1>(nrm, 1, red, part, 0, G);
+  reduce_slots_df<S, 1>(nrm, 1, red, part, 0, G);
 }
 
 // Second-pass decision per sample: ||w''||² < ||w'||² / 2.
@@ -380,7 +354,8 @@ __global__ void k_m_decide(const double* __restrict__ h1, const double* __restri
 
 // β_s, T entries, 1/β_s (0 for frozen or exhausted samples).
 __global__ void k_m_beta(double* T, int lm, int it0, const double* __restrict__ nrm1, const double* __restrict__ nrm2,
-                         const int* __restrict__ sec, double* invb, LanczosFlags* fl, const MultiCtl* ctl, int S) {
+                         const int* __restrict__ sec, double* invb, float2* beta2, LanczosFlags* fl,
+                         const MultiCtl* ctl, int S) {
   if (ctl->all_done) return;
   const int s = threadIdx.x;
   if (s >= S) return;
@@ -397,6 +372,9 @@ __global__ void k_m_beta(double* T, int lm, int it0, const double* __restrict__ 
     Ts[(int64_t)it0 * lm + it0 + 1] = beta;
     Ts[(int64_t)(it0 + 1) * lm + it0] = beta;
     invb[s] = 1.0 / beta;
+    float bh, bl;
+    df_from_double(beta, bh, bl);
+    beta2[s] = make_float2(bh, bl);
     f->second = second ? 1 : 0;
     if (second) f->n_second += 1;
   } else {
@@ -406,31 +384,39 @@ __global__ void k_m_beta(double* T, int lm, int it0, const double* __restrict__ 
   }
 }
 
-// v_{it0+1} = w / β per live sample
+// v_{it0+1} = w / β per live sample (w = wh + wl; 1/β split per thread)
 template <int S>
-__global__ void __launch_bounds__(kNT) k_m_scale(const double* __restrict__ w, float* __restrict__ vnext,
-                                                 const double* __restrict__ invb, int64_t len, const MultiCtl* ctl) {
+__global__ void __launch_bounds__(kNT) k_m_scale_df(const float* __restrict__ wh, const float* __restrict__ wl,
+                                                    float* __restrict__ vnext, const double* __restrict__ invb,
+                                                    int64_t len, const MultiCtl* ctl) {
   if (ctl->all_done) return;
   constexpr int Q = S / 4;
   const int64_t n4 = len * Q;
-  for (int64_t g = blockIdx.x * (int64_t)kNT + threadIdx.x; g < n4; g += (int64_t)gridDim.x * kNT) {
-    const int s0 = 4 * (int)(g % Q);
-    const int64_t e = 4 * g;
-    double ib[4], x[4];
-    bool all = true;
+  const int64_t g0 = blockIdx.x * (int64_t)kNT + threadIdx.x;
+  const int s0 = 4 * (int)(g0 % Q);  // the grid stride is a multiple of Q: fixed per thread
+  float ibh[4], ibl[4];
+  bool live[4], all = true;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      ib[u] = invb[s0 + u];
-      all = all && ib[u] != 0.0;
-    }
-    load4(w + e, x);
+  for (int u = 0; u < 4; ++u) {
+    const double ib = invb[s0 + u];
+    live[u] = ib != 0.0;
+    all = all && live[u];
+    df_from_double(ib, ibh[u], ibl[u]);
+  }
+  for (int64_t g = g0; g < n4; g += (int64_t)gridDim.x * kNT) {
+    const int64_t e = 4 * g;
+    const float4 a4 = *reinterpret_cast<const float4*>(wh + e);
+    const float4 b4 = *reinterpret_cast<const float4*>(wl + e);
+    const float h[4] = {a4.x, a4.y, a4.z, a4.w}, l[4] = {b4.x, b4.y, b4.z, b4.w};
+    float y[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) y[u] = __fmaf_rn(h[u], ibh[u], __fmaf_rn(l[u], ibh[u], __fmul_rn(h[u], ibl[u])));
     if (all) {
-      *reinterpret_cast<float4*>(vnext + e) =
-          make_float4((float)(x[0] * ib[0]), (float)(x[1] * ib[1]), (float)(x[2] * ib[2]), (float)(x[3] * ib[3]));
+      *reinterpret_cast<float4*>(vnext + e) = make_float4(y[0], y[1], y[2], y[3]);
     } else {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        if (ib[u] != 0.0) vnext[e + u] = (float)(x[u] * ib[u]);
+        if (live[u]) vnext[e + u] = y[u];
     }
   }
 }
@@ -705,29 +691,23 @@ void launch_m_sturm(const MultiDev& M, int k, int lock, cudaStream_t st) {
 
 static int reduce_grid(int count) { return (count * 32 + kNT - 1) / kNT; }
 
-void launch_m_orth(const MultiDev& M, float* V, double* w, int it0, cudaStream_t st) {
+void launch_m_orth(const MultiDev& M, float* V, float* wh, float* wl, int it0, cudaStream_t st) {
   const int m = it0 + 1, S = M.S, G = M.G;
-  // h_j (FP64) plus, when they fit the default 48 KB, their FP32 splits for
-  // the double-float update
-  const size_t hsh = sizeof(double) * (size_t)m * S;
-  const int df = 2 * hsh <= 48 * 1024 ? 1 : 0;
-  const size_t hshx = df ? 2 * hsh : hsh;
-  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 1,
-                                                     M.wsplit)));
+  const size_t hsh = 2 * sizeof(float) * (size_t)m * S;  // FP32 splits of the h_j
+  SMGPU_S_DISPATCH(S, (k_m_dot_df<SS><<<G, kNT, 0, st>>>(V, M.len, it0, wh, wl, M.T, M.lm, M.part, G, M.fl, M.ctl, 1)));
   k_m_reduce<<<reduce_grid((m + 1) * S), kNT, 0, st>>>(M.part, G, (m + 1) * S, M.h1, M.ctl, 1);
-  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hshx, st>>>(V, M.len, m, w, M.h1, M.part, G, M.fl, M.ctl, nullptr,
-                                                          df)));
+  SMGPU_S_DISPATCH(S, (k_m_axpy_df<SS><<<G, kNT, hsh, st>>>(V, M.len, m, wh, wl, M.h1, M.part, G, M.fl, M.ctl,
+                                                            nullptr)));
   k_m_reduce<<<reduce_grid(S), kNT, 0, st>>>(M.part, G, S, M.nrm1, M.ctl, 1);
   k_m_decide<<<1, 32, 0, st>>>(M.h1, M.nrm1, m, M.sec, M.fl, M.ctl, S);
-  SMGPU_S_DISPATCH(S, (k_m_dot<SS><<<G, kNT, 0, st>>>(V, M.len, it0, w, M.T, M.lm, M.part, G, M.fl, M.ctl, 0,
-                                                     M.wsplit)));
+  SMGPU_S_DISPATCH(S, (k_m_dot_df<SS><<<G, kNT, 0, st>>>(V, M.len, it0, wh, wl, M.T, M.lm, M.part, G, M.fl, M.ctl, 0)));
   k_m_reduce<<<reduce_grid(m * S), kNT, 0, st>>>(M.part, G, m * S, M.h2, M.ctl, 2);
-  SMGPU_S_DISPATCH(S, (k_m_axpy<SS><<<G, kNT, hshx, st>>>(V, M.len, m, w, M.h2, M.part, G, M.fl, M.ctl, M.sec,
-                                                          df)));
+  SMGPU_S_DISPATCH(S, (k_m_axpy_df<SS><<<G, kNT, hsh, st>>>(V, M.len, m, wh, wl, M.h2, M.part, G, M.fl, M.ctl,
+                                                            M.sec)));
   k_m_reduce<<<reduce_grid(S), kNT, 0, st>>>(M.part, G, S, M.nrm2, M.ctl, 2);
-  k_m_beta<<<1, 32, 0, st>>>(M.T, M.lm, it0, M.nrm1, M.nrm2, M.sec, M.invb, M.fl, M.ctl, S);
-  SMGPU_S_DISPATCH(S, (k_m_scale<SS><<<grid_for(M.len * S / 4), kNT, 0, st>>>(
-                          w, V + (int64_t)(it0 + 1) * M.len * S, M.invb, M.len, M.ctl)));
+  k_m_beta<<<1, 32, 0, st>>>(M.T, M.lm, it0, M.nrm1, M.nrm2, M.sec, M.invb, M.beta2, M.fl, M.ctl, S);
+  SMGPU_S_DISPATCH(S, (k_m_scale_df<SS><<<grid_for(M.len * S / 4), kNT, 0, st>>>(
+                          wh, wl, V + (int64_t)(it0 + 1) * M.len * S, M.invb, M.len, M.ctl)));
 }
 
 void launch_m_cycle_end(const MultiDev& M, cudaStream_t st) { k_m_cycle_end<<<1, 32, 0, st>>>(M.fl, M.ctl, M.S); }
