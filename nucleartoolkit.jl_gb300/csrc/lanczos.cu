@@ -622,7 +622,8 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
                                               const LanczosFlags* __restrict__ fl) {
   if (stopped(fl)) return;
   constexpr int TILE = 64;
-  extern __shared__ double tile[];  // (ls+1) x TILE of TX
+  constexpr int TS = TILE + 1;  // padded row: the 32 lanes of a warp read 32 different rows
+  extern __shared__ double tile[];  // (ls+1) x TS of TX
   TX* tl = reinterpret_cast<TX*>(tile);
   const int P = ls * (ls + 1) / 2 + ls;
   int64_t cb, ce;
@@ -637,7 +638,7 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
       int j = idx / TILE, x = idx % TILE;
       TX val = (TX)0;
       if (x < cnt) val = (j < ls) ? U[(int64_t)j * len + t0 + x] : vl[t0 + x];
-      tl[idx] = val;
+      tl[j * TS + x] = val;
     }
     __syncthreads();
 #pragma unroll
@@ -647,10 +648,10 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
       int k, l;
       gram_pair(pr, ls, k, l);
       if constexpr (sizeof(TX) == 4) {
-        for (int x = 0; x < cnt; ++x) dacc[q].add_prod(tl[k * TILE + x], tl[l * TILE + x]);
+        for (int x = 0; x < cnt; ++x) dacc[q].add_prod(tl[k * TS + x], tl[l * TS + x]);
       } else {
         double s = acc[q];
-        for (int x = 0; x < cnt; ++x) s = fma((double)tl[k * TILE + x], (double)tl[l * TILE + x], s);
+        for (int x = 0; x < cnt; ++x) s = fma((double)tl[k * TS + x], (double)tl[l * TS + x], s);
         acc[q] = s;
       }
     }
@@ -889,7 +890,7 @@ void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t
 }
 template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
-  k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 64, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
+  k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 65, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
 }
 void launch_gram_reduce(const LanczosDev& L, cudaStream_t st) {
   const int P = L.ls * (L.ls + 1) / 2 + L.ls;

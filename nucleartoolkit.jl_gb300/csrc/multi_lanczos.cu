@@ -475,22 +475,42 @@ __global__ void k_m_restart_small(double* T, int lm, int ls, const double* evals
 template <int S>
 __global__ void __launch_bounds__(kNT) k_m_rotate(const float* __restrict__ V, float* __restrict__ U,
                                                   const float* __restrict__ Yf, int m, int ls, int64_t len,
-                                                  const LanczosFlags* __restrict__ fl, const MultiCtl* ctl) {
+                                                  const LanczosFlags* __restrict__ fl, const MultiCtl* ctl,
+                                                  int use_smem) {
   if (ctl->all_done) return;
+  // 8 outputs per pass; the pass's slice of every sample's Y staged in shared
+  // memory as [j][q][s] (the lanes of a warp read consecutive samples)
+  // (staged when it fits, use_smem; otherwise read through L1)
+  extern __shared__ float ysh[];  // m * 8 * S
   const int s = threadIdx.x % S;
-  if (lane_stopped(fl, s)) return;
-  const float* __restrict__ Y = Yf + (int64_t)s * m * ls;
+  const bool live = !lane_stopped(fl, s);
   const int64_t LS = len * S;
-  for (int64_t e = blockIdx.x * (int64_t)kNT + threadIdx.x; e < LS; e += (int64_t)gridDim.x * kNT) {
-    for (int k0 = 0; k0 < ls; k0 += 8) {
+  for (int k0 = 0; k0 < ls; k0 += 8) {
+    if (use_smem) {
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < m * 8 * S; idx += kNT) {
+        const int ss = idx % S, q = (idx / S) % 8, j = idx / (8 * S);
+        ysh[idx] = (k0 + q < ls) ? Yf[(int64_t)ss * m * ls + (int64_t)(k0 + q) * m + j] : 0.f;
+      }
+      __syncthreads();
+    }
+    if (!live) continue;
+    const float* __restrict__ Ys = Yf + (int64_t)s * m * ls;
+    for (int64_t e = blockIdx.x * (int64_t)kNT + threadIdx.x; e < LS; e += (int64_t)gridDim.x * kNT) {
       KahanF acc[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) acc[q].init();
       for (int j = 0; j < m; ++j) {
         const float x = V[(int64_t)j * LS + e];
+        if (use_smem) {
+          const float* yj = ysh + j * 8 * S + s;
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (k0 + q < ls) acc[q].add(__fmul_rn(__ldg(Y + (int64_t)(k0 + q) * m + j), x));
+          for (int q = 0; q < 8; ++q) acc[q].add(__fmul_rn(yj[q * S], x));
+        } else {
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (k0 + q < ls) acc[q].add(__fmul_rn(__ldg(Ys + (int64_t)(k0 + q) * m + j), x));
+        }
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q)
@@ -513,11 +533,11 @@ __global__ void __launch_bounds__(kNT) k_m_gram(const float* __restrict__ U, con
   const int64_t LS = len * S;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
-  for (int c0 = 0; c0 < PS; c0 += 8 * kNT) {
-    DFAcc dacc[8];
-    int kk[8], ll[8];
+  for (int c0 = 0; c0 < PS; c0 += 16 * kNT) {
+    DFAcc dacc[16];
+    int kk[16], ll[16];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 16; ++q) {
       dacc[q].init();
       const int c = c0 + threadIdx.x + q * kNT;
       kk[q] = 0;
@@ -534,7 +554,7 @@ __global__ void __launch_bounds__(kNT) k_m_gram(const float* __restrict__ U, con
       }
       __syncthreads();
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
+      for (int q = 0; q < 16; ++q) {
         const int c = c0 + threadIdx.x + q * kNT;
         if (c >= PS) break;
         const int s = c % S;
@@ -545,7 +565,7 @@ __global__ void __launch_bounds__(kNT) k_m_gram(const float* __restrict__ U, con
       __syncthreads();
     }
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
+    for (int q = 0; q < 16; ++q) {
       const int c = c0 + threadIdx.x + q * kNT;
       if (c < PS) part[(int64_t)c * G + blockIdx.x] = dacc[q].get();
     }
@@ -717,7 +737,10 @@ void launch_m_restart(const MultiDev& M, float* V, float* U, cudaStream_t st) {
   const int64_t LS = M.len * S;
   k_m_jacobi<<<S, 256, jacobi_smem(m), st>>>(M.T, lm, m, M.jacA, M.jacZ, M.evals, M.fl, M.ctl, 1);
   k_m_restart_small<<<S, 256, 0, st>>>(M.T, lm, ls, M.evals, M.jacA, M.Yf, M.fl, M.ctl);
-  SMGPU_S_DISPATCH(S, (k_m_rotate<SS><<<grid_for(LS), kNT, 0, st>>>(V, U, M.Yf, m, ls, M.len, M.fl, M.ctl)));
+  const size_t ysh = sizeof(float) * (size_t)m * 8 * S;
+  const int use_smem = ysh <= 48 * 1024 ? 1 : 0;
+  SMGPU_S_DISPATCH(S, (k_m_rotate<SS><<<grid_for(LS), kNT, use_smem ? ysh : 0, st>>>(V, U, M.Yf, m, ls, M.len, M.fl,
+                                                                                  M.ctl, use_smem)));
   const int tile = gram_tile(ls, S);
   const size_t gsh = sizeof(float) * (size_t)(ls + 1) * tile * S;
   SMGPU_S_DISPATCH(S, (k_m_gram<SS><<<M.G, kNT, gsh, st>>>(U, V + (int64_t)(lm - 1) * LS, ls, M.len, tile, M.part,
