@@ -362,13 +362,15 @@ __global__ void __launch_bounds__(256) k_b_jacobi(const BatchDev B, int n, int g
   const int p = blockIdx.x;
   if (gate && (B.ctl->all_done || stopped(B.fl + p))) return;
   const int64_t o = (int64_t)p * B.lm * B.lm;
-  jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
+  if (n <= kJacobiSmemN) jacobi_eig_df<256>(B.T + o, B.lm, n, B.jacA + o, B.evals + (int64_t)p * B.lm);
+  else jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
 }
 
 // Jacobi of one problem for its Ritz vectors (grid of one CTA).
 __global__ void __launch_bounds__(256) k_b_jacobi_one(const BatchDev B, int p, int n) {
   const int64_t o = (int64_t)p * B.lm * B.lm;
-  jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
+  if (n <= kJacobiSmemN) jacobi_eig_df<256>(B.T + o, B.lm, n, B.jacA + o, B.evals + (int64_t)p * B.lm);
+  else jacobi_eig<256>(B.T + o, B.lm, n, B.jacA + o, B.jacZ + o, B.evals + (int64_t)p * B.lm);
 }
 
 __global__ void k_b_restart_small(const BatchDev B) {

@@ -315,7 +315,7 @@ struct Solve {
 
   void restart(cudaStream_t s) {
     // ThickRestart (lanczos_methods.jl:260-307)
-    launch_jacobi(L, L.lm - 1, true, s);
+    launch_jacobi(L, L.lm - 1, true, sizeof(TX) == 4, s);
     launch_restart_small(L, s);
     launch_restart_rotate<TX>(L, V, U, s);
     launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, s);
@@ -572,7 +572,7 @@ struct Solve {
     if (evecs_out && elit > 0) {
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, s);
+      launch_jacobi(L, elit, false, sizeof(TX) == 4, s);
       launch_ritz<TX>(L, V, elit, nev, R, s);
       for (int e = 0; e < nev; ++e) {
         double* r = R + (size_t)e * L.len;
@@ -670,7 +670,7 @@ struct Solve {
       // Ritz vectors (shellmodel_main.jl:208-224)
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, P->st);
+      launch_jacobi(L, elit, false, sizeof(TX) == 4, P->st);
       launch_ritz<TX>(L, V, elit, nev, R, P->st);
       launches += 2;
       for (int e = 0; e < nev; ++e) {

@@ -551,6 +551,12 @@ __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int
   if (gate && stopped(fl)) return;
   jacobi_eig<NT>(T, ldt, n, A, Z, evals);
 }
+template <int NT>
+__global__ void __launch_bounds__(NT) k_jacobi_df(const double* __restrict__ T, int ldt, int n, double* A,
+                                                  double* evals, const LanczosFlags* fl, int gate) {
+  if (gate && stopped(fl)) return;
+  jacobi_eig_df<NT>(T, ldt, n, A, evals);
+}
 
 // ThickRestart's small part (lanczos_methods.jl:261-271): new arrowhead T.
 __global__ void k_restart_small(double* T, int lm, int ls, const double* evals, const double* vecs, float* vecs_f,
@@ -876,9 +882,12 @@ void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
   k_sturm<<<1, threads, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.alpha_part, L.nalpha,
                                    L.fl);
 }
-void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st) {
+void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaStream_t st) {
   const size_t shm = jacobi_smem_bytes(n);
-  k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
+  if (df && n <= kJacobiSmemN)
+    k_jacobi_df<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.evals, L.fl, gate_on_done ? 1 : 0);
+  else
+    k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
 }
 void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
   k_restart_small<<<1, 256, 0, st>>>(L.T, L.lm, L.ls, L.evals, L.jacA, L.Yf, L.fl);

@@ -56,7 +56,8 @@ void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaS
 // The same for an FP32 basis with the residual kept in double-float, w = wh + wl.
 void launch_orth_iteration_df(const LanczosDev& L, float* V, float* wh, float* wl, int it0, cudaStream_t st);
 void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st);
-void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, cudaStream_t st);
+// df: the double-float Jacobi (FP32-mixed solves; orders above kJacobiSmemN use FP64)
+void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaStream_t st);
 void launch_restart_small(const LanczosDev& L, cudaStream_t st);
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st);

@@ -354,6 +354,149 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
   }
 }
 
+// (h, l) = (ah + al)(bh + bl) in double-float.
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
+  const float p = __fmul_rn(ah, bh);
+  float e = __fmaf_rn(ah, bh, -p);
+  e = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+  fast_two_sum(p, e, h, l);
+}
+
+// jacobi_eig in double-float arithmetic on the FP32 pipe (about 2^-47
+// relative), for the FP32-mixed solvers: GB300's FP64 pipe makes the FP64
+// rotations of jacobi_eig latency-bound.  Matrices of order n <= kJacobiSmemN
+// only (callers fall back to jacobi_eig above that); same shared memory as
+// jacobi_eig.  The rotation angle of a pair is taken in FP32 from the leading
+// parts; (c, s) are then made orthonormal to double-float precision
+// (c = (1 + t²)^(-1/2) by one Newton step, s = t c), and the rotated entries
+// are computed rather than set to zero, so an inexact angle costs convergence,
+// never orthogonality.  A pair is rotated while a_pq² > 1e-28 ||A||_F²; the
+// sweeps stop when no pair is above that.
+template <int NT>
+__device__ inline void jacobi_eig_df(const double* __restrict__ T, int ldt, int n, double* A, double* evals) {
+  __shared__ double red[NT / 32];
+  __shared__ int s_stop;
+  extern __shared__ double shj[];
+  const int N = n + (n & 1);
+  const int npair = N / 2;
+  float2* A_ = reinterpret_cast<float2*>(shj);
+  float2* Z_ = A_ + n * n;
+  float2* cc = Z_ + n * n;
+  float2* ss = cc + npair;
+  double* dg = reinterpret_cast<double*>(ss + npair);
+  int* pp = (int*)(dg + N);
+  int* qq = pp + npair;
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < n * n; idx += NT) {
+    const int i = idx % n, j = idx / n;
+    float h, l;
+    df_from_double(T[(int64_t)j * ldt + i], h, l);
+    A_[idx] = make_float2(h, l);
+    Z_[idx] = make_float2(i == j ? 1.f : 0.f, 0.f);
+  }
+  __syncthreads();
+  double fro = 0.0;
+  for (int idx = tid; idx < n * n; idx += NT) {
+    const double h = (double)A_[idx].x;
+    fro += h * h;
+  }
+  fro = block_sum_all<NT>(fro, red);
+  const float thr = (float)(1e-28 * fro);
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    double cnt = 0.0;
+    for (int idx = tid; idx < n * n; idx += NT) {
+      const int i = idx % n, j = idx / n;
+      const float a = A_[idx].x;
+      if (i < j && a * a > thr) cnt += 1.0;
+    }
+    cnt = block_sum_all<NT>(cnt, red);
+    if (tid == 0) s_stop = cnt == 0.0 ? 1 : 0;
+    __syncthreads();
+    if (s_stop) break;
+  for (int r = 0; r < N - 1; ++r) {
+      for (int k = tid; k < npair; k += NT) {
+        int p, q;
+        if (k == 0) { p = N - 1; q = r; }
+        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
+        if (p > q) { int x = p; p = q; q = x; }
+        float2 c = make_float2(1.f, 0.f), sn = make_float2(0.f, 0.f);
+        if (q < n) {
+          const float2 apq = A_[(int64_t)q * n + p];
+          if (apq.x * apq.x > thr) {
+            const float2 app = A_[(int64_t)p * n + p], aqq = A_[(int64_t)q * n + q];
+            float dh = aqq.x, dl = aqq.y;
+            df_add(dh, dl, -app.x, -app.y);
+            const float theta = dh / (2.f * apq.x);
+            const float t = (fabsf(theta) > 1e18f) ? 0.5f / theta
+                                                    : copysignf(1.f, theta) / (fabsf(theta) + sqrtf(1.f + theta * theta));
+            // r = 1 + t² (double-float), c = r^(-1/2) by one Newton step from rsqrtf
+            float rh, rl;
+            {
+              const float t2 = __fmul_rn(t, t), e = __fmaf_rn(t, t, -t2);
+              float s0, e0;
+              two_sum(1.f, t2, s0, e0);
+              fast_two_sum(s0, __fadd_rn(e0, e), rh, rl);
+            }
+            const float y = rsqrtf(rh);
+            float zh, zl;
+            {
+              const float y2 = __fmul_rn(y, y), ye = __fmaf_rn(y, y, -y2);
+              df_mul(rh, rl, y2, ye, zh, zl);
+            }
+            float oh = 1.f, ol = 0.f;
+            df_add(oh, ol, -zh, -zl);  // 1 - r y² (small)
+            float ch, cl;
+            fast_two_sum(y, __fmul_rn(0.5f * y, oh), ch, cl);
+            c = make_float2(ch, cl);
+            float sh, sl;
+            df_mul(t, 0.f, ch, cl, sh, sl);
+            sn = make_float2(sh, sl);
+          }
+        }
+        pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = sn;
+      }
+      __syncthreads();
+      // rows p, q of A, then columns, then Z; x' = c x - s y, y' = s x + c y
+      for (int pass = 0; pass < 3; ++pass) {
+        float2* M = pass == 2 ? Z_ : A_;
+        for (int idx = tid; idx < npair * n; idx += NT) {
+          const int k = idx / n, i = idx % n;
+          const float2 sk = ss[k];
+          if (sk.x == 0.f && sk.y == 0.f) continue;
+          const float2 ck = cc[k];
+          const int p = pp[k], q = qq[k];
+          const int64_t ip = pass == 1 ? (int64_t)i * n + p : (int64_t)p * n + i;
+          const int64_t iq = pass == 1 ? (int64_t)i * n + q : (int64_t)q * n + i;
+          const float2 x = M[ip], yv = M[iq];
+          float a1h, a1l, a2h, a2l, b1h, b1l, b2h, b2l;
+          df_mul(ck.x, ck.y, x.x, x.y, a1h, a1l);
+          df_mul(sk.x, sk.y, yv.x, yv.y, a2h, a2l);
+          df_mul(sk.x, sk.y, x.x, x.y, b1h, b1l);
+          df_mul(ck.x, ck.y, yv.x, yv.y, b2h, b2l);
+          df_add(a1h, a1l, -a2h, -a2l);
+          df_add(b1h, b1l, b2h, b2l);
+          M[ip] = make_float2(a1h, a1l);
+          M[iq] = make_float2(b1h, b1l);
+        }
+        __syncthreads();
+      }
+    }
+  }
+  for (int i = tid; i < n; i += NT) dg[i] = (double)A_[(int64_t)i * n + i].x + (double)A_[(int64_t)i * n + i].y;
+  __syncthreads();
+  for (int i = tid; i < n; i += NT) {
+    const double d = dg[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j)
+      if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
+    evals[rank] = d;
+    for (int r = 0; r < n; ++r) {
+      const float2 z = Z_[(int64_t)i * n + r];
+      A[(int64_t)rank * n + r] = (double)z.x + (double)z.y;
+    }
+  }
+}
+
 // Double-float accumulator: exact FP32 products (two-product by FMA) summed
 // with TwoSum into an unevaluated (hi, lo) pair — about 2^-48 relative, on
 // the FP32 pipe.  Used for the restart Gram matrix of FP32-stored vectors.

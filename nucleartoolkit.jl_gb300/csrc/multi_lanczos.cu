@@ -443,7 +443,8 @@ __global__ void __launch_bounds__(256) k_m_jacobi(const double* __restrict__ T, 
   const int s = blockIdx.x;
   if (gate && (ctl->all_done || lane_stopped(fl, s))) return;
   const int64_t o = (int64_t)s * lm * lm;
-  jacobi_eig<256>(T + o, lm, n, A + o, Z + o, evals + (int64_t)s * lm);
+  if (n <= kJacobiSmemN) jacobi_eig_df<256>(T + o, lm, n, A + o, evals + (int64_t)s * lm);
+  else jacobi_eig<256>(T + o, lm, n, A + o, Z + o, evals + (int64_t)s * lm);
 }
 
 // ThickRestart's small part (lanczos_methods.jl:261-271) per sample.
