@@ -391,13 +391,17 @@ def run_gpu(args, dist, rank, local):
     peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
     peak = (peaks or {}).get("hbm_gbs") or HBM_FALLBACK
     peak_src = "measured" if peaks and peaks.get("hbm_gbs") else "fallback"
-    prof = load_json(os.path.join(ROOT, "profiles", "hv_tile_pf4p4n_traffic.json")) or {}
+    prof = load_json(os.path.join(ROOT, "profiles", "hv_pf4p4n_traffic.json")) or {}
+    staged = bool(st.get("hv_staged"))
+    kname = "hv_staged_kernel" if staged else "hv_tile_kernel"
     roof = None
     if nnz:
         b_alg = nnz * (4 + 4) + 4 * (mdim + 1) + 2 * 1 * mdim * 4
         achieved = b_alg / (hv_ms_mixed * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": prof.get("mixed_bytes_per_launch"), "kernel": "hv_tile_kernel<float> (FP32-mixed H·v)",
+                "traffic": (prof.get(kname) or {}).get("mixed_bytes_per_launch"),
+                "kernel": f"{kname} (FP32-mixed H·v, launch shape {st['hv_threads']}x{st['hv_rows']}"
+                          f" min {st['hv_min_ctas']} CTAs/SM)",
                 "peak_source": peak_src, "algorithmic_bytes": b_alg,
                 "hv_ms": hv_ms_mixed, "hv_fp64_ms": hv_ms_fp64,
                 "hv_fp64_achieved": (nnz * (8 + 4) + 4 * (mdim + 1) + 2 * mdim * 8) / (hv_ms_fp64 * 1e-3) / 1e9}

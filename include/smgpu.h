@@ -216,11 +216,20 @@ int smgpu_timings(const smgpu_problem* h, double* times_out);
  * ms_out: mean milliseconds per launch. */
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
-/* Structural statistics of the factorised H (11 entries): [updates per H·v
+/* The H·v autotuner's measurements for this handle (no counterpart in the
+ * reference, whose operate_H! has one form): *count = number of candidate
+ * launch shapes timed when the handle was created (0 when the shape came
+ * from the cache or SMGPU_AUTOTUNE=0); for the first min(max, *count) of
+ * them, shapes[4k..4k+3] = (threads per CTA, rows per CTA, minimum CTAs per
+ * SM, kernel form: 0 row-tile, 1 staged pn) and ms[k] = mean ms per launch. */
+int smgpu_tune_report(const smgpu_problem* h, int max, int* shapes, double* ms, int* count);
+
+/* Structural statistics of the factorised H (12 entries): [updates per H·v
  * (multiply-adds), pn proton pull entries, pn neutron entries, pp entries,
  * nn entries, table bytes on the device, padded vector length, number of
- * links, H·v threads per CTA, H·v rows per CTA, H·v minimum CTAs per SM
- * (the autotuned launch shape)]. */
+ * links, H·v threads per CTA, H·v rows per CTA, H·v minimum CTAs per SM,
+ * H·v kernel form (0 row-tile, 1 staged pn) — the last four the autotuned
+ * launch shape]. */
 int smgpu_stats(const smgpu_problem* h, long long* stats_out);
 
 /* H·v that allocates nothing.  No counterpart in the reference: it exists for

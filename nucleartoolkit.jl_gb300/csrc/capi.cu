@@ -43,10 +43,10 @@ double now_s() {
 }
 
 
-// ---- autotuner cache: shape class -> (threads, rows)
+// ---- autotuner cache: shape class -> (threads, rows, min CTAs per SM, staged)
 typedef std::tuple<int, int, int, int, int, int> ShapeKey;  // precision, Lp, Ln, vp, vn, mtot2
 std::mutex g_tune_mu;
-std::map<ShapeKey, std::tuple<int, int, int>> g_tune;  // -> threads, rows, min CTAs per SM
+std::map<ShapeKey, std::tuple<int, int, int, int>> g_tune;
 bool g_tune_file_loaded = false;
 
 void tune_file_load() {
@@ -56,10 +56,10 @@ void tune_file_load() {
   if (!path) return;
   FILE* f = std::fopen(path, "r");
   if (!f) return;
-  int a[9];
-  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7],
-                     &a[8]) == 9)
-    g_tune[ShapeKey{a[0], a[1], a[2], a[3], a[4], a[5]}] = std::make_tuple(a[6], a[7], a[8]);
+  int a[10];
+  while (std::fscanf(f, "%d %d %d %d %d %d %d %d %d %d", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7],
+                     &a[8], &a[9]) == 10)
+    g_tune[ShapeKey{a[0], a[1], a[2], a[3], a[4], a[5]}] = std::make_tuple(a[6], a[7], a[8], a[9]);
   std::fclose(f);
 }
 void tune_file_store() {
@@ -68,21 +68,26 @@ void tune_file_store() {
   FILE* f = std::fopen(path, "w");
   if (!f) return;
   for (auto& kv : g_tune)
-    std::fprintf(f, "%d %d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
+    std::fprintf(f, "%d %d %d %d %d %d %d %d %d %d\n", std::get<0>(kv.first), std::get<1>(kv.first),
                  std::get<2>(kv.first), std::get<3>(kv.first), std::get<4>(kv.first), std::get<5>(kv.first),
-                 std::get<0>(kv.second), std::get<1>(kv.second), std::get<2>(kv.second));
+                 std::get<0>(kv.second), std::get<1>(kv.second), std::get<2>(kv.second), std::get<3>(kv.second));
   std::fclose(f);
 }
 }  // namespace
 
 void smgpu_problem::autotune() {
   ShapeKey key{precision, T.Lp, T.Ln, vp, vn, mtot2};
-  {
+  // SMGPU_HV_FORM=tile|staged restricts the candidates to one H·v kernel form
+  // (and bypasses the shape cache); unset, both forms compete.
+  const char* form_env = std::getenv("SMGPU_HV_FORM");
+  const std::string form = form_env ? form_env : "";
+  const bool forced = form == "tile" || form == "staged";
+  if (!forced) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     tune_file_load();
     auto it = g_tune.find(key);
     if (it != g_tune.end()) {
-      set_config(std::get<0>(it->second), std::get<1>(it->second), std::get<2>(it->second));
+      set_config(std::get<0>(it->second), std::get<1>(it->second), std::get<2>(it->second), std::get<3>(it->second));
       return;
     }
   }
@@ -101,12 +106,22 @@ void smgpu_problem::autotune() {
       launch_convert(d_start, (float*)d_v, T.len_pad, st);
     SMGPU_CUDA_TRY(cudaEventCreate(&a));
     SMGPU_CUDA_TRY(cudaEventCreate(&b));
-    int nc = 0;
-    const HvConfig* cand = hv_candidates(&nc);
+    int nc0 = 0, ns = 0;
+    const HvConfig* c0 = hv_candidates(&nc0);
+    const HvConfig* cs = hv_staged_candidates(&ns);
+    std::vector<HvConfig> cand;
+    if (form != "staged" || precision == SMGPU_FP64) cand.assign(c0, c0 + nc0);
+    if (precision != SMGPU_FP64 && form != "tile")
+      for (int k = 0; k < ns; ++k)
+        if (hv_staged_fits(cs[k], tt, nnmax_raw)) cand.push_back(cs[k]);
+    if (cand.empty()) cand.assign(c0, c0 + nc0);  // the staged form does not fit this problem
+    const int nc = (int)cand.size();
+    tune_shapes = cand;
+    tune_ms.assign(nc, 0.0);
     int best = -1;
     float best_ms = 1e30f;
     for (int c = 0; c < nc; ++c) {
-      set_config(cand[c].nt, cand[c].rows, cand[c].minb);
+      set_config(cand[c].nt, cand[c].rows, cand[c].minb, cand[c].staged);
       float total = 0.f;
       for (int rep = 0; rep < 3; ++rep) {
         SMGPU_CUDA_TRY(cudaEventRecord(a, st));
@@ -119,16 +134,18 @@ void smgpu_problem::autotune() {
         if (rep > 0) total += ms;  // first launch is the warm-up
       }
       SMGPU_CUDA_TRY(cudaGetLastError());
-      if (c < 16) tune_ms[c] = total / 2;
+      tune_ms[c] = total / 2;
       if (total < best_ms) {
         best_ms = total;
         best = c;
       }
     }
-    set_config(cand[best].nt, cand[best].rows, cand[best].minb);
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = std::make_tuple(cfg.nt, cfg.rows, cfg.minb);
-    tune_file_store();
+    set_config(cand[best].nt, cand[best].rows, cand[best].minb, cand[best].staged);
+    if (!forced) {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = std::make_tuple(cfg.nt, cfg.rows, cfg.minb, cfg.staged);
+      tune_file_store();
+    }
   } catch (...) {
     if (a) cudaEventDestroy(a);
     if (b) cudaEventDestroy(b);
@@ -1321,6 +1338,21 @@ int smgpu_jj(smgpu_problem* h, const double* vecs, int nvec, double* jj_out) {
   });
 }
 
+int smgpu_tune_report(const smgpu_problem* h, int max, int* shapes, double* ms, int* count) {
+  if (!h || !count || max < 0 || (max > 0 && (!shapes || !ms))) return SMGPU_ERR_ARG;
+  const int n = (int)h->tune_shapes.size();
+  *count = n;
+  for (int k = 0; k < n && k < max; ++k) {
+    const HvConfig& c = h->tune_shapes[k];
+    shapes[4 * k + 0] = c.nt;
+    shapes[4 * k + 1] = c.rows;
+    shapes[4 * k + 2] = c.minb;
+    shapes[4 * k + 3] = c.staged;
+    ms[k] = h->tune_ms[k];
+  }
+  return SMGPU_OK;
+}
+
 int smgpu_timings(const smgpu_problem* h, double* t) {
   if (!h || !t) return SMGPU_ERR_ARG;
   for (int k = 0; k < 8; ++k) t[k] = h->times[k];
@@ -1341,6 +1373,7 @@ int smgpu_stats(const smgpu_problem* h, long long* s) {
   s[8] = h->cfg.nt;
   s[9] = h->cfg.rows;
   s[10] = h->cfg.minb;
+  s[11] = h->cfg.staged;
   return SMGPU_OK;
 }
 

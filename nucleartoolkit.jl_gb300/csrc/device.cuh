@@ -84,6 +84,24 @@ struct TileTables {
   const int* rl;           // per (row, link slot): first proton entry; slot nl = end
   const int64_t* npn_ptr;  // neutron pull CSR row pointers (per link, nn[b]+1 each)
   const uint32_t* npn_ent; // n'<<14 | (sign*nA*nB + ib)
+  // staged pn form (FP32-mixed): per link, the pull entries regrouped by
+  // source neutron column ("push" lists).  Entry = slot | ib << 16 | sign << 31,
+  // slot = t * nn[b] + n' for the t-th pull entry of output column n'.
+  const int64_t* push_off;   // per link: offset of its nn[s]+1 list pointers in push_ptr / push_col
+  const int64_t* push_ptr;   // lists in descending order of length
+  const int* push_col;       // the source column of each list
+  const uint32_t* push_ent;
+  // nn term of the staged kernel: per block, the nn pull lists as an ELL
+  // array [k][n] (padded with zero coefficients on column n)
+  const int64_t* nnell_off;  // per block
+  const int* nnell_w;        // per block: longest list
+  const int* nnell_col;
+  const float* nnell_val;
+  int ymax;     // floats of one row's slot buffer: max over links of (longest pull list) * nn[b]
+  int nnmax;    // largest nn[b], rounded up to 4
+  int nbmax;    // largest neutron-operator count nB of a link
+  int astride;  // row stride (floats) of the per-row coefficient matrices, = 4 mod 8
+  int kpad;     // largest proton-entry count of one (row, link), rounded up to 4
 };
 
 struct HvConfig {
@@ -91,6 +109,7 @@ struct HvConfig {
   int rows;    // rows per CTA
   int ntasks;  // CTAs
   int minb;    // minimum resident CTAs per SM requested from the compiler (caps registers)
+  int staged;  // 1: the staged pn kernel (hv_staged.cu, FP32-mixed only); 0: the row-tile pull kernel
 };
 
 // Scalars and flags of the Lanczos driver (device memory, one per solve).
@@ -204,6 +223,19 @@ void launch_hv_mixed(const DevTables& t, const TileTables& tt, const HvConfig& c
 void launch_hv_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
                         const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
                         const HvEpilogue<float>& epi, cudaStream_t st);
+// Staged-pn FP32-mixed H·v (hv_staged.cu): candidate shapes (staged = 1),
+// whether a shape fits the problem, its dynamic shared memory, and the
+// one-time set-up of that shared-memory size (call before graph capture).
+const HvConfig* hv_staged_candidates(int* count);
+bool hv_staged_fits(const HvConfig& cfg, const TileTables& tt, int nnmax_raw);
+size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt);
+void hv_staged_prepare(const HvConfig& cfg, const TileTables& tt);
+void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
+                            const double* en, const CoefTables<float>& c, const float* v, double* w,
+                            const HvEpilogue<float>& epi, cudaStream_t st);
+void launch_hv_staged_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
+                               const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
+                               const HvEpilogue<float>& epi, cudaStream_t st);
 // Multi-sample H·V (hv_multi.cu).  S in {4, 8, 16}; tt1 = one-row tasks
 // (ntasks of them); v/w interleaved; cand = index into hv_multi_candidates().
 struct MultiHvConfig {

@@ -1,0 +1,387 @@
+// FP32-mixed H·v with the pn term in two shared-memory stages.
+//
+// Same output, tiling and epilogue as the row-tile kernel (hv.cu): a CTA owns
+// R consecutive rows (proton Slater determinants p) of one (Mp,Mn) block and
+// writes each of their elements once.  What differs is the pn term of a link
+// (output block b <- source block s):
+//
+//   w[p,n] += Σ_{(p',ia,±)∈P(p)} Σ_{(n',ib,±)∈N(n)} ± V[ia][ib] v[s,p',n']
+//
+// The row-tile kernel evaluates that sum per (row, column) with two gathers
+// per update (the coefficient and v), both through L1; on GB300 those
+// scattered loads, not HBM, bound it.  Here the sum is re-associated:
+//
+//   stage 1, one thread per SOURCE column n':  for every neutron operator ib
+//            that leaves n' in the block (the "push" list of n'),
+//            y = Σ_{(p',ia,±)} (±V[ia][ib]) v[s,p',n'] — the proton entries'
+//            coefficients for this row are first gathered into a dense
+//            matrix A[ib][j] in shared memory, so the inner loop is one
+//            float4 shared load per four FMAs with v[s,p',n'] in registers;
+//            y goes to the slot of its output column in shared memory.
+//   stage 2, one thread per OUTPUT column n: the sum of its slots (the slots
+//            of column n are laid out [t][n], so a warp reads consecutive
+//            words), added to the column's Kahan-compensated pn sum.
+//
+// Every update is still one FP32 multiply-add, in the order of the proton
+// entries; the partial sums are FP32 per (row, link, neutron entry), combined
+// with Kahan compensation per (row, link) as in the row-tile kernel.  The nn
+// term gathers from the CTA's rows of v staged in shared memory; pp, the
+// one-body term and the Lanczos epilogue are those of hv_tile.cuh.
+#include <cstdio>
+
+#include "device.cuh"
+#include "hv_tile.cuh"
+
+namespace smgpu {
+
+namespace {
+
+template <int NT, int R, int QM, int MINB, bool DF>
+__global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float, float> a) {
+  if (a.fl != nullptr && cta_gate(threadIdx.x == 0 && (a.fl->done || a.fl->exhausted))) return;
+  const DevTables& t = a.t;
+  const TileTables& tt = a.tt;
+  extern __shared__ float4 sm4[];
+  float* Y = reinterpret_cast<float*>(sm4);          // [R][ymax] slots
+  float* A = Y + R * tt.ymax;                        // [R][nbmax][astride] coefficients
+  float* vrow = A + R * tt.nbmax * tt.astride;       // [R][nnmax] the CTA's rows of v
+  int* so = reinterpret_cast<int*>(vrow + R * tt.nnmax);  // [R][kpad] source-row offsets into v
+  const int tid = threadIdx.x;
+  const int task = blockIdx.x;
+  const int b = tt.task_b[task], p0 = tt.task_p0[task];
+  const int np = t.np[b];
+  const int nr = min(R, np - p0);
+  const int nn = t.nn[b];
+  const int stride = t.stride[b];
+  const int64_t blk = t.off_pad[b];
+  const int pst = t.pstart[b], nst = t.nstart[b];
+  const int lb = tt.link_begin[b];
+  const int nl = tt.link_begin[b + 1] - lb;
+  const int64_t rlb = tt.rl_base[b] + (int64_t)p0 * (nl + 1);
+  const float* __restrict__ v = a.v;
+  const int as = tt.astride, kpad = tt.kpad;
+
+  for (int idx = tid; idx < nr * nn; idx += NT) {
+    const int r = idx / nn, n = idx - r * nn;
+    vrow[r * tt.nnmax + n] = v[blk + (int64_t)(p0 + r) * stride + n];
+  }
+
+  AccKahan pn[R][QM];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int q = 0; q < QM; ++q) pn[r][q].init();
+
+  for (int j = 0; j < nl; ++j) {
+    const int L = lb + j;
+    int kr[R];
+    int eb[R];
+    int kmx = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      kr[r] = 0;
+      eb[r] = 0;
+      if (r < nr) {
+        eb[r] = tt.rl[rlb + (int64_t)r * (nl + 1) + j];
+        kr[r] = tt.rl[rlb + (int64_t)r * (nl + 1) + j + 1] - eb[r];
+      }
+      kmx = max(kmx, kr[r]);
+    }
+    if (kmx == 0) continue;  // no proton entry of these rows uses the link (uniform over the CTA)
+    const int4 la = t.link_a[L];
+    const int s = la.x, nB = la.y;
+    const float* __restrict__ vt = a.c.vtab + t.link_v[L];  // V; the negated copy is not used here
+    const int kp = (kmx + 3) & ~3;
+    const int64_t soff = t.off_pad[s];
+    const int sstride = t.stride[s];
+    const int nns = t.nn[s];
+    // coefficient matrices A_r[ib][j] = ±V[ia_j][ib] (zero-padded to kp) and source offsets
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r >= nr || kr[r] == 0) continue;
+      float* Ar = A + r * tt.nbmax * as;
+      for (int idx = tid; idx < nB * kp; idx += NT) {
+        const int ib = idx / kp, jj = idx - ib * kp;
+        float val = 0.f;
+        if (jj < kr[r]) {
+          const uint32_t meta = t.ppn_meta[eb[r] + jj];
+          val = vt[(int)((meta >> 1) & 0x7fffu) * nB + ib];
+          if (meta & 1u) val = -val;
+        }
+        Ar[ib * as + jj] = val;
+      }
+      for (int jj = tid; jj < kr[r]; jj += NT) so[r * kpad + jj] = (int)(soff + (int64_t)t.ppn_src[eb[r] + jj] * sstride);
+    }
+    __syncthreads();
+    // stage 1: one thread per source column, columns in descending order of
+    // list length; the entry loop stops at the warp's longest list
+    const int64_t* __restrict__ pptr = tt.push_ptr + tt.push_off[L];
+    const int* __restrict__ pcol = tt.push_col + tt.push_off[L];
+    for (int i0 = 0; i0 < nns; i0 += NT) {
+      // every lane of the warp runs this loop body (the warp reductions need them all)
+      const int i = i0 + tid;
+      const bool act = i < nns;
+      const int n = act ? pcol[i] : 0;
+      const int64_t e0 = act ? pptr[i] : 0, e1 = act ? pptr[i + 1] : 0;
+      for (int64_t ec = e0;; ec += 16) {
+        const int ne = (int)max((int64_t)0, min((int64_t)16, e1 - ec));
+        const int kw = (int)__reduce_max_sync(0xffffffffu, (unsigned)ne);
+        if (kw == 0) break;
+        uint32_t ent[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) ent[k] = (k < ne) ? tt.push_ent[ec + k] : 0u;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r >= nr || kr[r] == 0) continue;
+          const float* Ar = A + r * tt.nbmax * as;
+          const int* sor = so + r * kpad;
+          float* Yr = Y + r * tt.ymax;
+          // proton entries in blocks of 16: v[s,p'_j,n'] of the block in registers
+          for (int j0 = 0; j0 < kr[r]; j0 += 16) {
+            const int kq = min(16, kr[r] - j0);
+            float x[16];
+#pragma unroll
+            for (int jj = 0; jj < 16; ++jj) x[jj] = (jj < kq) ? v[sor[j0 + jj] + n] : 0.f;
+            // four entries at a time, branch-free inside a group (entries past
+            // the lane's list read row 0 of A and are not stored)
+#pragma unroll
+            for (int k0 = 0; k0 < 16; k0 += 4) {
+              if (k0 >= kw) break;
+              const float* a0 = Ar + (int)((ent[k0] >> 16) & 0x7fffu) * as + j0;
+              const float* a1 = Ar + (int)((ent[k0 + 1] >> 16) & 0x7fffu) * as + j0;
+              const float* a2 = Ar + (int)((ent[k0 + 2] >> 16) & 0x7fffu) * as + j0;
+              const float* a3 = Ar + (int)((ent[k0 + 3] >> 16) & 0x7fffu) * as + j0;
+              float y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
+#pragma unroll
+              for (int jc = 0; jc < 16; jc += 4) {
+                if (jc >= kq) break;
+                const float4 b0 = *reinterpret_cast<const float4*>(a0 + jc);
+                const float4 b1 = *reinterpret_cast<const float4*>(a1 + jc);
+                const float4 b2 = *reinterpret_cast<const float4*>(a2 + jc);
+                const float4 b3 = *reinterpret_cast<const float4*>(a3 + jc);
+                y0 = __fmaf_rn(b0.w, x[jc + 3], __fmaf_rn(b0.z, x[jc + 2], __fmaf_rn(b0.y, x[jc + 1], __fmaf_rn(b0.x, x[jc], y0))));
+                y1 = __fmaf_rn(b1.w, x[jc + 3], __fmaf_rn(b1.z, x[jc + 2], __fmaf_rn(b1.y, x[jc + 1], __fmaf_rn(b1.x, x[jc], y1))));
+                y2 = __fmaf_rn(b2.w, x[jc + 3], __fmaf_rn(b2.z, x[jc + 2], __fmaf_rn(b2.y, x[jc + 1], __fmaf_rn(b2.x, x[jc], y2))));
+                y3 = __fmaf_rn(b3.w, x[jc + 3], __fmaf_rn(b3.z, x[jc + 2], __fmaf_rn(b3.y, x[jc + 1], __fmaf_rn(b3.x, x[jc], y3))));
+              }
+              const float yv[4] = {y0, y1, y2, y3};
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const uint32_t e = ent[k0 + u];
+                const float y = (e >> 31) ? -yv[u] : yv[u];
+                if (k0 + u < ne) {
+                  const uint32_t slot = e & 0xffffu;
+                  Yr[slot] = (j0 == 0) ? y : __fadd_rn(Yr[slot], y);
+                }
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // stage 2: one thread per output column; slots [t][n]
+    const int64_t* __restrict__ nptr = tt.npn_ptr + t.link_n[L];
+#pragma unroll
+    for (int q = 0; q < QM; ++q) {
+      const int n = tid + q * NT;
+      if (n < nn) {
+        const int K = (int)(nptr[n + 1] - nptr[n]);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r >= nr || kr[r] == 0) continue;
+          const float* Yr = Y + r * tt.ymax + n;
+          float sacc = 0.f;
+#pragma unroll 4
+          for (int k = 0; k < K; ++k) sacc = __fadd_rn(sacc, Yr[k * nn]);
+          pn[r][q].add(sacc);
+        }
+      }
+    }
+  }
+  __syncthreads();  // vrow complete (also when the block has no links)
+
+  const double beta = (a.vprev != nullptr) ? *a.beta : 0.0;
+  double apart = 0.0;
+  float ah = 0.f, al = 0.f;  // DF: α partial
+  float bh = 0.f, bl = 0.f;  // DF: β
+  if constexpr (DF) df_from_double(beta, bh, bl);
+#pragma unroll
+  for (int q = 0; q < QM; ++q) {
+    const int n = tid + q * NT;
+    if (n >= nn) continue;
+    AccKahan acc[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = pn[r][q];
+    // nn: same proton row, other neutron columns (ELL lists, rows of v in
+    // shared memory); FP32 partial sums, one compensated add per row
+    {
+      const int W = tt.nnell_w[b];
+      const int* __restrict__ ecol = tt.nnell_col + tt.nnell_off[b] + n;
+      const float* __restrict__ eval = tt.nnell_val + tt.nnell_off[b] + n;
+      float sn[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) sn[r] = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < W; ++k) {
+        const int c = ecol[(int64_t)k * nn];
+        const float cv = eval[(int64_t)k * nn];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (r < nr) sn[r] = __fmaf_rn(cv, vrow[r * tt.nnmax + c], sn[r]);
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) acc[r].add(sn[r]);
+    }
+    // pp: other proton rows of the block, same neutron column (coalesced)
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r >= nr) break;
+      const int g = pst + p0 + r;
+      const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
+      float sp = 0.f;
+#pragma unroll 4
+      for (int k = kb; k < ke; ++k) sp = __fmaf_rn(a.c.pp_val[k], v[blk + (int64_t)t.pp_col[k] * stride + n], sp);
+      acc[r].add(sp);
+    }
+    // one-body term, Lanczos epilogue, store
+    if constexpr (DF) {
+      const float2 en2 = a.en2[nst + n];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r >= nr) break;
+        const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
+        const float x = vrow[r * tt.nnmax + n];
+        float hh, hl;
+        fast_two_sum(acc[r].s, -acc[r].c, hh, hl);
+        const float2 ep2 = a.ep2[pst + p0 + r];
+        float dh = ep2.x, dl = ep2.y;
+        df_add(dh, dl, en2.x, en2.y);
+        df_fma(hh, hl, x, dh, dl);
+        {
+          const float p = __fmul_rn(x, hh);
+          const float pe = __fmaf_rn(x, hh, -p);
+          float s2, e2;
+          two_sum(ah, p, s2, e2);
+          ah = s2;
+          al = __fadd_rn(al, __fadd_rn(e2, __fmaf_rn(x, hl, pe)));
+        }
+        if (a.vprev != nullptr) df_fma(hh, hl, a.vprev[o], -bh, -bl);
+        a.wh[o] = hh;
+        a.wl[o] = hl;
+      }
+    } else {
+      const double enn = a.en[nst + n];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r >= nr) break;
+        const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
+        const double x = (double)vrow[r * tt.nnmax + n];
+        double hv = acc[r].result() + (a.ep[pst + p0 + r] + enn) * x;
+        apart = fma(x, hv, apart);
+        if (a.vprev != nullptr) hv = fma(-beta, (double)a.vprev[o], hv);
+        a.w[o] = hv;
+      }
+    }
+  }
+  if (a.alpha_part != nullptr) {
+    __shared__ double red[NT / 32];
+    if constexpr (DF) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, ah, o);
+        const float ol = __shfl_down_sync(0xffffffffu, al, o);
+        df_add(ah, al, oh, ol);
+      }
+      apart = (double)ah + (double)al;
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) apart += __shfl_down_sync(0xffffffffu, apart, o);
+    }
+    if ((tid & 31) == 0) red[tid >> 5] = apart;
+    __syncthreads();
+    if (tid == 0) {
+      double s2 = 0.0;
+      for (int k = 0; k < NT / 32; ++k) s2 += red[k];
+      a.alpha_part[task] = s2;
+    }
+  }
+}
+
+// {threads, rows, -, min CTAs per SM, staged}; a thread owns up to
+// qm_for(threads) output columns.
+constexpr int qm_for(int nt) { return nt <= 128 ? 5 : 3; }
+constexpr HvConfig kStagedCand[] = {{128, 1, 0, 1, 1}, {128, 1, 0, 4, 1}, {128, 1, 0, 5, 1}, {128, 2, 0, 3, 1},
+                                    {192, 1, 0, 2, 1}, {192, 2, 0, 2, 1}, {256, 1, 0, 1, 1}, {256, 1, 0, 2, 1},
+                                    {256, 2, 0, 2, 1}};
+
+template <bool DF>
+bool dispatch(const HvConfig& cfg, const HvArgs<float, float>& a, size_t smem, cudaStream_t st, bool prepare) {
+#define SMGPU_ST_CASE(NT_, R_, MB_)                                                                     \
+  if (cfg.nt == NT_ && cfg.rows == R_ && cfg.minb == MB_) {                                             \
+    auto k = hv_staged_kernel<NT_, R_, qm_for(NT_), MB_, DF>;                                           \
+    if (prepare) {                                                                                      \
+      SMGPU_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+    } else {                                                                                            \
+      k<<<cfg.ntasks, NT_, smem, st>>>(a);                                                              \
+    }                                                                                                   \
+    return true;                                                                                        \
+  }
+  SMGPU_ST_CASE(128, 1, 1)
+  SMGPU_ST_CASE(128, 1, 4)
+  SMGPU_ST_CASE(128, 1, 5)
+  SMGPU_ST_CASE(128, 2, 3)
+  SMGPU_ST_CASE(192, 1, 2)
+  SMGPU_ST_CASE(192, 2, 2)
+  SMGPU_ST_CASE(256, 1, 1)
+  SMGPU_ST_CASE(256, 1, 2)
+  SMGPU_ST_CASE(256, 2, 2)
+#undef SMGPU_ST_CASE
+  return false;
+}
+
+}  // namespace
+
+const HvConfig* hv_staged_candidates(int* count) {
+  *count = (int)(sizeof(kStagedCand) / sizeof(kStagedCand[0]));
+  return kStagedCand;
+}
+
+size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt) {
+  const size_t R = (size_t)cfg.rows;
+  return sizeof(float) * R * ((size_t)tt.ymax + (size_t)tt.nbmax * tt.astride + (size_t)tt.nnmax) +
+         sizeof(int) * R * (size_t)tt.kpad;
+}
+
+bool hv_staged_fits(const HvConfig& cfg, const TileTables& tt, int nnmax_raw) {
+  if (tt.push_ent == nullptr) return false;
+  if (nnmax_raw > cfg.nt * qm_for(cfg.nt)) return false;
+  return hv_staged_smem(cfg, tt) <= 200 * 1024;
+}
+
+void hv_staged_prepare(const HvConfig& cfg, const TileTables& tt) {
+  const size_t smem = hv_staged_smem(cfg, tt);
+  HvArgs<float, float> a{};
+  dispatch<false>(cfg, a, smem, nullptr, true);
+  dispatch<true>(cfg, a, smem, nullptr, true);
+}
+
+void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
+                            const double* en, const CoefTables<float>& c, const float* v, double* w,
+                            const HvEpilogue<float>& epi, cudaStream_t st) {
+  HvArgs<float, float> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
+                         nullptr, nullptr, nullptr, nullptr};
+  if (!dispatch<false>(cfg, a, hv_staged_smem(cfg, tt), st, false))
+    throw CudaError{cudaErrorInvalidConfiguration, "staged H·v launch shape", __FILE__, __LINE__};
+}
+
+void launch_hv_staged_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
+                               const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
+                               const HvEpilogue<float>& epi, cudaStream_t st) {
+  HvArgs<float, float> a{t, tt, c, nullptr, nullptr, v, nullptr, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
+                         wh, wl, ep2, en2};
+  if (!dispatch<true>(cfg, a, hv_staged_smem(cfg, tt), st, false))
+    throw CudaError{cudaErrorInvalidConfiguration, "staged H·v launch shape", __FILE__, __LINE__};
+}
+
+}  // namespace smgpu

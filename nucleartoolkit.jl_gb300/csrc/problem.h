@@ -87,13 +87,15 @@ struct smgpu_problem {
   const double* d_en = nullptr;
   const float2* d_ep2 = nullptr;  // one-body diagonals as double-float pairs (FP32-mixed solve)
   const float2* d_en2 = nullptr;
-  HvConfig cfg{128, 4, 0, 1};
+  HvConfig cfg{128, 4, 0, 1, 0};
+  int nnmax_raw = 0;  // largest nn[b]
   std::map<int, std::pair<const int*, const int*>> task_arrays;  // rows -> (task_b, task_p0)
   std::map<int, int> task_count;
   cudaStream_t st = nullptr, st2 = nullptr;
   std::string err;
   double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  double tune_ms[16] = {0};
+  std::vector<HvConfig> tune_shapes;  // candidates timed by the last autotune
+  std::vector<double> tune_ms;        // their mean ms per H·v launch
   int sms = 152;
   DeviceArena solver;  // Krylov basis and scratch of the last solve
   Interaction I;       // the interaction the tables were built from
@@ -125,14 +127,109 @@ struct smgpu_problem {
     task_arrays[R] = {tables.upload(tb), tables.upload(tp)};
     task_count[R] = (int)tb.size();
   }
-  void set_config(int nt, int R, int minb) {
+  void set_config(int nt, int R, int minb, int staged = 0) {
     ensure_tasks(R);
     cfg.nt = nt;
     cfg.rows = R;
     cfg.minb = minb;
+    cfg.staged = staged;
     cfg.ntasks = task_count[R];
     tt.task_b = task_arrays[R].first;
     tt.task_p0 = task_arrays[R].second;
+    if (staged) hv_staged_prepare(cfg, tt);
+  }
+
+  // Push lists of the staged pn kernel (hv_staged.cu): every link's neutron
+  // pull entries regrouped by source column, each carrying the slot of its
+  // output column.  Leaves tt.push_ent null when the packing limits are
+  // exceeded (the row-tile kernel is then the only H·v form).
+  void build_staged(const std::vector<int>& rl) {
+    tt.push_ent = nullptr;
+    const size_t nl = T.links.size();
+    std::vector<int64_t> poff(nl), pptr;
+    std::vector<int> pcol;
+    std::vector<uint32_t> pent;
+    int64_t ymax = 0;
+    int nbmax = 0, kmax = 0;
+    nnmax_raw = 0;
+    for (int b = 0; b < T.nb; ++b) nnmax_raw = std::max(nnmax_raw, T.nn[b]);
+    if (T.len_pad >= ((int64_t)1 << 31)) return;
+    for (size_t li = 0; li < nl; ++li) {
+      const auto& L = T.links[li];
+      const int nno = T.nn[L.b], nns = T.nn[L.s];
+      const int64_t* np_ = T.npn_ptr.data() + L.nptr_off;
+      std::vector<int64_t> cnt(nns + 1, 0);
+      int64_t kw = 0;
+      for (int n = 0; n < nno; ++n) {
+        kw = std::max(kw, np_[n + 1] - np_[n]);
+        for (int64_t g = np_[n]; g < np_[n + 1]; ++g) cnt[(T.npn_ent[g] >> 14) + 1]++;
+      }
+      if (kw * nno > 65536) return;
+      ymax = std::max(ymax, kw * nno);
+      nbmax = std::max(nbmax, L.nB);
+      if (L.nB >= (1 << 15)) return;
+      // source columns in descending order of their entry counts, so the
+      // lanes of a warp carry lists of about the same length
+      std::vector<int> order(nns);
+      for (int n = 0; n < nns; ++n) order[n] = n;
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cnt[x + 1] > cnt[y + 1]; });
+      std::vector<int64_t> start(nns + 1, 0);  // entry offset of each source column (position order)
+      std::vector<int> posof(nns);
+      for (int i = 0; i < nns; ++i) {
+        posof[order[i]] = i;
+        start[i + 1] = start[i] + cnt[order[i] + 1];
+      }
+      poff[li] = (int64_t)pptr.size();
+      const int64_t base = (int64_t)pent.size();
+      for (int i = 0; i <= nns; ++i) {
+        pptr.push_back(base + start[i]);
+        pcol.push_back(i < nns ? order[i] : 0);
+      }
+      pent.resize(base + start[nns]);
+      std::vector<int64_t> pos(start.begin(), start.end() - 1);
+      for (int n = 0; n < nno; ++n)
+        for (int64_t g = np_[n]; g < np_[n + 1]; ++g) {
+          const uint32_t e = T.npn_ent[g];
+          const uint32_t src = e >> 14, ib = (e >> 1) & 0x1fffu, sg = e & 1u;
+          const uint32_t slot = (uint32_t)((g - np_[n]) * nno + n);
+          pent[base + pos[posof[src]]++] = slot | (ib << 16) | (sg << 31);
+        }
+    }
+    for (size_t k = 0; k + 1 < rl.size(); ++k) kmax = std::max(kmax, rl[k + 1] - rl[k]);
+    // nn lists as ELL [k][n] per block
+    std::vector<int64_t> eoff(T.nb);
+    std::vector<int> ew(T.nb), ecol;
+    std::vector<float> evl;
+    for (int b = 0; b < T.nb; ++b) {
+      const int nnb = T.nn[b], g0 = T.nstart[b];
+      int w = 0;
+      for (int n = 0; n < nnb; ++n) w = std::max(w, T.nn_ptr[g0 + n + 1] - T.nn_ptr[g0 + n]);
+      eoff[b] = (int64_t)ecol.size();
+      ew[b] = w;
+      ecol.resize(ecol.size() + (size_t)w * nnb);
+      evl.resize(ecol.size());
+      for (int n = 0; n < nnb; ++n) {
+        const int kb = T.nn_ptr[g0 + n], ke = T.nn_ptr[g0 + n + 1];
+        for (int k = 0; k < w; ++k) {
+          const size_t o = (size_t)eoff[b] + (size_t)k * nnb + n;
+          ecol[o] = kb + k < ke ? T.nn_col[kb + k] : n;
+          evl[o] = kb + k < ke ? (float)T.nn_val[kb + k] : 0.f;
+        }
+      }
+    }
+    tt.nnell_off = tables.upload(eoff);
+    tt.nnell_w = tables.upload(ew);
+    tt.nnell_col = tables.upload(ecol);
+    tt.nnell_val = tables.upload(evl);
+    tt.push_off = tables.upload(poff);
+    tt.push_ptr = tables.upload(pptr);
+    tt.push_col = tables.upload(pcol);
+    tt.push_ent = tables.upload(pent);
+    tt.ymax = (int)((ymax + 3) & ~(int64_t)3);
+    tt.nnmax = (nnmax_raw + 3) & ~3;
+    tt.nbmax = std::max(nbmax, 1);
+    tt.kpad = std::max(4, (kmax + 3) & ~3);
+    tt.astride = (tt.kpad % 8 == 0) ? tt.kpad + 4 : tt.kpad;
   }
 
   // Device copies of the tables.  with_streams = false for problems that run
@@ -208,6 +305,7 @@ struct smgpu_problem {
       }
     }
     tt.npn_ent = tables.upload(ent);
+    if (precision != SMGPU_FP64) build_staged(rl);
     // signed coefficient tables
     const std::vector<double> vt2 = signed_vtab(T);
     if (precision == SMGPU_FP64) {
@@ -240,11 +338,13 @@ struct smgpu_problem {
     launch_hv_fp64(dt, tt, cfg, d_ep, d_en, c64, v, w, epi, s);
   }
   void hv(const float* v, double* w, const HvEpilogue<float>& epi, cudaStream_t s) {
-    launch_hv_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
+    if (cfg.staged) launch_hv_staged_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
+    else launch_hv_mixed(dt, tt, cfg, d_ep, d_en, c32, v, w, epi, s);
   }
   // FP32-mixed H·v with the Lanczos epilogue in double-float (w = wh + wl)
   void hv_df(const float* v, float* wh, float* wl, const HvEpilogue<float>& epi, cudaStream_t s) {
-    launch_hv_mixed_df(dt, tt, cfg, d_ep2, d_en2, c32, v, wh, wl, epi, s);
+    if (cfg.staged) launch_hv_staged_mixed_df(dt, tt, cfg, d_ep2, d_en2, c32, v, wh, wl, epi, s);
+    else launch_hv_mixed_df(dt, tt, cfg, d_ep2, d_en2, c32, v, wh, wl, epi, s);
   }
 
   // Time every candidate launch shape on a device vector and keep the fastest

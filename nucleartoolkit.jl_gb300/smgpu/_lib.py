@@ -50,6 +50,7 @@ SIGNATURES = {
     "smgpu_timings": (C.c_int, [_vp, _vp]),
     "smgpu_stats": (C.c_int, [_vp, _vp]),
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+    "smgpu_tune_report": (C.c_int, [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_int)]),
     "smgpu_matvec_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
     "smgpu_write_wav": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, C.c_int, _vp, _vp, _vp]),
     "smgpu_read_wav_header": (C.c_int, [C.c_char_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),

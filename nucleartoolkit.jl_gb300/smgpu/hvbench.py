@@ -61,6 +61,8 @@ def main():
     ms = P.time_matvec(reps=a.reps, flush_l2=not a.no_flush)
     out.update(mdim=int(getattr(P, "total_mdim", 0) or P.mdim), ms=ms)
     out.update(P.stats())
+    if hasattr(P, "tune_report"):
+        out["tune"] = P.tune_report()
     if a.nnz:
         if a.batch:
             b = a.nnz * 8 + 4 * (P.total_mdim + a.batch) + 2 * P.total_mdim * 4

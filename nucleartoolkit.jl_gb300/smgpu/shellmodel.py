@@ -77,11 +77,21 @@ class ShellModelProblem:
         return (ints, coef) if which in (2, 3) else ints
 
     def stats(self):
-        s = np.zeros(11, dtype=np.int64)
+        s = np.zeros(12, dtype=np.int64)
         check(load().smgpu_stats(self._h, _p(s)), self._h)
         keys = ["updates", "pn_proton_entries", "pn_neutron_entries", "pp_entries", "nn_entries", "table_bytes",
-                "len_pad", "links", "hv_threads", "hv_rows", "hv_min_ctas"]
+                "len_pad", "links", "hv_threads", "hv_rows", "hv_min_ctas", "hv_staged"]
         return dict(zip(keys, map(int, s)))
+
+    def tune_report(self):
+        """The H·v autotuner's candidates: list of dicts (threads, rows, min_ctas, staged, ms)."""
+        n = C.c_int(0)
+        check(load().smgpu_tune_report(self._h, 0, None, None, C.byref(n)), self._h)
+        shapes = np.zeros(4 * max(n.value, 1), dtype=np.int32)
+        ms = np.zeros(max(n.value, 1))
+        check(load().smgpu_tune_report(self._h, n.value, _p(shapes), _p(ms), C.byref(n)), self._h)
+        return [dict(threads=int(shapes[4 * k]), rows=int(shapes[4 * k + 1]), min_ctas=int(shapes[4 * k + 2]),
+                     staged=int(shapes[4 * k + 3]), ms=float(ms[k])) for k in range(n.value)]
 
     def timings(self):
         t = np.zeros(8)

@@ -133,6 +133,48 @@ def test_matvec_pf_full_size(lib, snt_dir):
     assert np.abs(M.matvec(v) - ref).max() <= MATVEC_MIXED_RTOL * scale
 
 
+@pytest.mark.parametrize("form", ["tile", "staged"])
+@pytest.mark.parametrize("case", ["ckpot_Be8", "usdb_Na21", "usdb_O19", "sd2p2n", "sd4p4n"])
+def test_matvec_mixed_each_kernel_form(lib, snt_dir, case, form, monkeypatch):
+    """Both FP32-mixed H·v kernels — the row-tile pull kernel and the staged
+    pn kernel — against the oracle's operate_H!, and the eigenvalues of a
+    solve that runs on the chosen kernel (its double-float epilogue)."""
+    snt, nuc = _cases(snt_dir)[case]
+    monkeypatch.setenv("SMGPU_HV_FORM", form)
+    O = _oracle(snt, nuc)
+    v = np.random.default_rng(11).standard_normal(O.mdim)
+    ref = O.operate_H(v)
+    M = _gpu(snt, nuc, 1)
+    assert M.stats()["hv_staged"] == (1 if form == "staged" else 0)
+    assert all(c["staged"] == (1 if form == "staged" else 0) for c in M.tune_report())
+    assert np.abs(M.matvec(v) - ref).max() <= MATVEC_MIXED_RTOL * np.abs(ref).max()
+    lm = min(40, O.mdim - 5)  # O19 has dimension 37
+    ro = O.trl(5, lm=lm, ls=15, tol=1e-8)
+    rm = M.solve(5, lm=lm, ls=15, tol=1e-8)
+    assert rm["converged"]
+    assert np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL
+
+
+@pytest.mark.parametrize("form", ["tile", "staged"])
+def test_matvec_mixed_each_kernel_form_pf(lib, snt_dir, form, monkeypatch):
+    """48Cr pf: each FP32-mixed H·v kernel against the FP64 kernel (which
+    equals the oracle to 1e-12, test_matvec_pf_full_size), on two vectors,
+    and the symmetry <u,Hv> = <Hu,v> of the mixed form."""
+    snt, nuc = snt_dir["pf4p4n"]
+    G = _gpu(snt, nuc, 0)
+    monkeypatch.setenv("SMGPU_HV_FORM", form)
+    M = _gpu(snt, nuc, 1)
+    assert M.stats()["hv_staged"] == (1 if form == "staged" else 0)
+    rng = np.random.default_rng(12)
+    u = rng.standard_normal(G.mdim)
+    v = rng.standard_normal(G.mdim)
+    ref = G.matvec(v)
+    w = M.matvec(v)
+    assert np.abs(w - ref).max() <= MATVEC_MIXED_RTOL * np.abs(ref).max()
+    hu = M.matvec(u)
+    assert abs(u @ w - hu @ v) <= 1e-6 * np.linalg.norm(u) * np.linalg.norm(w)
+
+
 def test_ckpot_known_answer_on_gpu(lib, golden):
     g = golden["ckpot_Be8"]
     for prec in (0, 1):
