@@ -206,43 +206,62 @@ __global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float,
   float ah = 0.f, al = 0.f;  // DF: α partial
   float bh = 0.f, bl = 0.f;  // DF: β
   if constexpr (DF) df_from_double(beta, bh, bl);
+  // pp and nn of all the thread's columns, entry-outer so that every entry
+  // issues one independent load per column (memory-level parallelism);
+  // FP32 partial sums, one compensated add per (row, column) each
+  float sp[R][QM], sn[R][QM];
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+#pragma unroll
+    for (int q = 0; q < QM; ++q) {
+      sp[r][q] = 0.f;
+      sn[r][q] = 0.f;
+    }
+  // pp: other proton rows of the block, same neutron column (coalesced)
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    if (r >= nr) break;
+    const int g = pst + p0 + r;
+    const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
+#pragma unroll 2
+    for (int k = kb; k < ke; ++k) {
+      const float pv = a.c.pp_val[k];
+      const float* __restrict__ src = v + blk + (int64_t)t.pp_col[k] * stride + tid;
+#pragma unroll
+      for (int q = 0; q < QM; ++q)
+        if (tid + q * NT < nn) sp[r][q] = __fmaf_rn(pv, src[q * NT], sp[r][q]);
+    }
+  }
+  // nn: same proton row, other neutron columns (ELL lists [k][n], rows of v
+  // in shared memory)
+  {
+    const int W = tt.nnell_w[b];
+    const int* __restrict__ ecol = tt.nnell_col + tt.nnell_off[b] + tid;
+    const float* __restrict__ eval = tt.nnell_val + tt.nnell_off[b] + tid;
+#pragma unroll 2
+    for (int k = 0; k < W; ++k) {
+#pragma unroll
+      for (int q = 0; q < QM; ++q) {
+        if (tid + q * NT < nn) {
+          const int c = ecol[(int64_t)k * nn + q * NT];
+          const float cv = eval[(int64_t)k * nn + q * NT];
+#pragma unroll
+          for (int r = 0; r < R; ++r)
+            if (r < nr) sn[r][q] = __fmaf_rn(cv, vrow[r * tt.nnmax + c], sn[r][q]);
+        }
+      }
+    }
+  }
 #pragma unroll
   for (int q = 0; q < QM; ++q) {
     const int n = tid + q * NT;
     if (n >= nn) continue;
     AccKahan acc[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) acc[r] = pn[r][q];
-    // nn: same proton row, other neutron columns (ELL lists, rows of v in
-    // shared memory); FP32 partial sums, one compensated add per row
-    {
-      const int W = tt.nnell_w[b];
-      const int* __restrict__ ecol = tt.nnell_col + tt.nnell_off[b] + n;
-      const float* __restrict__ eval = tt.nnell_val + tt.nnell_off[b] + n;
-      float sn[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) sn[r] = 0.f;
-#pragma unroll 4
-      for (int k = 0; k < W; ++k) {
-        const int c = ecol[(int64_t)k * nn];
-        const float cv = eval[(int64_t)k * nn];
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-          if (r < nr) sn[r] = __fmaf_rn(cv, vrow[r * tt.nnmax + c], sn[r]);
-      }
-#pragma unroll
-      for (int r = 0; r < R; ++r) acc[r].add(sn[r]);
-    }
-    // pp: other proton rows of the block, same neutron column (coalesced)
-#pragma unroll
     for (int r = 0; r < R; ++r) {
-      if (r >= nr) break;
-      const int g = pst + p0 + r;
-      const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
-      float sp = 0.f;
-#pragma unroll 4
-      for (int k = kb; k < ke; ++k) sp = __fmaf_rn(a.c.pp_val[k], v[blk + (int64_t)t.pp_col[k] * stride + n], sp);
-      acc[r].add(sp);
+      acc[r] = pn[r][q];
+      acc[r].add(sn[r][q]);
+      acc[r].add(sp[r][q]);
     }
     // one-body term, Lanczos epilogue, store
     if constexpr (DF) {

@@ -168,11 +168,24 @@ struct smgpu_problem {
       ymax = std::max(ymax, kw * nno);
       nbmax = std::max(nbmax, L.nB);
       if (L.nB >= (1 << 15)) return;
-      // source columns in descending order of their entry counts, so the
-      // lanes of a warp carry lists of about the same length
+      // source columns in descending order of their entry counts within
+      // windows of 128 consecutive columns: the lanes of a warp carry lists
+      // of about the same length, and a warp's loads of v stay inside four
+      // 128-byte lines
       std::vector<int> order(nns);
       for (int n = 0; n < nns; ++n) order[n] = n;
-      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cnt[x + 1] > cnt[y + 1]; });
+      for (int w0 = 0; w0 < nns; w0 += 128) {
+        std::stable_sort(order.begin() + w0, order.begin() + std::min(nns, w0 + 128),
+                         [&](int x, int y) { return cnt[x + 1] > cnt[y + 1]; });
+        // full windows: the four 32-column groups (longest first) rotate over
+        // the warps from window to window, so no warp always gets the longest
+        if (w0 + 128 <= nns) {
+          const int rot = (w0 / 128) % 4;
+          std::vector<int> win(order.begin() + w0, order.begin() + w0 + 128);
+          for (int g = 0; g < 4; ++g)
+            for (int l = 0; l < 32; ++l) order[w0 + ((g + rot) % 4) * 32 + l] = win[g * 32 + l];
+        }
+      }
       std::vector<int64_t> start(nns + 1, 0);  // entry offset of each source column (position order)
       std::vector<int> posof(nns);
       for (int i = 0; i < nns; ++i) {
@@ -194,6 +207,11 @@ struct smgpu_problem {
           const uint32_t slot = (uint32_t)((g - np_[n]) * nno + n);
           pent[base + pos[posof[src]]++] = slot | (ib << 16) | (sg << 31);
         }
+      // each list by operator index: lanes at the same position then tend to
+      // read the same or neighbouring coefficient rows (fewer bank conflicts)
+      for (int i = 0; i < nns; ++i)
+        std::sort(pent.begin() + base + start[i], pent.begin() + base + start[i + 1],
+                  [](uint32_t x, uint32_t y) { return ((x >> 16) & 0x7fffu) < ((y >> 16) & 0x7fffu); });
     }
     for (size_t k = 0; k + 1 < rl.size(); ++k) kmax = std::max(kmax, rl[k + 1] - rl[k]);
     // nn lists as ELL [k][n] per block
