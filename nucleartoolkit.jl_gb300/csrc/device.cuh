@@ -86,10 +86,12 @@ struct TileTables {
   const uint32_t* npn_ent; // n'<<14 | (sign*nA*nB + ib)
   // staged pn form (FP32-mixed): per link, the pull entries regrouped by
   // source neutron column ("push" lists).  Entry = slot | ib << 16 | sign << 31,
-  // slot = t * nn[b] + n' for the t-th pull entry of output column n'.
-  const int64_t* push_off;   // per link: offset of its nn[s]+1 list pointers in push_ptr / push_col
-  const int64_t* push_ptr;   // lists in descending order of length
-  const int* push_col;       // the source column of each list
+  // slot = t * nn[b] + n' for the t-th pull entry of output column n'.  The
+  // lists of a link are stored as an ELL array [k][position] (coalesced loads
+  // across a warp); position order = source columns sorted by list length.
+  const int64_t* push_off;   // per link: offset of its ELL array in push_ent
+  const int64_t* push_ioff;  // per link: offset of its nn[s] descriptors in push_info
+  const int* push_info;      // per position: source column | list length << 16
   const uint32_t* push_ent;
   // nn term of the staged kernel: per block, the nn pull lists as an ELL
   // array [k][n] (padded with zero coefficients on column n)

@@ -115,21 +115,21 @@ __global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float,
     __syncthreads();
     // stage 1: one thread per source column, columns in descending order of
     // list length; the entry loop stops at the warp's longest list
-    const int64_t* __restrict__ pptr = tt.push_ptr + tt.push_off[L];
-    const int* __restrict__ pcol = tt.push_col + tt.push_off[L];
+    const uint32_t* __restrict__ pell = tt.push_ent + tt.push_off[L];
+    const int* __restrict__ pinfo = tt.push_info + tt.push_ioff[L];
     for (int i0 = 0; i0 < nns; i0 += NT) {
       // every lane of the warp runs this loop body (the warp reductions need them all)
       const int i = i0 + tid;
       const bool act = i < nns;
-      const int n = act ? pcol[i] : 0;
-      const int64_t e0 = act ? pptr[i] : 0, e1 = act ? pptr[i + 1] : 0;
-      for (int64_t ec = e0;; ec += 16) {
-        const int ne = (int)max((int64_t)0, min((int64_t)16, e1 - ec));
+      const int info = act ? pinfo[i] : 0;
+      const int n = info & 0xffff, cnt = info >> 16;
+      for (int ec = 0;; ec += 16) {
+        const int ne = max(0, min(16, cnt - ec));
         const int kw = (int)__reduce_max_sync(0xffffffffu, (unsigned)ne);
         if (kw == 0) break;
         uint32_t ent[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) ent[k] = (k < ne) ? tt.push_ent[ec + k] : 0u;
+        for (int k = 0; k < 16; ++k) ent[k] = (k < ne) ? pell[(int64_t)(ec + k) * nns + i] : 0u;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if (r >= nr || kr[r] == 0) continue;

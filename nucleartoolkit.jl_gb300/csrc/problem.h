@@ -146,9 +146,9 @@ struct smgpu_problem {
   void build_staged(const std::vector<int>& rl) {
     tt.push_ent = nullptr;
     const size_t nl = T.links.size();
-    std::vector<int64_t> poff(nl), pptr;
-    std::vector<int> pcol;
-    std::vector<uint32_t> pent;
+    std::vector<int64_t> poff(nl), pioff(nl);
+    std::vector<int> pinfo;
+    std::vector<uint32_t> pell;
     int64_t ymax = 0;
     int nbmax = 0, kmax = 0;
     nnmax_raw = 0;
@@ -192,13 +192,8 @@ struct smgpu_problem {
         posof[order[i]] = i;
         start[i + 1] = start[i] + cnt[order[i] + 1];
       }
-      poff[li] = (int64_t)pptr.size();
-      const int64_t base = (int64_t)pent.size();
-      for (int i = 0; i <= nns; ++i) {
-        pptr.push_back(base + start[i]);
-        pcol.push_back(i < nns ? order[i] : 0);
-      }
-      pent.resize(base + start[nns]);
+      const int64_t base = 0;
+      std::vector<uint32_t> pent(start[nns]);
       std::vector<int64_t> pos(start.begin(), start.end() - 1);
       for (int n = 0; n < nno; ++n)
         for (int64_t g = np_[n]; g < np_[n + 1]; ++g) {
@@ -212,6 +207,18 @@ struct smgpu_problem {
       for (int i = 0; i < nns; ++i)
         std::sort(pent.begin() + base + start[i], pent.begin() + base + start[i + 1],
                   [](uint32_t x, uint32_t y) { return ((x >> 16) & 0x7fffu) < ((y >> 16) & 0x7fffu); });
+      // ELL [k][position] and the per-position descriptors
+      int64_t kwp = 0;
+      for (int i = 0; i < nns; ++i) kwp = std::max(kwp, start[i + 1] - start[i]);
+      if (nns >= 65536 || kwp >= 32768) return;
+      poff[li] = (int64_t)pell.size();
+      pioff[li] = (int64_t)pinfo.size();
+      pell.resize(pell.size() + (size_t)kwp * nns, 0u);
+      for (int i = 0; i < nns; ++i) {
+        const int64_t c = start[i + 1] - start[i];
+        pinfo.push_back(order[i] | (int)(c << 16));
+        for (int64_t k = 0; k < c; ++k) pell[poff[li] + k * nns + i] = pent[start[i] + k];
+      }
     }
     for (size_t k = 0; k + 1 < rl.size(); ++k) kmax = std::max(kmax, rl[k + 1] - rl[k]);
     // nn lists as ELL [k][n] per block
@@ -240,9 +247,9 @@ struct smgpu_problem {
     tt.nnell_col = tables.upload(ecol);
     tt.nnell_val = tables.upload(evl);
     tt.push_off = tables.upload(poff);
-    tt.push_ptr = tables.upload(pptr);
-    tt.push_col = tables.upload(pcol);
-    tt.push_ent = tables.upload(pent);
+    tt.push_ioff = tables.upload(pioff);
+    tt.push_info = tables.upload(pinfo);
+    tt.push_ent = tables.upload(pell);
     tt.ymax = (int)((ymax + 3) & ~(int64_t)3);
     tt.nnmax = (nnmax_raw + 3) & ~3;
     tt.nbmax = std::max(nbmax, 1);
