@@ -282,6 +282,7 @@ struct Solve {
     L.cvec = A.alloc<double>(ls);
     L.sc = A.alloc<LanczosScalars>(1);
     L.fl = A.alloc<LanczosFlags>(1);
+    L.alpha_df = sizeof(TX) == 4 ? 1 : 0;  // the FP32-mixed solve runs the double-float H·v epilogue
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(TX) * (size_t)lm * L.len, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * L.len, P->st));
     // the padding slots of the double-float residual are never written by H·v

@@ -306,13 +306,22 @@ __global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float,
   if (a.alpha_part != nullptr) {
     __shared__ double red[NT / 32];
     if constexpr (DF) {
+      // double-float all the way; the partial is stored as a (hi, lo) pair
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float oh = __shfl_down_sync(0xffffffffu, ah, o);
         const float ol = __shfl_down_sync(0xffffffffu, al, o);
         df_add(ah, al, oh, ol);
       }
-      apart = (double)ah + (double)al;
+      float2* r2 = reinterpret_cast<float2*>(red);
+      if ((tid & 31) == 0) r2[tid >> 5] = make_float2(ah, al);
+      __syncthreads();
+      if (tid == 0) {
+        float h = r2[0].x, l = r2[0].y;
+        for (int k = 1; k < NT / 32; ++k) df_add(h, l, r2[k].x, r2[k].y);
+        reinterpret_cast<float2*>(a.alpha_part)[task] = make_float2(h, l);
+      }
+      return;
     } else {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) apart += __shfl_down_sync(0xffffffffu, apart, o);

@@ -54,7 +54,8 @@ constexpr int KMAX = 16;
 // explicit arguments).  vprev: three-term correction w -= beta*vprev (null:
 // none); alpha_out: where the CTA's partial of v·Hv goes (null: none).
 // DF = true (FP32 v, Kahan accumulation): the epilogue runs in double-float
-// and writes w as the pair (a.wh, a.wl); the α partial is returned in FP64.
+// and writes w as the pair (a.wh, a.wl); the α partial is stored as a
+// double-float (hi, lo) float pair in the FP64 slot.
 template <class TV, class TC, class Acc, int NT, int R, bool DF = false>
 __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* __restrict__ v, double* w,
                                              const TV* vprev, const int b, const int p0, const double beta,
@@ -223,14 +224,22 @@ __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* 
   if (alpha_out != nullptr) {
     __shared__ double red[NT / 32];
     if constexpr (DF) {
-      // warp sums in double-float (FP32 pipe), one FP64 value per warp
+      // double-float all the way; the partial is stored as a (hi, lo) pair
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float oh = __shfl_down_sync(0xffffffffu, ah, o);
         const float ol = __shfl_down_sync(0xffffffffu, al, o);
         df_add(ah, al, oh, ol);
       }
-      apart = (double)ah + (double)al;
+      float2* r2 = reinterpret_cast<float2*>(red);
+      if ((threadIdx.x & 31) == 0) r2[threadIdx.x >> 5] = make_float2(ah, al);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        float h = r2[0].x, l = r2[0].y;
+        for (int k = 1; k < NT / 32; ++k) df_add(h, l, r2[k].x, r2[k].y);
+        *reinterpret_cast<float2*>(alpha_out) = make_float2(h, l);
+      }
+      return;
     } else {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) apart += __shfl_down_sync(0xffffffffu, apart, o);

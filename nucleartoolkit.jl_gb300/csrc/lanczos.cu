@@ -304,7 +304,10 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
 // ---------------------------------------- FP32 basis, double-float residual
 // The FP32-mixed solve keeps w = wh + wl as a double-float pair: every
 // vector-length operation below runs on the FP32 pipe (exact FP32 products
-// by fused two-products, sums in double-float); only per-CTA scalars are FP64.
+// by fused two-products, sums in double-float), and so do the CTA reductions
+// and the per-CTA partials (stored as (hi, lo) float pairs in the FP64 partial
+// arrays, α partials of the H·v epilogue included); FP64 is left to one
+// thread's scalar work (β, the second-pass test).
 // 512-thread CTAs, two per SM: the streams need the memory-level parallelism.
 constexpr int kONT = 512;
 
@@ -317,9 +320,9 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_dot_df(const float* __restrict
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kONT / 32];
   __shared__ double red8[(kONT / 32) * 8];
-  const double alpha = sum_partials<kONT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
-  float aH, aL;
-  df_from_double(-alpha, aH, aL);
+  const float2 alpha = sum_partials_df<kONT>(reinterpret_cast<const float2*>(alpha_part) + (int64_t)it0 * nalpha,
+                                             nalpha, reinterpret_cast<float2*>(red));
+  const float aH = -alpha.x, aL = -alpha.y;
   const float* __restrict__ vk = V + (int64_t)it0 * ld;
   const int m = it0 + 1;
   int64_t cb, ce;
@@ -356,9 +359,10 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_dot_df(const float* __restrict
         }
       }
     }
-    double s;
+    float2 s;
     block_sum_df<kONT, 8>(acc, red8, s);
-    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m) pdot[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m)
+      reinterpret_cast<float2*>(pdot)[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
   }
 }
 
@@ -367,11 +371,9 @@ __device__ __forceinline__ void orth_subtract_df(const float* __restrict__ V, in
                                                  float* __restrict__ wh, float* __restrict__ wl,
                                                  const double* __restrict__ ph, double* __restrict__ pout, int G,
                                                  double* hs, double* red) {
-  sum_partials_many<kONT>(ph, G, m, hs);
   float* hh = reinterpret_cast<float*>(hs + m + 2);
   float* hl = hh + m;
-  for (int j = threadIdx.x; j < m; j += kONT) df_from_double(hs[j], hh[j], hl[j]);
-  __syncthreads();
+  sum_partials_many_df<kONT>(reinterpret_cast<const float2*>(ph), G, m, hh, hl);
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
   DFAcc nrm;
@@ -400,9 +402,9 @@ __device__ __forceinline__ void orth_subtract_df(const float* __restrict__ V, in
     *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
   }
   DFAcc n1[1] = {nrm};
-  double s;
+  float2 s;
   block_sum_df<kONT, 1>(n1, red, s);
-  if (threadIdx.x == 0) pout[blockIdx.x] = s;
+  if (threadIdx.x == 0) reinterpret_cast<float2*>(pout)[blockIdx.x] = s;
 }
 
 __global__ void __launch_bounds__(kONT, 2) k_orth_axpy_df(const float* __restrict__ V, int64_t ld, int it0, float* wh,
@@ -415,16 +417,18 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_axpy_df(const float* __restric
   const int m = it0 + 1;
   if (blockIdx.x == 0) {
     // ||w − α v_k||² (slot m of the first-pass partials), for the second-pass test
-    const double n0 = sum_partials<kONT>(pdot + (int64_t)m * G, G, red);
-    if (threadIdx.x == 0) sc->w_norm2 = n0;
+    const float2 n0 = sum_partials_df<kONT>(reinterpret_cast<const float2*>(pdot) + (int64_t)m * G, G,
+                                            reinterpret_cast<float2*>(red));
+    if (threadIdx.x == 0) sc->w_norm2 = (double)n0.x + (double)n0.y;
   }
   orth_subtract_df(V, ld, m, wh, wl, pdot, pn1, G, hs, red);
 }
 
 // Second-pass decision of the double-float solve: ||w''||² < ||w'||² / 2.
+// The sum in double-float; one thread compares in FP64 and broadcasts.
 __device__ __forceinline__ bool need_second_df(const LanczosScalars* sc, const double* pn1, int G, double* red) {
-  const double n1 = sum_partials<kONT>(pn1, G, red);
-  return n1 < 0.5 * sc->w_norm2;
+  const float2 n1 = sum_partials_df<kONT>(reinterpret_cast<const float2*>(pn1), G, reinterpret_cast<float2*>(red));
+  return cta_gate(threadIdx.x == 0 && (double)n1.x + (double)n1.y < 0.5 * sc->w_norm2);
 }
 
 __global__ void __launch_bounds__(kONT, 2) k_orth_dot2_df(const float* __restrict__ V, int64_t ld, int it0,
@@ -456,9 +460,10 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_dot2_df(const float* __restric
           acc[q].add_prod2(x.w, a.w, b.w);
         }
     }
-    double s;
+    float2 s;
     block_sum_df<kONT, 8>(acc, red8, s);
-    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m) pdot2[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m)
+      reinterpret_cast<float2*>(pdot2)[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
   }
 }
 
@@ -482,26 +487,32 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_scale_df(const float* __restri
                                                        int lm, int64_t len, LanczosScalars* sc, LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kONT / 32];
+  __shared__ float s_inv[2];
   const bool second = need_second_df(sc, pn1, G, red);
-  const double nrm = sum_partials<kONT>(second ? pn2 : pn1, G, red);
-  const double beta = sqrt(nrm);
-  const bool ok = (beta > 0.0) && (beta < INFINITY);
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (ok) {
-      T[(int64_t)it0 * lm + it0 + 1] = beta;
-      T[(int64_t)(it0 + 1) * lm + it0] = beta;
-      sc->beta = beta;
-      sc->inv_beta = 1.0 / beta;
-      fl->second = second ? 1 : 0;
-      if (second) fl->n_second += 1;
-    } else {
-      fl->exh_k = it0 + 1;
-      fl->exhausted = 1;
+  const float2 nrm =
+      sum_partials_df<kONT>(reinterpret_cast<const float2*>(second ? pn2 : pn1), G, reinterpret_cast<float2*>(red));
+  // β and 1/β by one thread (FP64), broadcast as a double-float pair
+  bool ok0 = false;
+  if (threadIdx.x == 0) {
+    const double beta = sqrt((double)nrm.x + (double)nrm.y);
+    ok0 = (beta > 0.0) && (beta < INFINITY);
+    if (blockIdx.x == 0) {
+      if (ok0) {
+        T[(int64_t)it0 * lm + it0 + 1] = beta;
+        T[(int64_t)(it0 + 1) * lm + it0] = beta;
+        sc->beta = beta;
+        sc->inv_beta = 1.0 / beta;
+        fl->second = second ? 1 : 0;
+        if (second) fl->n_second += 1;
+      } else {
+        fl->exh_k = it0 + 1;
+        fl->exhausted = 1;
+      }
     }
+    if (ok0) df_from_double(1.0 / beta, s_inv[0], s_inv[1]);
   }
-  if (!ok) return;
-  float ih, il;
-  df_from_double(1.0 / beta, ih, il);
+  if (!cta_gate(ok0)) return;
+  const float ih = s_inv[0], il = s_inv[1];
   for (int64_t i = 4 * (blockIdx.x * (int64_t)kONT + threadIdx.x); i < len; i += 4 * (int64_t)gridDim.x * kONT) {
     const float4 h = *reinterpret_cast<const float4*>(wh + i);
     const float4 l = *reinterpret_cast<const float4*>(wl + i);
@@ -518,7 +529,7 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_scale_df(const float* __restri
 // H·v epilogue partials, then sturm_step.
 __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num_ev, double* en, int nh,
                         double tol, int64_t mdim, const double* __restrict__ alpha_part, int nalpha,
-                        LanczosFlags* fl) {
+                        int alpha_df, LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && fl->done)) return;
   if (cta_gate(threadIdx.x == 0 && fl->exhausted && k > fl->exh_k)) {
     // the Krylov space ended at exh_k; T_k was never completed
@@ -530,7 +541,12 @@ __global__ void k_sturm(double* __restrict__ T, int lm, int k, int lock, int num
   // α of this iteration from the H·v epilogue partials
   {
     double x = 0.0;
-    for (int i = tid; i < nalpha; i += blockDim.x) x += alpha_part[(int64_t)(k - 1) * nalpha + i];
+    if (alpha_df) {  // double-float (hi, lo) partials of the FP32-mixed H·v
+      const float2* ap = reinterpret_cast<const float2*>(alpha_part) + (int64_t)(k - 1) * nalpha;
+      for (int i = tid; i < nalpha; i += blockDim.x) x += (double)ap[i].x + (double)ap[i].y;
+    } else {
+      for (int i = tid; i < nalpha; i += blockDim.x) x += alpha_part[(int64_t)(k - 1) * nalpha + i];
+    }
     x = warp_sum(x);
     if ((tid & 31) == 0) red[tid >> 5] = x;
     __syncthreads();
@@ -880,7 +896,7 @@ void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
   if (threads < 32) threads = 32;
   size_t shm = sizeof(double) * (3 * (size_t)L.lm + L.num_ev);
   k_sturm<<<1, threads, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.alpha_part, L.nalpha,
-                                   L.fl);
+                                   L.alpha_df, L.fl);
 }
 void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaStream_t st) {
   const size_t shm = jacobi_smem_bytes(n);

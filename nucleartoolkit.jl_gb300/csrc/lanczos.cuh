@@ -39,6 +39,7 @@ struct LanczosDev {
   double* cvec;         // ls
   LanczosScalars* sc;
   LanczosFlags* fl;
+  int alpha_df;         // 1: alpha_part holds double-float (hi, lo) float pairs (FP32-mixed H·v)
 };
 
 void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st);

@@ -526,13 +526,15 @@ struct DFAcc {
   __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
 };
 
-// Sums of NQ double-float accumulators over a CTA: warp shuffles in
-// double-float on the FP32 pipe, one FP64 sum of the warp totals per value
-// (GB300 runs FP64 adds at a small fraction of the FP32 rate).  Thread q < NQ
-// gets value q in *out; red holds (NT/32)*NQ doubles.
+// Sums of NQ double-float accumulators over a CTA, all on the FP32 pipe
+// (warp shuffles and the sum of the warp totals in double-float; on GB300
+// even a handful of dependent FP64 adds per CTA costs microseconds).  Thread
+// q < NQ gets value q as an unevaluated (hi, lo) pair in *out; red holds
+// (NT/32)*NQ doubles of shared memory (used as float2).
 template <int NT, int NQ>
-__device__ __forceinline__ void block_sum_df(DFAcc (&acc)[NQ], double* red, double& out) {
+__device__ __forceinline__ void block_sum_df(DFAcc (&acc)[NQ], double* red, float2& out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2* r2 = reinterpret_cast<float2*>(red);
 #pragma unroll
   for (int q = 0; q < NQ; ++q) {
     float h = acc[q].hi, l = acc[q].lo;
@@ -548,12 +550,76 @@ __device__ __forceinline__ void block_sum_df(DFAcc (&acc)[NQ], double* red, doub
   __syncthreads();
   if (lane == 0) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) red[wid * NQ + q] = (double)acc[q].hi + (double)acc[q].lo;
+    for (int q = 0; q < NQ; ++q) r2[wid * NQ + q] = make_float2(acc[q].hi, acc[q].lo);
   }
   __syncthreads();
-  out = 0.0;
-  if (threadIdx.x < NQ)
-    for (int k = 0; k < NT / 32; ++k) out += red[k * NQ + threadIdx.x];
+  out = make_float2(0.f, 0.f);
+  if (threadIdx.x < NQ) {
+    float h = 0.f, l = 0.f;
+    for (int k = 0; k < NT / 32; ++k) {
+      const float2 x = r2[k * NQ + threadIdx.x];
+      df_add(h, l, x.x, x.y);
+    }
+    out = make_float2(h, l);
+  }
+}
+
+// Double-float sum over a CTA on the FP32 pipe; every thread gets the same
+// (hi, lo).  red: NT/32 float2 of shared memory.
+template <int NT>
+__device__ __forceinline__ float2 block_sum_df2(float h, float l, float2* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+    df_add(h, l, oh, ol);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[wid] = make_float2(h, l);
+  __syncthreads();
+  float sh = red[0].x, sl = red[0].y;
+#pragma unroll
+  for (int k = 1; k < NT / 32; ++k) df_add(sh, sl, red[k].x, red[k].y);
+  return make_float2(sh, sl);
+}
+
+// Sum of n double-float partials (float2 pairs) in a fixed order, every
+// thread gets the same value.
+template <int NT>
+__device__ __forceinline__ float2 sum_partials_df(const float2* __restrict__ p, int n, float2* red) {
+  float h = 0.f, l = 0.f;
+  for (int i = threadIdx.x; i < n; i += NT) {
+    const float2 x = p[i];
+    df_add(h, l, x.x, x.y);
+  }
+  return block_sum_df2<NT>(h, l, red);
+}
+
+// m sums of G double-float partials each (one warp per sum), results as
+// (hi, lo) into shared hh[j], hl[j].
+template <int NT>
+__device__ __forceinline__ void sum_partials_many_df(const float2* __restrict__ p, int G, int m, float* hh,
+                                                     float* hl) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < m; j += NT / 32) {
+    float h = 0.f, l = 0.f;
+    for (int g = lane; g < G; g += 32) {
+      const float2 x = p[(int64_t)j * G + g];
+      df_add(h, l, x.x, x.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+      df_add(h, l, oh, ol);
+    }
+    if (lane == 0) {
+      hh[j] = h;
+      hl[j] = l;
+    }
+  }
+  __syncthreads();
 }
 
 // x = hi + lo with hi = x rounded to FP32 and lo the FP32 rounding of the rest.
