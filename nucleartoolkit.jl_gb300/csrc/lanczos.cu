@@ -327,10 +327,15 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_dot_df(const float* __restrict
   const int m = it0 + 1;
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
-  for (int j0 = 0; j0 <= m; j0 += 8) {
-    DFAcc acc[8];
+  // blocks of 16 basis vectors per pass over the chunk.  The per-thread sums
+  // are FP32 (a thread adds ~16 products of one chunk; the rounding they
+  // leave in h_j is ~1e-10 ||w||, far below the FP32 basis itself), the CTA
+  // sums double-float.
+  constexpr int JB = 16;
+  for (int j0 = 0; j0 <= m; j0 += JB) {
+    float acc[JB];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q].init();
+    for (int q = 0; q < JB; ++q) acc[q] = 0.f;
     for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kONT) {
       const float4 a = *reinterpret_cast<const float4*>(wh + i);
       const float4 b = *reinterpret_cast<const float4*>(wl + i);
@@ -345,24 +350,30 @@ __global__ void __launch_bounds__(kONT, 2) k_orth_dot_df(const float* __restrict
         *reinterpret_cast<float4*>(wl + i) = make_float4(l[0], l[1], l[2], l[3]);
       }
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
+      for (int q = 0; q < JB; ++q) {
         const int j = j0 + q;
         if (j < m) {
           const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * ld + i);
-          acc[q].add_prod2(x.x, h[0], l[0]);
-          acc[q].add_prod2(x.y, h[1], l[1]);
-          acc[q].add_prod2(x.z, h[2], l[2]);
-          acc[q].add_prod2(x.w, h[3], l[3]);
+          acc[q] = __fmaf_rn(x.w, h[3], __fmaf_rn(x.z, h[2], __fmaf_rn(x.y, h[1], __fmaf_rn(x.x, h[0], acc[q]))));
         } else if (j == m) {
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
+          acc[q] = __fmaf_rn(h[3], h[3], __fmaf_rn(h[2], h[2], __fmaf_rn(h[1], h[1], __fmaf_rn(h[0], h[0], acc[q]))));
         }
       }
     }
-    float2 s;
-    block_sum_df<kONT, 8>(acc, red8, s);
-    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m)
-      reinterpret_cast<float2*>(pdot)[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
+#pragma unroll
+    for (int g = 0; g < JB / 8; ++g) {
+      if (j0 + 8 * g > m) break;
+      DFAcc d[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        d[q].hi = acc[8 * g + q];
+        d[q].lo = 0.f;
+      }
+      float2 s;
+      block_sum_df<kONT, 8>(d, red8, s);
+      const int j = j0 + 8 * g + (int)threadIdx.x;
+      if (threadIdx.x < 8 && j <= m) reinterpret_cast<float2*>(pdot)[(int64_t)j * G + blockIdx.x] = s;
+    }
   }
 }
 
@@ -632,6 +643,168 @@ __global__ void __launch_bounds__(kNT) k_restart_rotate(const TX* __restrict__ V
           if (k0 + q < ls) U[(int64_t)(k0 + q) * len + i] = (TX)acc[q];
       }
     }
+  }
+}
+
+// FP32-mixed forms of the restart streams: every basis vector is read once,
+// products compensated (Kahan with the product inside the fused step).
+//   rotate: U_k = Σ_{j<m} Y[j,k] V_j, one element per thread, all ls outputs
+//           in registers, Y broadcast from shared memory (rows padded to 16).
+constexpr int kRLS = 16;  // largest ls of the register-resident restart kernels
+__global__ void __launch_bounds__(kNT) k_restart_rotate_f(const float* __restrict__ V, float* __restrict__ U,
+                                                          const float* __restrict__ Yf, int m, int ls, int64_t len,
+                                                          const LanczosFlags* __restrict__ fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  extern __shared__ float ys[];  // m x kRLS: ys[j*kRLS + k] = Y[j,k]
+  for (int idx = threadIdx.x; idx < m * kRLS; idx += kNT) {
+    const int j = idx / kRLS, k = idx % kRLS;
+    ys[idx] = k < ls ? Yf[(int64_t)k * m + j] : 0.f;
+  }
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    KahanF acc[kRLS];
+#pragma unroll
+    for (int k = 0; k < kRLS; ++k) acc[k].init();
+    int j = 0;
+    for (; j + 4 <= m; j += 4) {
+      float x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = V[(int64_t)(j + u) * len + i];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4* y4 = reinterpret_cast<const float4*>(ys + (j + u) * kRLS);
+#pragma unroll
+        for (int q = 0; q < kRLS / 4; ++q) {
+          const float4 y = y4[q];
+          acc[4 * q].add_prod(y.x, x[u]);
+          acc[4 * q + 1].add_prod(y.y, x[u]);
+          acc[4 * q + 2].add_prod(y.z, x[u]);
+          acc[4 * q + 3].add_prod(y.w, x[u]);
+        }
+      }
+    }
+    for (; j < m; ++j) {
+      const float x = V[(int64_t)j * len + i];
+      const float4* y4 = reinterpret_cast<const float4*>(ys + j * kRLS);
+#pragma unroll
+      for (int q = 0; q < kRLS / 4; ++q) {
+        const float4 y = y4[q];
+        acc[4 * q].add_prod(y.x, x);
+        acc[4 * q + 1].add_prod(y.y, x);
+        acc[4 * q + 2].add_prod(y.z, x);
+        acc[4 * q + 3].add_prod(y.w, x);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kRLS; ++k)
+      if (k < ls) U[(int64_t)k * len + i] = acc[k].get();
+  }
+}
+
+//   apply: V_k = Σ_{j<=k} X[j,k] U_j, V_ls = V_{lm-1} − Σ_k c_k V_k; the ls
+//          values of U in registers.
+__global__ void __launch_bounds__(kNT) k_restart_apply_f(const float* __restrict__ U, float* __restrict__ V,
+                                                         const double* __restrict__ X,
+                                                         const double* __restrict__ cvec, int ls, int lm,
+                                                         int64_t len, const LanczosFlags* __restrict__ fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  __shared__ float xf[kRLS * kRLS + kRLS];
+  for (int idx = threadIdx.x; idx < ls * ls; idx += kNT) xf[idx] = (float)X[idx];
+  for (int idx = threadIdx.x; idx < ls; idx += kNT) xf[ls * ls + idx] = (float)cvec[idx];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
+    float u[kRLS];
+#pragma unroll
+    for (int j = 0; j < kRLS; ++j) u[j] = j < ls ? U[(int64_t)j * len + i] : 0.f;
+    KahanF last;
+    last.init();
+    last.add(V[(int64_t)(lm - 1) * len + i]);
+#pragma unroll
+    for (int k = 0; k < kRLS; ++k) {
+      if (k >= ls) break;
+      KahanF q;
+      q.init();
+#pragma unroll
+      for (int j = 0; j <= k; ++j) q.add_prod(xf[k * ls + j], u[j]);
+      const float qv = q.get();
+      V[(int64_t)k * len + i] = qv;
+      last.add_prod(-xf[ls * ls + k], qv);
+    }
+    V[(int64_t)ls * len + i] = last.get();
+  }
+}
+
+//   Gram: tiles of 128 elements of the ls+1 vectors staged in shared memory,
+//         double-buffered through registers (the next tile's loads are in
+//         flight while the current one is multiplied); one thread per pair,
+//         double-float sums, partials as (hi, lo) pairs.
+__global__ void __launch_bounds__(kNT) k_gram_f(const float* __restrict__ U, const float* __restrict__ vl, int ls,
+                                                int64_t len, double* __restrict__ partials, int G,
+                                                const LanczosFlags* __restrict__ fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  constexpr int TILE = 128;
+  constexpr int TS = TILE + 1;
+  constexpr int LD = ((kRLS + 1) * TILE + kNT - 1) / kNT;  // elements a thread stages per tile
+  extern __shared__ float gt[];                 // 2 x (ls+1) x TS
+  const int nv = ls + 1;
+  const int P = ls * (ls + 1) / 2 + ls;
+  int64_t cb, ce;
+  chunk_of(len, G, cb, ce);
+  int k = 0, l = 0;
+  const bool act = (int)threadIdx.x < P;
+  if (act) gram_pair(threadIdx.x, ls, k, l);
+  DFAcc acc;
+  acc.init();
+  float st[LD];
+  auto load = [&](int64_t t0) {
+#pragma unroll
+    for (int u = 0; u < LD; ++u) {
+      const int idx = threadIdx.x + u * kNT;
+      const int j = idx / TILE, x = idx % TILE;
+      float val = 0.f;
+      if (j < nv && t0 + x < ce) val = (j < ls) ? U[(int64_t)j * len + t0 + x] : vl[t0 + x];
+      st[u] = val;
+    }
+  };
+  auto store = [&](int buf) {
+    float* tl = gt + buf * nv * TS;
+#pragma unroll
+    for (int u = 0; u < LD; ++u) {
+      const int idx = threadIdx.x + u * kNT;
+      const int j = idx / TILE, x = idx % TILE;
+      if (j < nv) tl[j * TS + x] = st[u];
+    }
+  };
+  int buf = 0;
+  if (cb < ce) {
+    load(cb);
+    store(0);
+  }
+  __syncthreads();
+  for (int64_t t0 = cb; t0 < ce; t0 += TILE) {
+    const bool more = t0 + TILE < ce;
+    if (more) load(t0 + TILE);
+    const float* tl = gt + buf * nv * TS;
+    if (act) {
+      const int cnt = (int)min((int64_t)TILE, ce - t0);
+      for (int x = 0; x < cnt; ++x) acc.add_prod(tl[k * TS + x], tl[l * TS + x]);
+    }
+    if (more) store(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+  if (act) reinterpret_cast<float2*>(partials)[(int64_t)threadIdx.x * G + blockIdx.x] = make_float2(acc.hi, acc.lo);
+}
+
+__global__ void __launch_bounds__(kNT) k_gram_reduce_f(const double* __restrict__ partials, int G, int P,
+                                                       double* __restrict__ out, const LanczosFlags* fl) {
+  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  __shared__ float hh[1024], hl[1024];
+  for (int j0 = 0; j0 < P; j0 += 1024) {
+    const int mm = min(1024, P - j0);
+    sum_partials_many_df<kNT>(reinterpret_cast<const float2*>(partials) + (int64_t)j0 * G, G, mm, hh, hl);
+    for (int j = threadIdx.x; j < mm; j += kNT) out[j0 + j] = (double)hh[j] + (double)hl[j];
+    __syncthreads();
   }
 }
 
@@ -911,21 +1084,40 @@ void launch_restart_small(const LanczosDev& L, cudaStream_t st) {
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st) {
   int m = L.lm - 1;
+  if constexpr (sizeof(TX) == 4) {
+    if (L.ls <= kRLS && sizeof(float) * (size_t)m * kRLS <= 48 * 1024) {
+      k_restart_rotate_f<<<grid_for(L.len), kNT, sizeof(float) * m * kRLS, st>>>(V, U, L.Yf, m, L.ls, L.len, L.fl);
+      return;
+    }
+  }
   k_restart_rotate<TX><<<grid_for(L.len), kNT, 0, st>>>(V, U, L.jacA, L.Yf, m, L.ls, L.len, L.fl);
 }
 template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
+  if constexpr (sizeof(TX) == 4) {
+    if (L.ls <= kRLS && L.ls * (L.ls + 1) / 2 + L.ls <= kNT) {
+      k_gram_f<<<L.G, kNT, sizeof(float) * 2 * (L.ls + 1) * 129, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
+      return;
+    }
+  }
   k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 65, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
 }
-void launch_gram_reduce(const LanczosDev& L, cudaStream_t st) {
+void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st) {
   const int P = L.ls * (L.ls + 1) / 2 + L.ls;
-  k_gram_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, P, L.gram, L.fl);
+  if (df && L.ls <= kRLS && P <= kNT) k_gram_reduce_f<<<1, kNT, 0, st>>>(L.partials, L.G, P, L.gram, L.fl);
+  else k_gram_reduce<<<1, kNT, 0, st>>>(L.partials, L.G, P, L.gram, L.fl);
 }
 void launch_chol(const LanczosDev& L, cudaStream_t st) {
   k_chol<<<1, 32, sizeof(double) * L.ls * L.ls, st>>>(L.gram, L.ls, L.X, L.cvec, L.fl);
 }
 template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st) {
+  if constexpr (sizeof(TX) == 4) {
+    if (L.ls <= kRLS) {
+      k_restart_apply_f<<<grid_for(L.len), kNT, 0, st>>>(U, V, L.X, L.cvec, L.ls, L.lm, L.len, L.fl);
+      return;
+    }
+  }
   k_restart_apply<TX><<<grid_for(L.len), kNT, (sizeof(double) + sizeof(float)) * (L.ls * L.ls + L.ls), st>>>(
       U, V, L.X, L.cvec, L.ls,
                                                                                              L.lm, L.len, L.fl);

@@ -64,7 +64,8 @@ template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st);
 template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st);
-void launch_gram_reduce(const LanczosDev& L, cudaStream_t st);
+// df: the partials of the FP32-basis Gram kernel ((hi, lo) pairs)
+void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st);
 void launch_chol(const LanczosDev& L, cudaStream_t st);
 template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st);

@@ -105,6 +105,13 @@ struct KahanF {
     c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
   }
+  // += a·b, the product rounded once inside the compensated step
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float y = __fmaf_rn(a, b, -c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
   __device__ __forceinline__ float get() const { return __fsub_rn(s, c); }
 };
 
