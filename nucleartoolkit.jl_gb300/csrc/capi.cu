@@ -338,7 +338,7 @@ struct Solve {
     launch_restart_rotate<TX>(L, V, U, s);
     launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, s);
     launch_gram_reduce(L, sizeof(TX) == 4, s);
-    launch_chol(L, s);
+    launch_chol(L, sizeof(TX) == 4, s);
     launch_restart_apply<TX>(L, U, V, s);
   }
 

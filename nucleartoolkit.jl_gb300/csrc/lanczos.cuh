@@ -66,7 +66,8 @@ template <class TX>
 void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st);
 // df: the partials of the FP32-basis Gram kernel ((hi, lo) pairs)
 void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st);
-void launch_chol(const LanczosDev& L, cudaStream_t st);
+// df: the double-float form on one warp (FP32-mixed solves, ls <= 32)
+void launch_chol(const LanczosDev& L, bool df, cudaStream_t st);
 template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st);
 template <class TX>

@@ -596,6 +596,7 @@ __device__ __forceinline__ float2 block_sum_df2(float h, float l, float2* red) {
 template <int NT>
 __device__ __forceinline__ float2 sum_partials_df(const float2* __restrict__ p, int n, float2* red) {
   float h = 0.f, l = 0.f;
+#pragma unroll 4
   for (int i = threadIdx.x; i < n; i += NT) {
     const float2 x = p[i];
     df_add(h, l, x.x, x.y);
@@ -611,6 +612,7 @@ __device__ __forceinline__ void sum_partials_many_df(const float2* __restrict__ 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < m; j += NT / 32) {
     float h = 0.f, l = 0.f;
+#pragma unroll 4
     for (int g = lane; g < G; g += 32) {
       const float2 x = p[(int64_t)j * G + g];
       df_add(h, l, x.x, x.y);
