@@ -907,101 +907,14 @@ __global__ void k_chol(const double* __restrict__ gram, int ls, double* X, doubl
   }
 }
 
-// The same Cholesky and inverse in double-float arithmetic on one warp (FP32
-// pipe; the single-thread FP64 form above is latency-bound on GB300's FP64
-// unit).  Right-looking factorisation with the lanes over the columns of the
-// trailing update; the inverse by back substitution, one column per lane.
-// ls <= 32.  Division and square root: an FP32 estimate and one Newton
-// correction in double-float.
-__device__ __forceinline__ float2 dfw_sub(float2 a, float2 b) {
-  df_add(a.x, a.y, -b.x, -b.y);
-  return a;
-}
-__device__ __forceinline__ float2 dfw_mul(float2 a, float2 b) {
-  float h, l;
-  df_mul(a.x, a.y, b.x, b.y, h, l);
-  return make_float2(h, l);
-}
-__device__ __forceinline__ float2 dfw_div(float2 a, float2 b) {
-  const float q1 = __fdiv_rn(a.x, b.x);
-  const float2 r = dfw_sub(a, dfw_mul(make_float2(q1, 0.f), b));
-  const float q2 = __fdiv_rn(r.x, b.x);
-  float h, l;
-  fast_two_sum(q1, q2, h, l);
-  return make_float2(h, l);
-}
-__device__ __forceinline__ float2 dfw_sqrt(float2 a) {
-  const float s = __fsqrt_rn(a.x);
-  const float2 r = dfw_sub(a, dfw_mul(make_float2(s, 0.f), make_float2(s, 0.f)));
-  float h, l;
-  fast_two_sum(s, __fdiv_rn(r.x, 2.f * s), h, l);
-  return make_float2(h, l);
-}
+// The same Cholesky and inverse in double-float on one warp (chol_df_warp).
 __global__ void __launch_bounds__(32) k_chol_df(const double* __restrict__ gram, int ls, double* X, double* cvec,
                                                 LanczosFlags* fl) {
   if (stopped(fl)) return;  // one warp: every lane reads the same flags
-  __shared__ float2 A[32 * 32];  // A[j*32 + i]: the Gram matrix (upper), then R(i,j) in place
-  __shared__ float2 Xs[32 * 32];
-  __shared__ int bad;
-  const int lane = threadIdx.x;
-  if (lane == 0) bad = 0;
-  for (int k = 0, off = 0; k < ls; off += ls - k, ++k)
-    for (int l = k + lane; l < ls; l += 32) {
-      float h, lo;
-      df_from_double(gram[off + (l - k)], h, lo);
-      A[l * 32 + k] = make_float2(h, lo);
-    }
-  __syncwarp();
-  for (int k = 0; k < ls; ++k) {
-    if (lane == 0) {
-      float2 d = A[k * 32 + k];
-      if (!(d.x > 0.f)) {
-        bad = 1;
-        d = make_float2(1e-30f, 0.f);
-      }
-      A[k * 32 + k] = dfw_sqrt(d);
-    }
-    __syncwarp();
-    const float2 rkk = A[k * 32 + k];
-    for (int j = k + 1 + lane; j < ls; j += 32) A[j * 32 + k] = dfw_div(A[j * 32 + k], rkk);
-    __syncwarp();
-    // trailing update A(i,j) -= R(k,i) R(k,j), k < i <= j; lane over j
-    for (int j = k + 1 + lane; j < ls; j += 32) {
-      const float2 rkj = A[j * 32 + k];
-      for (int i = k + 1; i <= j; ++i) A[j * 32 + i] = dfw_sub(A[j * 32 + i], dfw_mul(A[i * 32 + k], rkj));
-    }
-    __syncwarp();
-  }
-  // X = R^{-1}: column j by lane j, rows from the bottom
-  for (int j = lane; j < ls; j += 32) {
-    for (int i = ls - 1; i >= 0; --i) {
-      float2 sacc = make_float2(i == j ? 1.f : 0.f, 0.f);
-      if (i <= j) {
-        for (int k = i + 1; k <= j; ++k) sacc = dfw_sub(sacc, dfw_mul(A[k * 32 + i], Xs[j * 32 + k]));
-        sacc = dfw_div(sacc, A[i * 32 + i]);
-      } else {
-        sacc = make_float2(0.f, 0.f);
-      }
-      Xs[j * 32 + i] = sacc;
-    }
-  }
-  __syncwarp();
-  for (int idx = lane; idx < ls * ls; idx += 32) {
-    const int j = idx / ls, i = idx % ls;
-    X[j * ls + i] = (double)Xs[j * 32 + i].x + (double)Xs[j * 32 + i].y;
-  }
-  const int gofs = ls * (ls + 1) / 2;
-  for (int k = lane; k < ls; k += 32) {
-    float2 sacc = make_float2(0.f, 0.f);
-    for (int j = 0; j <= k; ++j) {
-      float gh, gl;
-      df_from_double(gram[gofs + j], gh, gl);
-      const float2 p = dfw_mul(Xs[k * 32 + j], make_float2(gh, gl));
-      df_add(sacc.x, sacc.y, p.x, p.y);
-    }
-    cvec[k] = (double)sacc.x + (double)sacc.y;
-  }
-  if (lane == 0 && bad) fl->bad = 1;
+  const bool bad = chol_df_warp(
+      ls, [&](int idx) { return gram[idx]; }, [&](int j, int i, double x) { X[j * ls + i] = x; },
+      [&](int k, double c) { cvec[k] = c; });
+  if (threadIdx.x == 0 && bad) fl->bad = 1;
 }
 
 // V_k = Σ_{j<=k} X[j,k] U_j (k < ls);  V_ls = V_{lm-1} - Σ_k c_k V_k.

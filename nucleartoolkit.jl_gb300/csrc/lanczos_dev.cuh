@@ -631,6 +631,102 @@ __device__ __forceinline__ void sum_partials_many_df(const float2* __restrict__ 
   __syncthreads();
 }
 
+// Double-float scalar arithmetic for one warp's small dense algebra
+// (division and square root: an FP32 estimate and one Newton correction).
+__device__ __forceinline__ float2 dfw_sub(float2 a, float2 b) {
+  df_add(a.x, a.y, -b.x, -b.y);
+  return a;
+}
+__device__ __forceinline__ float2 dfw_mul(float2 a, float2 b) {
+  float h, l;
+  df_mul(a.x, a.y, b.x, b.y, h, l);
+  return make_float2(h, l);
+}
+__device__ __forceinline__ float2 dfw_div(float2 a, float2 b) {
+  const float q1 = __fdiv_rn(a.x, b.x);
+  const float2 r = dfw_sub(a, dfw_mul(make_float2(q1, 0.f), b));
+  const float q2 = __fdiv_rn(r.x, b.x);
+  float h, l;
+  fast_two_sum(q1, q2, h, l);
+  return make_float2(h, l);
+}
+__device__ __forceinline__ float2 dfw_sqrt(float2 a) {
+  const float s = __fsqrt_rn(a.x);
+  const float2 r = dfw_sub(a, dfw_mul(make_float2(s, 0.f), make_float2(s, 0.f)));
+  float h, l;
+  fast_two_sum(s, __fdiv_rn(r.x, 2.f * s), h, l);
+  return make_float2(h, l);
+}
+
+// ThickRestart's Cholesky G = RᵀR, X = R⁻¹ and c = Xᵀ g in double-float
+// arithmetic on one warp (the FP32 pipe; a single-thread FP64 form is
+// latency-bound on GB300's FP64 unit).  gram(idx) reads the packed upper
+// triangle (row by row) followed by g; putX(j, i, x) stores X(i, j)
+// (zero below the diagonal); putc(k, c).  Right-looking factorisation with
+// the lanes over the columns of the trailing update, the inverse by back
+// substitution one column per lane.  ls <= 32.  Returns true (in every lane)
+// when a pivot was not positive.
+template <class GF, class XF, class CF>
+__device__ inline bool chol_df_warp(int ls, GF gram, XF putX, CF putc) {
+  __shared__ float2 A[32 * 32];   // A[j*32 + i]: the Gram matrix (upper), then R(i,j) in place
+  __shared__ float2 Xs[32 * 32];
+  const int lane = threadIdx.x & 31;
+  int bad = 0;
+  for (int k = 0, off = 0; k < ls; off += ls - k, ++k)
+    for (int l = k + lane; l < ls; l += 32) {
+      float h, lo;
+      df_from_double(gram(off + (l - k)), h, lo);
+      A[l * 32 + k] = make_float2(h, lo);
+    }
+  __syncwarp();
+  for (int k = 0; k < ls; ++k) {
+    float2 d = A[k * 32 + k];
+    if (!(d.x > 0.f)) {
+      bad = 1;
+      d = make_float2(1e-30f, 0.f);
+    }
+    const float2 rkk = dfw_sqrt(d);
+    __syncwarp();
+    if (lane == 0) A[k * 32 + k] = rkk;
+    for (int j = k + 1 + lane; j < ls; j += 32) A[j * 32 + k] = dfw_div(A[j * 32 + k], rkk);
+    __syncwarp();
+    for (int j = k + 1 + lane; j < ls; j += 32) {
+      const float2 rkj = A[j * 32 + k];
+      for (int i = k + 1; i <= j; ++i) A[j * 32 + i] = dfw_sub(A[j * 32 + i], dfw_mul(A[i * 32 + k], rkj));
+    }
+    __syncwarp();
+  }
+  for (int j = lane; j < ls; j += 32) {
+    for (int i = ls - 1; i >= 0; --i) {
+      float2 sacc = make_float2(0.f, 0.f);
+      if (i <= j) {
+        sacc.x = i == j ? 1.f : 0.f;
+        for (int k = i + 1; k <= j; ++k) sacc = dfw_sub(sacc, dfw_mul(A[k * 32 + i], Xs[j * 32 + k]));
+        sacc = dfw_div(sacc, A[i * 32 + i]);
+      }
+      Xs[j * 32 + i] = sacc;
+    }
+  }
+  __syncwarp();
+  for (int idx = lane; idx < ls * ls; idx += 32) {
+    const int j = idx / ls, i = idx % ls;
+    putX(j, i, (double)Xs[j * 32 + i].x + (double)Xs[j * 32 + i].y);
+  }
+  const int gofs = ls * (ls + 1) / 2;
+  for (int k = lane; k < ls; k += 32) {
+    float2 sacc = make_float2(0.f, 0.f);
+    for (int j = 0; j <= k; ++j) {
+      float gh, gl;
+      df_from_double(gram(gofs + j), gh, gl);
+      const float2 p = dfw_mul(Xs[k * 32 + j], make_float2(gh, gl));
+      df_add(sacc.x, sacc.y, p.x, p.y);
+    }
+    putc(k, (double)sacc.x + (double)sacc.y);
+  }
+  __syncwarp();
+  return bad != 0;
+}
+
 // x = hi + lo with hi = x rounded to FP32 and lo the FP32 rounding of the rest.
 __device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
   hi = __double2float_rn(x);

@@ -520,6 +520,125 @@ __global__ void __launch_bounds__(kNT) k_m_rotate(const float* __restrict__ V, f
   }
 }
 
+// The same rotation with the basis read once: all ls <= 16 outputs of a
+// thread's element in registers, compensated FMA sums, every sample's Y in
+// shared memory as [j][s][16] (a thread reads its sample's row as float4s).
+constexpr int kMRLS = 16;
+template <int S>
+__global__ void __launch_bounds__(kNT) k_m_rotate_r(const float* __restrict__ V, float* __restrict__ U,
+                                                    const float* __restrict__ Yf, int m, int ls, int64_t len,
+                                                    const LanczosFlags* __restrict__ fl, const MultiCtl* ctl) {
+  if (cta_gate(threadIdx.x == 0 && ctl->all_done)) return;
+  extern __shared__ float ysh[];  // m x S x kMRLS
+  for (int idx = threadIdx.x; idx < m * S * kMRLS; idx += kNT) {
+    const int k = idx % kMRLS, ss = (idx / kMRLS) % S, j = idx / (kMRLS * S);
+    ysh[idx] = k < ls ? Yf[(int64_t)ss * m * ls + (int64_t)k * m + j] : 0.f;
+  }
+  __syncthreads();
+  const int s = threadIdx.x % S;
+  if (lane_stopped(fl, s)) return;
+  const int64_t LS = len * S;
+  for (int64_t e = blockIdx.x * (int64_t)kNT + threadIdx.x; e < LS; e += (int64_t)gridDim.x * kNT) {
+    KahanF acc[kMRLS];
+#pragma unroll
+    for (int k = 0; k < kMRLS; ++k) acc[k].init();
+    int j = 0;
+    for (; j + 4 <= m; j += 4) {
+      float x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = V[(int64_t)(j + u) * LS + e];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4* y4 = reinterpret_cast<const float4*>(ysh + ((j + u) * S + s) * kMRLS);
+#pragma unroll
+        for (int q = 0; q < kMRLS / 4; ++q) {
+          const float4 y = y4[q];
+          acc[4 * q].add_prod(y.x, x[u]);
+          acc[4 * q + 1].add_prod(y.y, x[u]);
+          acc[4 * q + 2].add_prod(y.z, x[u]);
+          acc[4 * q + 3].add_prod(y.w, x[u]);
+        }
+      }
+    }
+    for (; j < m; ++j) {
+      const float x = V[(int64_t)j * LS + e];
+      const float4* y4 = reinterpret_cast<const float4*>(ysh + (j * S + s) * kMRLS);
+#pragma unroll
+      for (int q = 0; q < kMRLS / 4; ++q) {
+        const float4 y = y4[q];
+        acc[4 * q].add_prod(y.x, x);
+        acc[4 * q + 1].add_prod(y.y, x);
+        acc[4 * q + 2].add_prod(y.z, x);
+        acc[4 * q + 3].add_prod(y.w, x);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kMRLS; ++k)
+      if (k < ls) U[(int64_t)k * LS + e] = acc[k].get();
+  }
+}
+
+// The apply with U of a thread's element in registers and every sample's X
+// in shared memory (odd row stride: the lanes' samples hit distinct banks).
+template <int S>
+__global__ void __launch_bounds__(kNT) k_m_apply_r(const float* __restrict__ U, float* __restrict__ V,
+                                                   const float* __restrict__ Xf, int ls, int lm, int64_t len,
+                                                   const LanczosFlags* __restrict__ fl, const MultiCtl* ctl) {
+  if (cta_gate(threadIdx.x == 0 && ctl->all_done)) return;
+  extern __shared__ float xsh[];  // S x XST
+  const int XN = ls * ls + ls, XST = XN | 1;
+  for (int idx = threadIdx.x; idx < S * XN; idx += kNT) {
+    const int ss = idx / XN, r = idx % XN;
+    xsh[ss * XST + r] = Xf[(int64_t)ss * XN + r];
+  }
+  __syncthreads();
+  const int s = threadIdx.x % S;
+  if (lane_stopped(fl, s)) return;
+  const float* xf = xsh + s * XST;
+  const int64_t LS = len * S;
+  for (int64_t e = blockIdx.x * (int64_t)kNT + threadIdx.x; e < LS; e += (int64_t)gridDim.x * kNT) {
+    float u[kMRLS];
+#pragma unroll
+    for (int j = 0; j < kMRLS; ++j) u[j] = j < ls ? U[(int64_t)j * LS + e] : 0.f;
+    KahanF last;
+    last.init();
+    last.add(V[(int64_t)(lm - 1) * LS + e]);
+#pragma unroll
+    for (int k = 0; k < kMRLS; ++k) {
+      if (k >= ls) break;
+      KahanF q;
+      q.init();
+#pragma unroll
+      for (int j = 0; j <= k; ++j) q.add_prod(xf[k * ls + j], u[j]);
+      const float qv = q.get();
+      V[(int64_t)k * LS + e] = qv;
+      last.add_prod(-xf[ls * ls + k], qv);
+    }
+    V[(int64_t)ls * LS + e] = last.get();
+  }
+}
+
+// Each sample's Cholesky on one warp in double-float (chol_df_warp).
+__global__ void __launch_bounds__(32) k_m_chol_df(const double* __restrict__ gram, int ls, int S, double* X,
+                                                  float* Xf, double* cvec, LanczosFlags* fl, const MultiCtl* ctl) {
+  const int s = blockIdx.x;
+  if (ctl->all_done || lane_stopped(fl, s)) return;  // one warp: uniform
+  double* Xs = X + (int64_t)s * ls * ls;
+  double* cs = cvec + (int64_t)s * ls;
+  float* xf = Xf + (int64_t)s * (ls * ls + ls);
+  const bool bad = chol_df_warp(
+      ls, [&](int idx) { return gram[(int64_t)idx * S + s]; },
+      [&](int j, int i, double x) {
+        Xs[j * ls + i] = x;
+        xf[j * ls + i] = (float)x;
+      },
+      [&](int k, double c) {
+        cs[k] = c;
+        xf[ls * ls + k] = (float)c;
+      });
+  if (threadIdx.x == 0 && bad) fl[s].bad = 1;
+}
+
 // Gram matrices of U_s (packed upper triangle) and U_k,s·v_last,s for every
 // sample, double-float sums.  Pair order as k_gram; c = pair*S + s.
 template <int S>
@@ -740,16 +859,27 @@ void launch_m_restart(const MultiDev& M, float* V, float* U, cudaStream_t st) {
   k_m_restart_small<<<S, 256, 0, st>>>(M.T, lm, ls, M.evals, M.jacA, M.Yf, M.fl, M.ctl);
   const size_t ysh = sizeof(float) * (size_t)m * 8 * S;
   const int use_smem = ysh <= 48 * 1024 ? 1 : 0;
-  SMGPU_S_DISPATCH(S, (k_m_rotate<SS><<<grid_for(LS), kNT, use_smem ? ysh : 0, st>>>(V, U, M.Yf, m, ls, M.len, M.fl,
-                                                                                  M.ctl, use_smem)));
+  const size_t yshr = sizeof(float) * (size_t)m * S * kMRLS;
+  if (ls <= kMRLS && yshr <= 48 * 1024) {
+    SMGPU_S_DISPATCH(S, (k_m_rotate_r<SS><<<grid_for(LS), kNT, yshr, st>>>(V, U, M.Yf, m, ls, M.len, M.fl, M.ctl)));
+  } else {
+    SMGPU_S_DISPATCH(S, (k_m_rotate<SS><<<grid_for(LS), kNT, use_smem ? ysh : 0, st>>>(V, U, M.Yf, m, ls, M.len, M.fl,
+                                                                                    M.ctl, use_smem)));
+  }
   const int tile = gram_tile(ls, S);
   const size_t gsh = sizeof(float) * (size_t)(ls + 1) * tile * S;
   SMGPU_S_DISPATCH(S, (k_m_gram<SS><<<M.G, kNT, gsh, st>>>(U, V + (int64_t)(lm - 1) * LS, ls, M.len, tile, M.part,
                                                            M.G, M.ctl)));
   const int PS = (ls * (ls + 1) / 2 + ls) * S;
   k_m_reduce<<<reduce_grid(PS), kNT, 0, st>>>(M.part, M.G, PS, M.gram, M.ctl, 1);
-  k_m_chol<<<S, 32, sizeof(double) * ls * ls, st>>>(M.gram, ls, S, M.X, M.Xf, M.cvec, M.fl, M.ctl);
-  SMGPU_S_DISPATCH(S, (k_m_apply<SS><<<grid_for(LS), kNT, 0, st>>>(U, V, M.Xf, ls, lm, M.len, M.fl, M.ctl)));
+  if (ls <= 32) k_m_chol_df<<<S, 32, 0, st>>>(M.gram, ls, S, M.X, M.Xf, M.cvec, M.fl, M.ctl);
+  else k_m_chol<<<S, 32, sizeof(double) * ls * ls, st>>>(M.gram, ls, S, M.X, M.Xf, M.cvec, M.fl, M.ctl);
+  const size_t xsh = sizeof(float) * (size_t)S * ((ls * ls + ls) | 1);
+  if (ls <= kMRLS && xsh <= 48 * 1024) {
+    SMGPU_S_DISPATCH(S, (k_m_apply_r<SS><<<grid_for(LS), kNT, xsh, st>>>(U, V, M.Xf, ls, lm, M.len, M.fl, M.ctl)));
+  } else {
+    SMGPU_S_DISPATCH(S, (k_m_apply<SS><<<grid_for(LS), kNT, 0, st>>>(U, V, M.Xf, ls, lm, M.len, M.fl, M.ctl)));
+  }
 }
 
 void launch_m_jacobi_one(const MultiDev& M, int s, int n, cudaStream_t st) {
