@@ -670,17 +670,19 @@ __global__ void __launch_bounds__(kNT) k_restart_rotate_f(const float* __restric
       float x[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) x[u] = V[(int64_t)(j + u) * len + i];
+      // the four terms of a group summed with plain FMAs, the group sums
+      // compensated (half the operations of a compensated step per term)
+      const float4* y0 = reinterpret_cast<const float4*>(ys + (j + 0) * kRLS);
+      const float4* y1 = reinterpret_cast<const float4*>(ys + (j + 1) * kRLS);
+      const float4* y2 = reinterpret_cast<const float4*>(ys + (j + 2) * kRLS);
+      const float4* y3 = reinterpret_cast<const float4*>(ys + (j + 3) * kRLS);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float4* y4 = reinterpret_cast<const float4*>(ys + (j + u) * kRLS);
-#pragma unroll
-        for (int q = 0; q < kRLS / 4; ++q) {
-          const float4 y = y4[q];
-          acc[4 * q].add_prod(y.x, x[u]);
-          acc[4 * q + 1].add_prod(y.y, x[u]);
-          acc[4 * q + 2].add_prod(y.z, x[u]);
-          acc[4 * q + 3].add_prod(y.w, x[u]);
-        }
+      for (int q = 0; q < kRLS / 4; ++q) {
+        const float4 a = y0[q], b = y1[q], c = y2[q], d = y3[q];
+        acc[4 * q].add(__fmaf_rn(d.x, x[3], __fmaf_rn(c.x, x[2], __fmaf_rn(b.x, x[1], __fmul_rn(a.x, x[0])))));
+        acc[4 * q + 1].add(__fmaf_rn(d.y, x[3], __fmaf_rn(c.y, x[2], __fmaf_rn(b.y, x[1], __fmul_rn(a.y, x[0])))));
+        acc[4 * q + 2].add(__fmaf_rn(d.z, x[3], __fmaf_rn(c.z, x[2], __fmaf_rn(b.z, x[1], __fmul_rn(a.z, x[0])))));
+        acc[4 * q + 3].add(__fmaf_rn(d.w, x[3], __fmaf_rn(c.w, x[2], __fmaf_rn(b.w, x[1], __fmul_rn(a.w, x[0])))));
       }
     }
     for (; j < m; ++j) {

@@ -246,12 +246,14 @@ __global__ void __launch_bounds__(kNT) k_m_dot_df(const float* __restrict__ V, i
   const float* __restrict__ vk = V + (int64_t)it0 * LS;
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
+  // FP32 per-thread sums (a thread adds a few products of one chunk per
+  // sample; their rounding is far below the FP32 basis), double-float CTA sums
   for (int j0 = 0; j0 < mt; j0 += 8) {
-    DFAcc acc[8][4];
+    float acc[8][4];
 #pragma unroll
     for (int q8 = 0; q8 < 8; ++q8)
 #pragma unroll
-      for (int u = 0; u < 4; ++u) acc[q8][u].init();
+      for (int u = 0; u < 4; ++u) acc[q8][u] = 0.f;
     for (int64_t i = cb + r; i < ce; i += RPP) {
       const int64_t e = i * S + s0;
       const float4 a4 = *reinterpret_cast<const float4*>(wh + e);
@@ -271,17 +273,25 @@ __global__ void __launch_bounds__(kNT) k_m_dot_df(const float* __restrict__ V, i
         const int j = j0 + q8;
         if (j < m) {
           const float4 x = *reinterpret_cast<const float4*>(V + (int64_t)j * LS + e);
-          acc[q8][0].add_prod2(x.x, h[0], l[0]);
-          acc[q8][1].add_prod2(x.y, h[1], l[1]);
-          acc[q8][2].add_prod2(x.z, h[2], l[2]);
-          acc[q8][3].add_prod2(x.w, h[3], l[3]);
+          acc[q8][0] = __fmaf_rn(x.x, h[0], acc[q8][0]);
+          acc[q8][1] = __fmaf_rn(x.y, h[1], acc[q8][1]);
+          acc[q8][2] = __fmaf_rn(x.z, h[2], acc[q8][2]);
+          acc[q8][3] = __fmaf_rn(x.w, h[3], acc[q8][3]);
         } else if (first && j == m) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q8][u].add_prod2(h[u], h[u], 2.0f * l[u]);
+          for (int u = 0; u < 4; ++u) acc[q8][u] = __fmaf_rn(h[u], h[u], acc[q8][u]);
         }
       }
     }
-    reduce_slots_df<S, 8>(acc, min(8, mt - j0), red, part, j0, G);
+    DFAcc dacc[8][4];
+#pragma unroll
+    for (int q8 = 0; q8 < 8; ++q8)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        dacc[q8][u].hi = acc[q8][u];
+        dacc[q8][u].lo = 0.f;
+      }
+    reduce_slots_df<S, 8>(dacc, min(8, mt - j0), red, part, j0, G);
   }
 }
 
@@ -547,17 +557,19 @@ __global__ void __launch_bounds__(kNT) k_m_rotate_r(const float* __restrict__ V,
       float x[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) x[u] = V[(int64_t)(j + u) * LS + e];
+      // the four terms of a group summed with plain FMAs, the group sums
+      // compensated (half the operations of a compensated step per term)
+      const float4* y0 = reinterpret_cast<const float4*>(ysh + ((j + 0) * S + s) * kMRLS);
+      const float4* y1 = reinterpret_cast<const float4*>(ysh + ((j + 1) * S + s) * kMRLS);
+      const float4* y2 = reinterpret_cast<const float4*>(ysh + ((j + 2) * S + s) * kMRLS);
+      const float4* y3 = reinterpret_cast<const float4*>(ysh + ((j + 3) * S + s) * kMRLS);
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const float4* y4 = reinterpret_cast<const float4*>(ysh + ((j + u) * S + s) * kMRLS);
-#pragma unroll
-        for (int q = 0; q < kMRLS / 4; ++q) {
-          const float4 y = y4[q];
-          acc[4 * q].add_prod(y.x, x[u]);
-          acc[4 * q + 1].add_prod(y.y, x[u]);
-          acc[4 * q + 2].add_prod(y.z, x[u]);
-          acc[4 * q + 3].add_prod(y.w, x[u]);
-        }
+      for (int q = 0; q < kMRLS / 4; ++q) {
+        const float4 a = y0[q], b = y1[q], c = y2[q], d = y3[q];
+        acc[4 * q].add(__fmaf_rn(d.x, x[3], __fmaf_rn(c.x, x[2], __fmaf_rn(b.x, x[1], __fmul_rn(a.x, x[0])))));
+        acc[4 * q + 1].add(__fmaf_rn(d.y, x[3], __fmaf_rn(c.y, x[2], __fmaf_rn(b.y, x[1], __fmul_rn(a.y, x[0])))));
+        acc[4 * q + 2].add(__fmaf_rn(d.z, x[3], __fmaf_rn(c.z, x[2], __fmaf_rn(b.z, x[1], __fmul_rn(a.z, x[0])))));
+        acc[4 * q + 3].add(__fmaf_rn(d.w, x[3], __fmaf_rn(c.w, x[2], __fmaf_rn(b.w, x[1], __fmul_rn(a.w, x[0])))));
       }
     }
     for (; j < m; ++j) {
