@@ -739,7 +739,8 @@ __global__ void __launch_bounds__(kNT) k_restart_apply_f(const float* __restrict
 //   Gram: tiles of 128 elements of the ls+1 vectors staged in shared memory,
 //         double-buffered through registers (the next tile's loads are in
 //         flight while the current one is multiplied); one thread per pair,
-//         double-float sums, partials as (hi, lo) pairs.
+//         FP32 sums per tile added in double-float, partials as (hi, lo)
+//         pairs.
 __global__ void __launch_bounds__(kNT) k_gram_f(const float* __restrict__ U, const float* __restrict__ vl, int ls,
                                                 int64_t len, double* __restrict__ partials, int G,
                                                 const LanczosFlags* __restrict__ fl) {
@@ -788,8 +789,17 @@ __global__ void __launch_bounds__(kNT) k_gram_f(const float* __restrict__ U, con
     if (more) load(t0 + TILE);
     const float* tl = gt + buf * nv * TS;
     if (act) {
+      // the tile's products summed in FP32 (128 terms of O(1/len) each), the
+      // tile sums added in double-float
       const int cnt = (int)min((int64_t)TILE, ce - t0);
-      for (int x = 0; x < cnt; ++x) acc.add_prod(tl[k * TS + x], tl[l * TS + x]);
+      float p0 = 0.f, p1 = 0.f;
+      int x = 0;
+      for (; x + 1 < cnt; x += 2) {
+        p0 = __fmaf_rn(tl[k * TS + x], tl[l * TS + x], p0);
+        p1 = __fmaf_rn(tl[k * TS + x + 1], tl[l * TS + x + 1], p1);
+      }
+      if (x < cnt) p0 = __fmaf_rn(tl[k * TS + x], tl[l * TS + x], p0);
+      df_add(acc.hi, acc.lo, __fadd_rn(p0, p1), 0.f);
     }
     if (more) store(buf ^ 1);
     __syncthreads();
