@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(kNT) k_b_init_scale(const BatchDev B, const do
   __shared__ double red[kNT / 32];
   const int4 ch = B.chunks[blockIdx.x];
   const BatchProblemDev& P = B.probs[ch.x];
-  const double inv = 1.0 / sqrt(sum_partials<kNT>(B.pn1 + P.chunk0, P.nchunks, red));
+  const double inv = 1.0 / sqrt(sum_partials_d2<kNT>(B.pn1 + P.chunk0, P.nchunks, red));
   for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) v[P.voff + i] = (float)(w[P.voff + i] * inv);
 }
 
@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
   __shared__ double red[kNT / 32];
-  const double alpha = sum_partials<kNT>(B.alpha_part + (int64_t)it0 * B.nslots + P.slot0, P.nslots, red);
+  __shared__ double red8[(kNT / 32) * 8];
+  const double alpha = sum_partials_d2<kNT>(B.alpha_part + (int64_t)it0 * B.nslots + P.slot0, P.nslots, red);
   const float* __restrict__ Vb = V + P.voff;
   const float* __restrict__ vk = Vb + (int64_t)it0 * B.LEN;
   double* wb = w + P.voff;
@@ -163,19 +164,18 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
         }
       }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q > m) break;
-      const double s = block_sum_all<kNT>(acc[q].get(), red);
-      if (threadIdx.x == 0) B.pdot[(int64_t)(j0 + q) * B.nchunks + c] = s;
-    }
+    // the eight sums in one double-float CTA reduction on the FP32 pipe
+    float2 s;
+    block_sum_df<kNT, 8>(acc, red8, s);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m)
+      B.pdot[(int64_t)(j0 + threadIdx.x) * B.nchunks + c] = (double)s.x + (double)s.y;
   }
 }
 
 // Second-pass decision of the problem, identical in all its CTAs.
 __device__ __forceinline__ bool b_need_second(const BatchDev& B, const BatchProblemDev& P, int m, double* red) {
-  const double n0 = sum_partials<kNT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
-  const double n1 = sum_partials<kNT>(B.pn1 + P.chunk0, P.nchunks, red);
+  const double n0 = sum_partials_d2<kNT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
+  const double n1 = sum_partials_d2<kNT>(B.pn1 + P.chunk0, P.nchunks, red);
   return n1 < 0.5 * n0;
 }
 
@@ -215,7 +215,7 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
     }
     store4(wb + i, t);
   }
-  const double s = block_sum_all<kNT>(nrm, red);
+  const double s = block_sum_d2<kNT>(nrm, red);
   if (threadIdx.x == 0) pout[blockIdx.x] = s;
 }
 
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
   const bool second = b_need_second(B, P, m, red);
-  const double nrm = sum_partials<kNT>((second ? B.pn2 : B.pn1) + P.chunk0, P.nchunks, red);
+  const double nrm = sum_partials_d2<kNT>((second ? B.pn2 : B.pn1) + P.chunk0, P.nchunks, red);
   const double beta = sqrt(nrm);
   const bool ok = (beta > 0.0) && (beta < INFINITY);
   if (c == P.chunk0 && threadIdx.x == 0) {

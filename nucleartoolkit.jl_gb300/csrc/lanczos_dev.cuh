@@ -604,6 +604,31 @@ __device__ __forceinline__ float2 sum_partials_df(const float2* __restrict__ p, 
   return block_sum_df2<NT>(h, l, red);
 }
 
+// Sum of n FP64 partials reduced in double-float on the FP32 pipe (each
+// partial split once); the double result in every thread.  red: NT/32 doubles.
+template <int NT>
+__device__ __forceinline__ double sum_partials_d2(const double* __restrict__ p, int n, double* red) {
+  float h = 0.f, l = 0.f;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < n; i += NT) {
+    float xh, xl;
+    df_from_double(p[i], xh, xl);
+    df_add(h, l, xh, xl);
+  }
+  const float2 s = block_sum_df2<NT>(h, l, reinterpret_cast<float2*>(red));
+  return (double)s.x + (double)s.y;
+}
+
+// Block sum of one FP64 value per thread, reduced in double-float (FP32
+// pipe); the double result in every thread.  red: NT/32 doubles.
+template <int NT>
+__device__ __forceinline__ double block_sum_d2(double x, double* red) {
+  float h, l;
+  df_from_double(x, h, l);
+  const float2 s = block_sum_df2<NT>(h, l, reinterpret_cast<float2*>(red));
+  return (double)s.x + (double)s.y;
+}
+
 // m sums of G double-float partials each (one warp per sum), results as
 // (hi, lo) into shared hh[j], hl[j].
 template <int NT>
