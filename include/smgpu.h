@@ -206,7 +206,8 @@ int smgpu_solve_block(smgpu_problem* h, int q, int num_ev, int lm, int ls, doubl
  * [setup (host wall), lanczos (CUDA events on the handle's stream, start
  *  vector to converged eigenvalues), last matvec call (host wall), graph
  *  capture + instantiation (host wall), ritz vectors (events), solve call
- *  (host wall), reserved, reserved]. */
+ *  (host wall), set-up part: basis and jump tables (host wall), set-up
+ *  part: device tables, staged-kernel tables and autotuning (host wall)]. */
 int smgpu_timings(const smgpu_problem* h, double* times_out);
 
 /* Time `reps` back-to-back H·v launches on the handle's stream with CUDA

@@ -200,10 +200,13 @@ int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision
     double t0 = now_s();
     build_tables(I, vp, vn, mtot2, h->T);
     if (h->T.mdim == 0) throw SetupError{SMGPU_ERR_EMPTY, "M-scheme dimension is zero"};
+    const double t1 = now_s();
     h->upload();
     h->autotune();
     SMGPU_CUDA_TRY(cudaStreamSynchronize(h->st));
     h->times[0] = now_s() - t0;
+    h->times[6] = t1 - t0;
+    h->times[7] = now_s() - t1;
   } catch (...) {
     delete h;
     throw;

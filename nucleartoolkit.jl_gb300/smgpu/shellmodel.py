@@ -96,7 +96,7 @@ class ShellModelProblem:
     def timings(self):
         t = np.zeros(8)
         check(load().smgpu_timings(self._h, _p(t)), self._h)
-        keys = ["setup", "lanczos", "matvec", "capture", "ritz", "solve_wall", "r6", "r7"]
+        keys = ["setup", "lanczos", "matvec", "capture", "ritz", "solve_wall", "setup_tables", "setup_upload"]
         return dict(zip(keys, map(float, t)))
 
     def time_matvec(self, reps=20, flush_l2=True):
