@@ -176,6 +176,16 @@ long long graph_kernel_nodes(cudaGraph_t g) {
 // Time every launch shape on the whole batch (3 launches each, the first a
 // warm-up) and keep the fastest.  SMGPU_AUTOTUNE=0 keeps the default.
 void smgpu_batch::autotune() {
+  // SMGPU_BATCH_CAND=k selects candidate k of hv_batch_candidates outright
+  // (for tests that run every shape)
+  if (const char* c = std::getenv("SMGPU_BATCH_CAND")) {
+    int nc = 0;
+    hv_batch_candidates(&nc);
+    const int k = std::atoi(c);
+    if (k < 0 || k >= nc) throw SetupError{SMGPU_ERR_ARG, "SMGPU_BATCH_CAND out of range"};
+    set_cand(k);
+    return;
+  }
   const char* off = std::getenv("SMGPU_AUTOTUNE");
   if (off && std::string(off) == "0") return;
   DeviceArena tmp;

@@ -77,6 +77,26 @@ void tune_file_store() {
 
 void smgpu_problem::autotune() {
   ShapeKey key{precision, T.Lp, T.Ln, vp, vn, mtot2};
+  // SMGPU_HV_SHAPE="threads,rows,min_ctas,staged" selects one candidate
+  // launch shape outright (for tests that run every shape); unknown or
+  // non-fitting shapes are an error.
+  if (const char* shape = std::getenv("SMGPU_HV_SHAPE")) {
+    HvConfig want{0, 0, 0, 0, 0};
+    if (std::sscanf(shape, "%d,%d,%d,%d", &want.nt, &want.rows, &want.minb, &want.staged) != 4)
+      throw SetupError{SMGPU_ERR_ARG, "SMGPU_HV_SHAPE must be threads,rows,min_ctas,staged"};
+    int n0 = 0, n1 = 0;
+    const HvConfig* c0 = hv_candidates(&n0);
+    const HvConfig* c1 = hv_staged_candidates(&n1);
+    bool known = false;
+    for (int k = 0; k < n0 && !known; ++k)
+      known = !want.staged && c0[k].nt == want.nt && c0[k].rows == want.rows && c0[k].minb == want.minb;
+    for (int k = 0; k < n1 && !known; ++k)
+      known = want.staged && precision != SMGPU_FP64 && c1[k].nt == want.nt && c1[k].rows == want.rows &&
+              c1[k].minb == want.minb && hv_staged_fits(c1[k], tt, nnmax_raw);
+    if (!known) throw SetupError{SMGPU_ERR_ARG, "SMGPU_HV_SHAPE is not a candidate shape for this problem"};
+    set_config(want.nt, want.rows, want.minb, want.staged);
+    return;
+  }
   // SMGPU_HV_FORM=tile|staged restricts the candidates to one H·v kernel form
   // (and bypasses the shape cache); unset, both forms compete.
   const char* form_env = std::getenv("SMGPU_HV_FORM");

@@ -140,6 +140,16 @@ std::map<MultiKey, int> g_mtune;
 void smgpu_multi::autotune() {
   const Tables& T = base.T;
   const MultiKey key{S, T.Lp, T.Ln, base.vp, base.vn, base.mtot2};
+  // SMGPU_MULTI_CAND=k selects candidate k of hv_multi_candidates outright
+  // (for tests that run every shape)
+  if (const char* c = std::getenv("SMGPU_MULTI_CAND")) {
+    int nc = 0;
+    hv_multi_candidates(&nc);
+    const int k = std::atoi(c);
+    if (k < 0 || k >= nc) throw SetupError{SMGPU_ERR_ARG, "SMGPU_MULTI_CAND out of range"};
+    cand = k;
+    return;
+  }
   {
     std::lock_guard<std::mutex> lk(g_mtune_mu);
     auto it = g_mtune.find(key);

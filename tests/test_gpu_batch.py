@@ -66,6 +66,30 @@ def test_batch_matvec_vs_oracle(lib, mixed_batch):
         assert np.abs(w_acc[p] - (ref + 0.25)).max() <= MATVEC_MIXED_RTOL * scale, (p, nuc)
 
 
+def test_batch_matvec_every_launch_shape(lib, mixed_batch, monkeypatch):
+    """Every candidate launch shape of the batched H·v against the oracle."""
+    from smgpu import _lib
+    probs = mixed_batch[:8]
+    v = None
+    refs = None
+    ncand = 0
+    while True:
+        monkeypatch.setenv("SMGPU_BATCH_CAND", str(ncand))
+        try:
+            G = _batch(probs)
+        except _lib.SmgpuError:
+            break  # past the last candidate
+        if v is None:
+            v = np.random.default_rng(19).standard_normal(G.total_mdim)
+            refs = [_oracle(snt, nuc).operate_H(vp) for (snt, nuc), vp in zip(probs, G.split(v))]
+        w = G.split(G.matvec(v))
+        for p, ref in enumerate(refs):
+            scale = max(np.abs(ref).max(), 1e-30)
+            assert np.abs(w[p] - ref).max() <= MATVEC_MIXED_RTOL * scale, (ncand, p)
+        ncand += 1
+    assert ncand >= 5
+
+
 def test_batch_solve_vs_oracle(lib, mixed_batch):
     G = _batch(mixed_batch)
     r = G.solve(5, lm=30, ls=15, tol=1e-8, want_vecs=True)

@@ -67,6 +67,27 @@ def test_multi_matvec_vs_oracle(lib, samples, n):
         assert np.abs(w_acc[s] - (ref + 0.5)).max() <= MATVEC_MIXED_RTOL * scale, s
 
 
+def test_multi_matvec_every_launch_shape(lib, samples, monkeypatch):
+    """Every candidate launch shape of the multi-sample H·V (threads, register
+    cap, cached neutron entries) against the oracle, 16 samples."""
+    from smgpu import _lib
+    files = samples[("sd2p2n", 16)]
+    v = np.random.default_rng(17).standard_normal((16, 640))
+    refs = [_oracle(f, "Ne20").operate_H(v[s]) for s, f in enumerate(files)]
+    ncand = 0
+    while True:
+        monkeypatch.setenv("SMGPU_MULTI_CAND", str(ncand))
+        try:
+            G = _multi(files, "Ne20")
+        except _lib.SmgpuError:
+            break  # past the last candidate
+        w = G.matvec(v)
+        for s in range(16):
+            assert np.abs(w[s] - refs[s]).max() <= MATVEC_MIXED_RTOL * np.abs(refs[s]).max(), (ncand, s)
+        ncand += 1
+    assert ncand >= 5
+
+
 def test_multi_solve_vs_oracle(lib, samples):
     """5 samples (8 lanes, 3 idle), the pf workload's Lanczos parameters."""
     files = samples[("sd4p4n", 5)]

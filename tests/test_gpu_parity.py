@@ -175,6 +175,45 @@ def test_matvec_mixed_each_kernel_form_pf(lib, snt_dir, form, monkeypatch):
     assert abs(u @ w - hu @ v) <= 1e-6 * np.linalg.norm(u) * np.linalg.norm(w)
 
 
+def _shapes(snt, nuc, prec, form, monkeypatch):
+    """The candidate H·v launch shapes of one kernel form for this problem."""
+    monkeypatch.delenv("SMGPU_HV_SHAPE", raising=False)
+    monkeypatch.setenv("SMGPU_HV_FORM", form)
+    shapes = [(c["threads"], c["rows"], c["min_ctas"], c["staged"]) for c in _gpu(snt, nuc, prec).tune_report()]
+    monkeypatch.delenv("SMGPU_HV_FORM", raising=False)
+    return shapes
+
+
+@pytest.mark.parametrize("case", ["usdb_Na21", "sd4p4n"])
+def test_matvec_every_launch_shape(lib, snt_dir, case, monkeypatch):
+    """Every candidate launch shape of every H·v kernel (FP64 row-tile; FP32
+    row-tile and staged) against the oracle, not only the autotuner's pick;
+    the staged shapes also through a solve (double-float epilogue)."""
+    snt, nuc = _cases(snt_dir)[case]
+    O = _oracle(snt, nuc)
+    v = np.random.default_rng(13).standard_normal(O.mdim)
+    ref = O.operate_H(v)
+    scale = np.abs(ref).max()
+    ro = O.trl(5, lm=30, ls=15, tol=1e-8) if case == "usdb_Na21" else None
+    runs = [(0, sh) for sh in _shapes(snt, nuc, 0, "tile", monkeypatch)]
+    runs += [(1, sh) for sh in _shapes(snt, nuc, 1, "tile", monkeypatch)]
+    runs += [(1, sh) for sh in _shapes(snt, nuc, 1, "staged", monkeypatch)]
+    assert len(runs) >= 13 + 13 + 5
+    for prec, sh in runs:
+        monkeypatch.setenv("SMGPU_HV_SHAPE", ",".join(map(str, sh)))
+        G = _gpu(snt, nuc, prec)
+        st = G.stats()
+        assert (st["hv_threads"], st["hv_rows"], st["hv_min_ctas"], st["hv_staged"]) == sh
+        tol = MATVEC_FP64_RTOL if prec == 0 else MATVEC_MIXED_RTOL
+        assert np.abs(G.matvec(v) - ref).max() <= tol * scale, sh
+        if ro is not None and sh[3] == 1:
+            rm = G.solve(5, lm=30, ls=15, tol=1e-8)
+            assert rm["converged"] and np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, sh
+    monkeypatch.setenv("SMGPU_HV_SHAPE", "999,1,1,1")
+    with pytest.raises(Exception):
+        _gpu(snt, nuc, 1)
+
+
 def test_ckpot_known_answer_on_gpu(lib, golden):
     g = golden["ckpot_Be8"]
     for prec in (0, 1):
