@@ -423,6 +423,132 @@ __global__ void __launch_bounds__(kNT) k_b_rotate(const BatchDev B, const float*
   }
 }
 
+// The rotation with the basis read once: all ls <= 16 outputs of a thread's
+// element in registers, the problem's Y in shared memory (rows padded to 16),
+// groups of four terms summed with FMAs and the group sums compensated.
+constexpr int kBRLS = 16;
+__global__ void __launch_bounds__(kNT) k_b_rotate_r(const BatchDev B, const float* __restrict__ V,
+                                                    float* __restrict__ U) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  const int m = B.lm - 1, ls = B.ls;
+  extern __shared__ float ys[];  // m x kBRLS
+  const float* __restrict__ Y = B.Yf + (int64_t)ch.x * m * ls;
+  for (int idx = threadIdx.x; idx < m * kBRLS; idx += kNT) {
+    const int j = idx / kBRLS, k = idx % kBRLS;
+    ys[idx] = k < ls ? Y[(int64_t)k * m + j] : 0.f;
+  }
+  __syncthreads();
+  const float* __restrict__ Vb = V + P.voff;
+  float* __restrict__ Ub = U + P.voff;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    KahanF acc[kBRLS];
+#pragma unroll
+    for (int k = 0; k < kBRLS; ++k) acc[k].init();
+    int j = 0;
+    for (; j + 4 <= m; j += 4) {
+      float x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = Vb[(int64_t)(j + u) * B.LEN + i];
+      const float4* y0 = reinterpret_cast<const float4*>(ys + (j + 0) * kBRLS);
+      const float4* y1 = reinterpret_cast<const float4*>(ys + (j + 1) * kBRLS);
+      const float4* y2 = reinterpret_cast<const float4*>(ys + (j + 2) * kBRLS);
+      const float4* y3 = reinterpret_cast<const float4*>(ys + (j + 3) * kBRLS);
+#pragma unroll
+      for (int q = 0; q < kBRLS / 4; ++q) {
+        const float4 a = y0[q], b = y1[q], c = y2[q], d = y3[q];
+        acc[4 * q].add(__fmaf_rn(d.x, x[3], __fmaf_rn(c.x, x[2], __fmaf_rn(b.x, x[1], __fmul_rn(a.x, x[0])))));
+        acc[4 * q + 1].add(__fmaf_rn(d.y, x[3], __fmaf_rn(c.y, x[2], __fmaf_rn(b.y, x[1], __fmul_rn(a.y, x[0])))));
+        acc[4 * q + 2].add(__fmaf_rn(d.z, x[3], __fmaf_rn(c.z, x[2], __fmaf_rn(b.z, x[1], __fmul_rn(a.z, x[0])))));
+        acc[4 * q + 3].add(__fmaf_rn(d.w, x[3], __fmaf_rn(c.w, x[2], __fmaf_rn(b.w, x[1], __fmul_rn(a.w, x[0])))));
+      }
+    }
+    for (; j < m; ++j) {
+      const float x = Vb[(int64_t)j * B.LEN + i];
+      const float4* y4 = reinterpret_cast<const float4*>(ys + j * kBRLS);
+#pragma unroll
+      for (int q = 0; q < kBRLS / 4; ++q) {
+        const float4 y = y4[q];
+        acc[4 * q].add_prod(y.x, x);
+        acc[4 * q + 1].add_prod(y.y, x);
+        acc[4 * q + 2].add_prod(y.z, x);
+        acc[4 * q + 3].add_prod(y.w, x);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kBRLS; ++k)
+      if (k < ls) Ub[(int64_t)k * B.LEN + i] = acc[k].get();
+  }
+}
+
+// The apply with the problem's U values of a thread's element in registers.
+__global__ void __launch_bounds__(kNT) k_b_apply_r(const BatchDev B, const float* __restrict__ U,
+                                                   float* __restrict__ V) {
+  const int4 ch = B.chunks[blockIdx.x];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  const int ls = B.ls, lm = B.lm;
+  __shared__ float xf[kBRLS * kBRLS + kBRLS];
+  const float* __restrict__ xg = B.Xf + (int64_t)ch.x * (ls * ls + ls);
+  for (int idx = threadIdx.x; idx < ls * ls + ls; idx += kNT) xf[idx] = xg[idx];
+  __syncthreads();
+  const float* __restrict__ Ub = U + P.voff;
+  float* __restrict__ Vb = V + P.voff;
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) {
+    float u[kBRLS];
+#pragma unroll
+    for (int j = 0; j < kBRLS; ++j) u[j] = j < ls ? Ub[(int64_t)j * B.LEN + i] : 0.f;
+    KahanF last;
+    last.init();
+    last.add(Vb[(int64_t)(lm - 1) * B.LEN + i]);
+#pragma unroll
+    for (int k = 0; k < kBRLS; ++k) {
+      if (k >= ls) break;
+      KahanF q;
+      q.init();
+#pragma unroll
+      for (int j = 0; j <= k; ++j) q.add_prod(xf[k * ls + j], u[j]);
+      const float qv = q.get();
+      Vb[(int64_t)k * B.LEN + i] = qv;
+      last.add_prod(-xf[ls * ls + k], qv);
+    }
+    Vb[(int64_t)ls * B.LEN + i] = last.get();
+  }
+}
+
+// Each problem's Cholesky on one warp in double-float (chol_df_warp); the
+// Gram entries summed over the problem's chunks first.
+__global__ void __launch_bounds__(32) k_b_chol_df(const BatchDev B) {
+  const int p = blockIdx.x;
+  if (B.ctl->all_done || stopped(B.fl + p)) return;  // one warp: uniform
+  const BatchProblemDev& P = B.probs[p];
+  const int ls = B.ls;
+  const int NP = ls * (ls + 1) / 2 + ls;
+  __shared__ double g[32 * 33 / 2 + 32];
+  for (int pr = threadIdx.x; pr < NP; pr += 32) {
+    double x = 0.0;
+    const double* src = B.part + (int64_t)pr * B.nchunks + P.chunk0;
+    for (int q = 0; q < P.nchunks; ++q) x += src[q];
+    g[pr] = x;
+  }
+  __syncwarp();
+  double* X = B.X + (int64_t)p * ls * ls;
+  double* cv = B.cvec + (int64_t)p * ls;
+  float* xf = B.Xf + (int64_t)p * (ls * ls + ls);
+  const bool bad = chol_df_warp(
+      ls, [&](int idx) { return g[idx]; },
+      [&](int j, int i, double x) {
+        X[j * ls + i] = x;
+        xf[j * ls + i] = (float)x;
+      },
+      [&](int k, double c) {
+        cv[k] = c;
+        xf[ls * ls + k] = (float)c;
+      });
+  if (threadIdx.x == 0 && bad) B.fl[p].bad = 1;
+}
+
 // Chunk partials of the Gram matrix of U and of U_k·v_last (pair order of
 // k_gram), double-float sums: part[pair*nchunks + c].
 __global__ void __launch_bounds__(kNT) k_b_gram(const BatchDev B, const float* __restrict__ U,
@@ -616,10 +742,14 @@ void launch_b_restart(const BatchDev& B, float* V, float* U, cudaStream_t st) {
   const int NP = ls * (ls + 1) / 2 + ls;
   k_b_jacobi<<<B.nprob, 256, jacobi_smem(m), st>>>(B, m, 1);
   k_b_restart_small<<<B.nprob, 256, 0, st>>>(B);
-  k_b_rotate<<<B.nchunks, kNT, 0, st>>>(B, V, U);
+  const bool reg = ls <= kBRLS && sizeof(float) * (size_t)m * kBRLS <= 48 * 1024;
+  if (reg) k_b_rotate_r<<<B.nchunks, kNT, sizeof(float) * m * kBRLS, st>>>(B, V, U);
+  else k_b_rotate<<<B.nchunks, kNT, 0, st>>>(B, V, U);
   k_b_gram<<<B.nchunks, kNT, sizeof(float) * (ls + 1) * 64, st>>>(B, U, V + (int64_t)(B.lm - 1) * B.LEN);
-  k_b_chol<<<B.nprob, 128, sizeof(double) * (NP + ls * ls), st>>>(B);
-  k_b_apply<<<B.nchunks, kNT, 0, st>>>(B, U, V);
+  if (ls <= 32) k_b_chol_df<<<B.nprob, 32, 0, st>>>(B);
+  else k_b_chol<<<B.nprob, 128, sizeof(double) * (NP + ls * ls), st>>>(B);
+  if (reg) k_b_apply_r<<<B.nchunks, kNT, 0, st>>>(B, U, V);
+  else k_b_apply<<<B.nchunks, kNT, 0, st>>>(B, U, V);
 }
 void launch_b_jacobi_one(const BatchDev& B, int p, int n, cudaStream_t st) {
   k_b_jacobi_one<<<1, 256, jacobi_smem(n), st>>>(B, p, n);
