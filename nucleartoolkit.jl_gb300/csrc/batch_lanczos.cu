@@ -517,6 +517,75 @@ __global__ void __launch_bounds__(kNT) k_b_apply_r(const BatchDev B, const float
   }
 }
 
+// The Gram partials with one thread per pair (ls <= 16): tiles of 128
+// elements with padded rows (no bank conflicts), double-buffered through
+// registers, FP32 sums per tile added in double-float.
+__global__ void __launch_bounds__(kNT) k_b_gram_r(const BatchDev B, const float* __restrict__ U,
+                                                  const float* __restrict__ Vlast) {
+  const int c = blockIdx.x;
+  const int4 ch = B.chunks[c];
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  const BatchProblemDev& P = B.probs[ch.x];
+  constexpr int TILE = 128, TS = TILE + 1;
+  constexpr int LD = ((kBRLS + 1) * TILE + kNT - 1) / kNT;
+  extern __shared__ float gt[];  // 2 x (ls+1) x TS
+  const int ls = B.ls, nv = ls + 1;
+  const int NP = ls * (ls + 1) / 2 + ls;
+  const float* __restrict__ Ub = U + P.voff;
+  const float* __restrict__ vl = Vlast + P.voff;
+  const bool act = (int)threadIdx.x < NP;
+  int k = 0, l = 0;
+  if (act) gram_pair(threadIdx.x, ls, k, l);
+  DFAcc acc;
+  acc.init();
+  float st[LD];
+  auto load = [&](int64_t t0) {
+#pragma unroll
+    for (int u = 0; u < LD; ++u) {
+      const int idx = threadIdx.x + u * kNT;
+      const int j = idx / TILE, x = idx % TILE;
+      float val = 0.f;
+      if (j < nv && t0 + x < ch.z) val = (j < ls) ? Ub[(int64_t)j * B.LEN + t0 + x] : vl[t0 + x];
+      st[u] = val;
+    }
+  };
+  auto store = [&](int buf) {
+    float* tl = gt + buf * nv * TS;
+#pragma unroll
+    for (int u = 0; u < LD; ++u) {
+      const int idx = threadIdx.x + u * kNT;
+      const int j = idx / TILE, x = idx % TILE;
+      if (j < nv) tl[j * TS + x] = st[u];
+    }
+  };
+  int buf = 0;
+  if (ch.y < ch.z) {
+    load(ch.y);
+    store(0);
+  }
+  __syncthreads();
+  for (int64_t t0 = ch.y; t0 < ch.z; t0 += TILE) {
+    const bool more = t0 + TILE < ch.z;
+    if (more) load(t0 + TILE);
+    const float* tl = gt + buf * nv * TS;
+    if (act) {
+      const int cnt = (int)min((int64_t)TILE, ch.z - t0);
+      float p0 = 0.f, p1 = 0.f;
+      int x = 0;
+      for (; x + 1 < cnt; x += 2) {
+        p0 = __fmaf_rn(tl[k * TS + x], tl[l * TS + x], p0);
+        p1 = __fmaf_rn(tl[k * TS + x + 1], tl[l * TS + x + 1], p1);
+      }
+      if (x < cnt) p0 = __fmaf_rn(tl[k * TS + x], tl[l * TS + x], p0);
+      df_add(acc.hi, acc.lo, __fadd_rn(p0, p1), 0.f);
+    }
+    if (more) store(buf ^ 1);
+    __syncthreads();
+    buf ^= 1;
+  }
+  if (act) B.part[(int64_t)threadIdx.x * B.nchunks + c] = acc.get();
+}
+
 // Each problem's Cholesky on one warp in double-float (chol_df_warp); the
 // Gram entries summed over the problem's chunks first.
 __global__ void __launch_bounds__(32) k_b_chol_df(const BatchDev B) {
@@ -745,7 +814,10 @@ void launch_b_restart(const BatchDev& B, float* V, float* U, cudaStream_t st) {
   const bool reg = ls <= kBRLS && sizeof(float) * (size_t)m * kBRLS <= 48 * 1024;
   if (reg) k_b_rotate_r<<<B.nchunks, kNT, sizeof(float) * m * kBRLS, st>>>(B, V, U);
   else k_b_rotate<<<B.nchunks, kNT, 0, st>>>(B, V, U);
-  k_b_gram<<<B.nchunks, kNT, sizeof(float) * (ls + 1) * 64, st>>>(B, U, V + (int64_t)(B.lm - 1) * B.LEN);
+  if (ls <= kBRLS && NP <= kNT)
+    k_b_gram_r<<<B.nchunks, kNT, sizeof(float) * 2 * (ls + 1) * 129, st>>>(B, U, V + (int64_t)(B.lm - 1) * B.LEN);
+  else
+    k_b_gram<<<B.nchunks, kNT, sizeof(float) * (ls + 1) * 64, st>>>(B, U, V + (int64_t)(B.lm - 1) * B.LEN);
   if (ls <= 32) k_b_chol_df<<<B.nprob, 32, 0, st>>>(B);
   else k_b_chol<<<B.nprob, 128, sizeof(double) * (NP + ls * ls), st>>>(B);
   if (reg) k_b_apply_r<<<B.nchunks, kNT, 0, st>>>(B, U, V);
