@@ -652,7 +652,8 @@ __global__ void __launch_bounds__(32) k_m_chol_df(const double* __restrict__ gra
 }
 
 // Gram matrices of U_s (packed upper triangle) and U_k,s·v_last,s for every
-// sample, double-float sums.  Pair order as k_gram; c = pair*S + s.
+// sample: FP32 sums per tile, double-float across tiles.  Pair order as
+// k_gram; c = pair*S + s.
 template <int S>
 __global__ void __launch_bounds__(kNT) k_m_gram(const float* __restrict__ U, const float* __restrict__ vl, int ls,
                                                 int64_t len, int tile, double* __restrict__ part, int G,
@@ -692,7 +693,10 @@ __global__ void __launch_bounds__(kNT) k_m_gram(const float* __restrict__ U, con
         const int s = c % S;
         const float* a = tl + kk[q] * TS + s;
         const float* b = tl + ll[q] * TS + s;
-        for (int x = 0; x < cnt; ++x) dacc[q].add_prod(a[x * S], b[x * S]);
+        // the tile's products summed in FP32, the tile sums in double-float
+        float p = 0.f;
+        for (int x = 0; x < cnt; ++x) p = __fmaf_rn(a[x * S], b[x * S], p);
+        df_add(dacc[q].hi, dacc[q].lo, p, 0.f);
       }
       __syncthreads();
     }
