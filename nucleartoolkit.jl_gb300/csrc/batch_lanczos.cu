@@ -125,10 +125,13 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
   // products in double-float on the FP32 pipe.
   float* __restrict__ wh = B.wsplit + P.voff;
   float* __restrict__ wl = B.wsplit + B.LEN + P.voff;
+  // FP32 per-thread sums of the projections (a thread adds a handful of
+  // products of one chunk; their rounding is far below the FP32 basis), the
+  // CTA sums in double-float
   for (int j0 = 0; j0 <= m; j0 += 8) {
-    DFAcc acc[8];
+    float acc[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) acc[q].init();
+    for (int q = 0; q < 8; ++q) acc[q] = 0.f;
     for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
       float h[4], l[4];
       if (j0 == 0) {
@@ -154,19 +157,21 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
         const int j = j0 + q;
         if (j < m) {
           const float4 x = *reinterpret_cast<const float4*>(Vb + (int64_t)j * B.LEN + i);
-          acc[q].add_prod2(x.x, h[0], l[0]);
-          acc[q].add_prod2(x.y, h[1], l[1]);
-          acc[q].add_prod2(x.z, h[2], l[2]);
-          acc[q].add_prod2(x.w, h[3], l[3]);
+          acc[q] = __fmaf_rn(x.w, h[3], __fmaf_rn(x.z, h[2], __fmaf_rn(x.y, h[1], __fmaf_rn(x.x, h[0], acc[q]))));
         } else if (j == m) {
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q].add_prod2(h[u], h[u], 2.0f * l[u]);
+          acc[q] = __fmaf_rn(h[3], h[3], __fmaf_rn(h[2], h[2], __fmaf_rn(h[1], h[1], __fmaf_rn(h[0], h[0], acc[q]))));
         }
       }
     }
     // the eight sums in one double-float CTA reduction on the FP32 pipe
+    DFAcc dacc[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      dacc[q].hi = acc[q];
+      dacc[q].lo = 0.f;
+    }
     float2 s;
-    block_sum_df<kNT, 8>(acc, red8, s);
+    block_sum_df<kNT, 8>(dacc, red8, s);
     if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m)
       B.pdot[(int64_t)(j0 + threadIdx.x) * B.nchunks + c] = (double)s.x + (double)s.y;
   }
