@@ -163,16 +163,28 @@ __global__ void k_onebody(const uint64_t* __restrict__ bits, int64_t N, const ui
 // same block (prep_2bjumps).  A pair below the diagonal takes the value and
 // sign of the conjugate operator, as the reference stores it on the other
 // row.
+// One warp per row: lane l takes the l-th contiguous slice of the operator
+// list, so the lanes' entries concatenated in lane order are in list order.
+__device__ __forceinline__ void op_slice(int nops, int lane, int& k0, int& k1) {
+  const int per = (nops + 31) / 32;
+  k0 = min(nops, lane * per);
+  k1 = min(nops, k0 + per);
+}
+
 __global__ void __launch_bounds__(kT) k_2b_count(const Op2* __restrict__ ops, int nops,
                                                  const uint64_t* __restrict__ bits, const int* __restrict__ start,
                                                  int nb, int64_t nrow, int* __restrict__ cnt) {
-  for (int64_t g = blockIdx.x * (int64_t)kT + threadIdx.x; g < nrow; g += (int64_t)gridDim.x * kT) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (kT / 32);
+  int k0, k1;
+  op_slice(nops, lane, k0, k1);
+  for (int64_t g = blockIdx.x * (int64_t)(kT / 32) + (threadIdx.x >> 5); g < nrow; g += nwarps) {
     const int b = block_of(start, nb, g);
     const uint64_t* blk = bits + start[b];
     const int n = start[b + 1] - start[b];
     const uint64_t sd = bits[g];
     int c = 0;
-    for (int k = 0; k < nops; ++k) {
+    for (int k = k0; k < k1; ++k) {
       const Op2 o = ops[k];
       if (o.v == 0.0) continue;
       uint64_t f;
@@ -181,7 +193,9 @@ __global__ void __launch_bounds__(kT) k_2b_count(const Op2* __restrict__ ops, in
       if (sd_find_desc(blk, n, f) < 0) continue;
       ++c;
     }
-    cnt[g] = c;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) cnt[g] = c;
   }
 }
 
@@ -189,14 +203,35 @@ __global__ void __launch_bounds__(kT) k_2b_fill(const Op2* __restrict__ ops, con
                                                 const uint64_t* __restrict__ bits, const int* __restrict__ start,
                                                 int nb, int64_t nrow, const int64_t* __restrict__ off,
                                                 int* __restrict__ col, double* __restrict__ val) {
-  for (int64_t g = blockIdx.x * (int64_t)kT + threadIdx.x; g < nrow; g += (int64_t)gridDim.x * kT) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (kT / 32);
+  int k0, k1;
+  op_slice(nops, lane, k0, k1);
+  for (int64_t g = blockIdx.x * (int64_t)(kT / 32) + (threadIdx.x >> 5); g < nrow; g += nwarps) {
     const int b = block_of(start, nb, g);
     const uint64_t* blk = bits + start[b];
     const int n = start[b + 1] - start[b];
     const int i = (int)(g - start[b]);
     const uint64_t sd = bits[g];
-    int64_t w = off[g];
-    for (int k = 0; k < nops; ++k) {
+    // this lane's count, then its offset by an exclusive warp scan
+    int c = 0;
+    for (int k = k0; k < k1; ++k) {
+      const Op2 o = ops[k];
+      if (o.v == 0.0) continue;
+      uint64_t f;
+      int odd;
+      if (!sd_apply2(sd, o.a, o.b, o.c, o.d, f, odd)) continue;
+      if (sd_find_desc(blk, n, f) < 0) continue;
+      ++c;
+    }
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int64_t w = off[g] + (incl - c);
+    for (int k = k0; k < k1; ++k) {
       const Op2 o = ops[k];
       if (o.v == 0.0) continue;
       uint64_t f;
@@ -444,13 +479,14 @@ void build_2b_device(DeviceArena& A, const std::vector<Op2>& ops, const uint64_t
   int* cnt = A.alloc<int>(nrow);
   int64_t* off = A.alloc<int64_t>(nrow);
   const int nops = (int)ops.size();
-  k_2b_count<<<grid_for(nrow), kT, 0, st>>>(d_ops, nops, d_bits, d_start, nb, nrow, cnt);
+  const int gw = (int)std::min<int64_t>((nrow + kT / 32 - 1) / (kT / 32), 65535);  // one warp per row
+  k_2b_count<<<gw, kT, 0, st>>>(d_ops, nops, d_bits, d_start, nb, nrow, cnt);
   const int64_t raw = scan_exclusive<int>(A, cnt, nrow, off, st);
   int* craw = A.alloc<int>(raw);
   double* vraw = A.alloc<double>(raw);
   int* mcnt = A.alloc<int>(nrow);
   int64_t* moff = A.alloc<int64_t>(nrow);
-  k_2b_fill<<<grid_for(nrow), kT, 0, st>>>(d_ops, d_conj, nops, d_bits, d_start, nb, nrow, off, craw, vraw);
+  k_2b_fill<<<gw, kT, 0, st>>>(d_ops, d_conj, nops, d_bits, d_start, nb, nrow, off, craw, vraw);
   k_2b_merge<<<grid_for(nrow), kT, 0, st>>>(nrow, off, cnt, craw, vraw, mcnt);
   const int64_t total = scan_exclusive<int>(A, mcnt, nrow, moff, st);
   if (total >= (1ll << 31)) throw SetupError{SMGPU_ERR_LIMIT, "two-body jump table too large"};
