@@ -222,11 +222,27 @@ double clebsch_gordan(int tj1, int tm1, int tj2, int tm2, int tJ, int tM) {
     return clebsch_gordan_exact(tj1, tm1, tj2, tm2, tJ, tM);
   const uint64_t key = ((uint64_t)tj1 << 52) | ((uint64_t)(tm1 + 1024) << 40) | ((uint64_t)tj2 << 31) |
                        ((uint64_t)(tm2 + 1024) << 19) | ((uint64_t)tJ << 9) | (uint64_t)((tM + 2048) & 0x1ff);
+  // a direct-mapped cache in front of the map (a shell-model set-up asks for
+  // a few thousand distinct coefficients some 10^5 times)
+  struct Ent {
+    uint64_t key;
+    int tM;
+    double v;
+  };
+  constexpr int kCache = 8192;
+  thread_local std::vector<Ent> cache(kCache, Ent{~0ull, 0, 0.0});
+  Ent& c = cache[(size_t)((key * 0x9E3779B97F4A7C15ull) >> 51) & (kCache - 1)];
+  if (c.key == key && c.tM == tM) return c.v;
   thread_local std::unordered_map<uint64_t, std::pair<int, double>> memo;
   auto it = memo.find(key);
-  if (it != memo.end() && it->second.first == tM) return it->second.second;
-  const double v = clebsch_gordan_exact(tj1, tm1, tj2, tm2, tJ, tM);
-  memo[key] = {tM, v};
+  double v;
+  if (it != memo.end() && it->second.first == tM) {
+    v = it->second.second;
+  } else {
+    v = clebsch_gordan_exact(tj1, tm1, tj2, tm2, tJ, tM);
+    memo[key] = {tM, v};
+  }
+  c = Ent{key, tM, v};
   return v;
 }
 
@@ -363,19 +379,40 @@ struct Key4H {
     return (size_t)(h ^ (h >> 32));
   }
 };
+// Where an operator (one-hot masks a, b, c, d) sits in its list: a dense
+// array over the four bit positions when the m-state counts are small (the
+// shell-model spaces in practice), a hash map otherwise.  Each key belongs to
+// one list, so several lists can share one index.
+struct OpIndex {
+  int La = 0, Lb = 0;
+  bool dense = false;
+  std::vector<int32_t> slot;
+  std::unordered_map<Key4, int32_t, Key4H> map;
+  OpIndex(int la, int lb) : La(la), Lb(lb) {
+    const size_t n = (size_t)la * la * lb * lb;
+    dense = n <= ((size_t)1 << 22);
+    if (dense) slot.assign(n, -1);
+  }
+  static int pos(uint64_t m) { return __builtin_ctzll(m); }
+  // the slot of the key (-1: new; the caller then stores its position)
+  int32_t& at(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+    if (dense) return slot[(((size_t)pos(a) * Lb + pos(b)) * La + pos(c)) * Lb + pos(d)];
+    auto it = map.emplace(Key4{a, b, c, d}, -1).first;
+    return it->second;
+  }
+};
+
 // Operator list with first-insertion order and in-place accumulation: same
 // order and sums as the reference's `tl in blist` linear search.
 struct OpList {
   std::vector<Op2> ops;
-  std::unordered_map<Key4, size_t, Key4H> where;
-  void add(uint64_t a, uint64_t b, uint64_t c, uint64_t d, double v) {
-    Key4 k{a, b, c, d};
-    auto it = where.find(k);
-    if (it == where.end()) {
-      where.emplace(k, ops.size());
+  void add(OpIndex& ix, uint64_t a, uint64_t b, uint64_t c, uint64_t d, double v) {
+    int32_t& w = ix.at(a, b, c, d);
+    if (w < 0) {
+      w = (int32_t)ops.size();
       ops.push_back(Op2{a, b, c, d, v});
     } else {
-      ops[it->second].v += v;
+      ops[w].v += v;
     }
   }
 };
@@ -400,6 +437,7 @@ std::vector<Op2> two_body_ops(const std::vector<Interaction::TB>& tbs, const std
                               const std::vector<MState>& ms, int loff) {
   int L = (int)ms.size();
   OpList list;
+  OpIndex ix(L, L);
   for (const auto& t : tbs) {
     int oa = t.a - 1 - loff, ob = t.b - 1 - loff, oc = t.c - 1 - loff, od = t.d - 1 - loff;
     auto ia = mstates_of(ms, oa), ib = mstates_of(ms, ob), ic = mstates_of(ms, oc), id = mstates_of(ms, od);
@@ -418,7 +456,7 @@ std::vector<Op2> two_body_ops(const std::vector<Interaction::TB>& tbs, const std
             if (ma + mb != Mani) continue;
             double cg1 = clebsch_gordan(orb[oa].j2, ma, orb[ob].j2, mb, J2, Mani);
             double cg2 = clebsch_gordan(orb[oc].j2, mc, orb[od].j2, md, J2, Mani);
-            list.add(bit_of(L, ka), bit_of(L, kb), bit_of(L, kc), bit_of(L, kd), t.v * nfac * cg1 * cg2);
+            list.add(ix, bit_of(L, ka), bit_of(L, kb), bit_of(L, kc), bit_of(L, kd), t.v * nfac * cg1 * cg2);
           }
       }
   }
@@ -457,26 +495,54 @@ void build_operators(const Interaction& I, Tables& T) {
     std::reverse(Mzs.begin(), Mzs.end());
     T.delMs = Mzs;
     std::vector<OpList> lists(Mzs.size());
+    OpIndex ix(T.Lp, T.Ln);  // a key's ΔM fixes its list
+    // m-state lists of every orbit, and the list index of every ΔM value
+    std::vector<std::vector<int>> mp_of(I.porb.size()), mn_of(I.norb.size());
+    for (size_t o = 0; o < I.porb.size(); ++o) mp_of[o] = mstates_of(T.msp, (int)o);
+    for (size_t o = 0; o < I.norb.size(); ++o) mn_of[o] = mstates_of(T.msn, (int)o);
+    const int dm0 = Mzs.empty() ? 0 : Mzs.back();
+    std::vector<int> dm_idx(Mzs.empty() ? 0 : (size_t)(Mzs.front() - dm0 + 1), (int)Mzs.size());
+    for (size_t k = 0; k < Mzs.size(); ++k) dm_idx[Mzs[k] - dm0] = (int)k;
+    std::vector<double> cgcd, cgab;
     for (const auto& t : I.tb[2]) {
       int oa = t.a - 1, oc = t.c - 1, ob = t.b - 1 - I.lp, od = t.d - 1 - I.lp;
-      auto ia = mstates_of(T.msp, oa), ic = mstates_of(T.msp, oc);
-      auto ib = mstates_of(T.msn, ob), id = mstates_of(T.msn, od);
+      const std::vector<int>& ia = mp_of[oa];
+      const std::vector<int>& ic = mp_of[oc];
+      const std::vector<int>& ib = mn_of[ob];
+      const std::vector<int>& id = mn_of[od];
       int J2 = 2 * t.J;
-      for (int kc : ic) {
+      // the line's Clebsch–Gordan coefficients, once per m-state pair
+      cgcd.assign(ic.size() * id.size(), 0.0);
+      for (size_t u = 0; u < ic.size(); ++u)
+        for (size_t w = 0; w < id.size(); ++w) {
+          const int mc = T.msp[ic[u]].m2, md = T.msn[id[w]].m2;
+          if (std::abs(mc + md) <= J2) cgcd[u * id.size() + w] = clebsch_gordan(I.porb[oc].j2, mc, I.norb[od].j2, md, J2, mc + md);
+        }
+      cgab.assign(ia.size() * ib.size(), 0.0);
+      for (size_t u = 0; u < ia.size(); ++u)
+        for (size_t w = 0; w < ib.size(); ++w) {
+          const int ma = T.msp[ia[u]].m2, mb = T.msn[ib[w]].m2;
+          cgab[u * ib.size() + w] = clebsch_gordan(I.porb[oa].j2, ma, I.norb[ob].j2, mb, J2, ma + mb);
+        }
+      for (size_t uc = 0; uc < ic.size(); ++uc) {
+        const int kc = ic[uc];
         int mc = T.msp[kc].m2;
-        for (int ka : ia) {
+        for (size_t ua = 0; ua < ia.size(); ++ua) {
+          const int ka = ia[ua];
           int ma = T.msp[ka].m2;
           int Mp = ma - mc;
-          int idx = (int)(std::find(Mzs.begin(), Mzs.end(), Mp) - Mzs.begin());
-          for (int kd : id) {
+          int idx = dm_idx[Mp - dm0];
+          for (size_t ud = 0; ud < id.size(); ++ud) {
+            const int kd = id[ud];
             int md = T.msn[kd].m2;
             if (std::abs(mc + md) > J2) continue;
-            double tfac = t.v * clebsch_gordan(I.porb[oc].j2, mc, I.norb[od].j2, md, J2, mc + md);
-            for (int kb : ib) {
+            double tfac = t.v * cgcd[uc * id.size() + ud];
+            for (size_t ub = 0; ub < ib.size(); ++ub) {
+              const int kb = ib[ub];
               int mb = T.msn[kb].m2;
               if (mb - md + Mp != 0) continue;
-              double fac = tfac * clebsch_gordan(I.porb[oa].j2, ma, I.norb[ob].j2, mb, J2, ma + mb);
-              lists[idx].add(bit_of(T.Lp, ka), bit_of(T.Ln, kb), bit_of(T.Lp, kc), bit_of(T.Ln, kd), fac);
+              double fac = tfac * cgab[ua * ib.size() + ub];
+              lists[idx].add(ix, bit_of(T.Lp, ka), bit_of(T.Ln, kb), bit_of(T.Lp, kc), bit_of(T.Ln, kd), fac);
             }
           }
         }
