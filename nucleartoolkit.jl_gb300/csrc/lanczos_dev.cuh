@@ -361,6 +361,9 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
   }
 }
 
+template <int NT>
+__device__ __forceinline__ float2 block_sum_df2(float h, float l, float2* red);
+
 // (h, l) = (ah + al)(bh + bl) in double-float.
 __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& h, float& l) {
   const float p = __fmul_rn(ah, bh);
@@ -382,7 +385,6 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
 template <int NT>
 __device__ inline void jacobi_eig_df(const double* __restrict__ T, int ldt, int n, double* A, double* evals) {
   __shared__ double red[NT / 32];
-  __shared__ int s_stop;
   extern __shared__ double shj[];
   const int N = n + (n & 1);
   const int npair = N / 2;
@@ -402,24 +404,24 @@ __device__ inline void jacobi_eig_df(const double* __restrict__ T, int ldt, int 
     Z_[idx] = make_float2(i == j ? 1.f : 0.f, 0.f);
   }
   __syncthreads();
-  double fro = 0.0;
+  // the Frobenius norm² in double-float and the per-sweep test by a barrier
+  // vote: no FP64 reduction (slow on this GPU) in the sweep loop
+  float fh = 0.f, fl = 0.f;
   for (int idx = tid; idx < n * n; idx += NT) {
-    const double h = (double)A_[idx].x;
-    fro += h * h;
+    const float h = A_[idx].x;
+    const float p = __fmul_rn(h, h);
+    df_add(fh, fl, p, __fmaf_rn(h, h, -p));
   }
-  fro = block_sum_all<NT>(fro, red);
-  const float thr = (float)(1e-28 * fro);
+  const float2 fro2 = block_sum_df2<NT>(fh, fl, reinterpret_cast<float2*>(red));
+  const float thr = 1e-28f * fro2.x;
   for (int sweep = 0; sweep < 64; ++sweep) {
-    double cnt = 0.0;
+    int above = 0;
     for (int idx = tid; idx < n * n; idx += NT) {
       const int i = idx % n, j = idx / n;
       const float a = A_[idx].x;
-      if (i < j && a * a > thr) cnt += 1.0;
+      if (i < j && a * a > thr) above = 1;
     }
-    cnt = block_sum_all<NT>(cnt, red);
-    if (tid == 0) s_stop = cnt == 0.0 ? 1 : 0;
-    __syncthreads();
-    if (s_stop) break;
+    if (!__syncthreads_or(above)) break;
   for (int r = 0; r < N - 1; ++r) {
       for (int k = tid; k < npair; k += NT) {
         int p, q;
