@@ -27,7 +27,6 @@
 // with Kahan compensation per (row, link) as in the row-tile kernel.  The nn
 // term gathers from the CTA's rows of v staged in shared memory; pp, the
 // one-body term and the Lanczos epilogue are those of hv_tile.cuh.
-#include <cstdio>
 
 #include "device.cuh"
 #include "hv_tile.cuh"
