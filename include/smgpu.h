@@ -370,9 +370,10 @@ int smgpu_batch_matvec(smgpu_batch* h, const double* v, double* w, int accumulat
 int smgpu_batch_solve(smgpu_batch* h, int num_ev, int lm, int ls, double tol, int max_restarts,
                       const double* v1, double* evals_out, double* evecs_out, int* stats_out);
 
-/* Statistics (8 entries): [multiply-adds per batched H·v, problems, chunks,
+/* Statistics (9 entries): [multiply-adds per batched H·v, problems, chunks,
  * H·v tasks, and the autotuned launch shape: threads per CTA, rows per CTA,
- * minimum CTAs per SM; device table bytes]. */
+ * minimum CTAs per SM; device table bytes; 1 when that shape is the staged
+ * pn form]. */
 int smgpu_batch_stats(const smgpu_batch* h, long long* stats_out);
 
 /* As smgpu_timings, for the last create / solve / matvec call on h. */

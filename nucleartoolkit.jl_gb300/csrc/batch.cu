@@ -47,6 +47,7 @@ struct smgpu_batch {
   std::map<int, std::pair<int4*, int>> tasks;                 // rows per task -> (device list, count)
   std::map<int, std::vector<std::pair<int, int>>> slots;      // rows per task -> per problem (slot0, nslots)
   int cand = 4;
+  size_t smem = 0;  // dynamic shared memory of the selected shape
   double tune_ms[16] = {0};
   std::string err;
   double times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -96,9 +97,32 @@ struct smgpu_batch {
     slots[R] = sl;
   }
 
+  // Dynamic shared memory of a staged launch shape (the largest over the
+  // problems) and whether every problem fits it; 0 / true for the others.
+  size_t staged_smem(int c) const {
+    int nc = 0;
+    const BatchHvConfig& k = hv_batch_candidates(&nc)[c];
+    if (!k.staged) return 0;
+    const HvConfig hc{k.nt, k.rows, 0, k.minb, 1};
+    size_t m = 0;
+    for (const smgpu_problem* p : P) m = std::max(m, hv_staged_smem(hc, p->tt));
+    return m;
+  }
+  bool fits(int c) const {
+    int nc = 0;
+    const BatchHvConfig& k = hv_batch_candidates(&nc)[c];
+    if (!k.staged) return true;
+    for (const smgpu_problem* p : P)
+      if (p->tt.push_ent == nullptr || p->nnmax_raw > hv_batch_staged_cols(k)) return false;
+    return staged_smem(c) <= 200 * 1024;
+  }
+
   // Select a launch shape; the per-problem α slot ranges follow its rows.
   void set_cand(int c) {
+    if (!fits(c)) throw SetupError{SMGPU_ERR_ARG, "batched H·v launch shape does not fit these problems"};
     cand = c;
+    smem = staged_smem(c);
+    if (smem > 0) hv_batch_prepare(c, smem);
     const int R = rows();
     ensure_tasks(R);
     for (int p = 0; p < nprob; ++p) {
@@ -112,7 +136,7 @@ struct smgpu_batch {
 
   void hv(const float* v, double* w, const BatchEpi& e, cudaStream_t s) {
     const auto& tk = tasks[rows()];
-    launch_hv_batch(cand, d_probs, tk.first, tk.second, v, w, e, s);
+    launch_hv_batch(cand, d_probs, tk.first, tk.second, v, w, e, smem, s);
   }
 
   BatchDev view() const {
@@ -204,6 +228,7 @@ void smgpu_batch::autotune() {
     int best = cand;
     float best_ms = 1e30f;
     for (int c = 0; c < nc; ++c) {
+      if (!fits(c)) continue;
       set_cand(c);
       float total = 0.f;
       for (int rep = 0; rep < 3; ++rep) {
@@ -627,6 +652,7 @@ int smgpu_batch_stats(const smgpu_batch* h, long long* s) {
   s[5] = c[h->cand].rows;
   s[6] = c[h->cand].minb;
   s[7] = bytes;
+  s[8] = c[h->cand].staged;
   return SMGPU_OK;
 }
 

@@ -71,11 +71,17 @@ struct BatchEpi {
 
 struct BatchHvConfig {
   int nt, rows, minb;
+  int staged;  // 1: the staged pn row body (hv_staged.cuh); 0: the row-tile body
 };
 const BatchHvConfig* hv_batch_candidates(int* count);
-// tasks: (problem, block, first row, α slot), cand: index into hv_batch_candidates()
+// Column capacity (threads x columns per thread) of a staged batch shape.
+int hv_batch_staged_cols(const BatchHvConfig& c);
+// tasks: (problem, block, first row, α slot), cand: index into hv_batch_candidates();
+// smem: dynamic shared memory of a staged shape (the largest over the problems)
 void launch_hv_batch(int cand, const BatchProblemDev* probs, const int4* tasks, int ntasks, const float* v, double* w,
-                     const BatchEpi& epi, cudaStream_t st);
+                     const BatchEpi& epi, size_t smem, cudaStream_t st);
+// One-time set-up of a staged shape's shared-memory size (before graph capture).
+void hv_batch_prepare(int cand, size_t smem);
 
 void launch_b_start(const BatchDev& B, uint64_t seed, double* w, cudaStream_t st);
 void launch_b_to_padded(const BatchDev& B, const double* src, double* w, cudaStream_t st);  // src: problems' mdim concatenated

@@ -297,9 +297,10 @@ class BatchProblem:
         return [x[o:o + m] for o, m in zip(self.moff, self.mdims)]
 
     def stats(self):
-        s = np.zeros(8, dtype=np.int64)
+        s = np.zeros(9, dtype=np.int64)
         _lib.check_batch(load().smgpu_batch_stats(self._h, _p(s)), self._h)
-        keys = ["updates", "problems", "chunks", "hv_tasks", "hv_threads", "hv_rows", "hv_min_ctas", "table_bytes"]
+        keys = ["updates", "problems", "chunks", "hv_tasks", "hv_threads", "hv_rows", "hv_min_ctas", "table_bytes",
+                "hv_staged"]
         return dict(zip(keys, map(int, s)))
 
     def timings(self):

@@ -73,6 +73,7 @@ def test_batch_matvec_every_launch_shape(lib, mixed_batch, monkeypatch):
     v = None
     refs = None
     ncand = 0
+    n_staged = 0
     while True:
         monkeypatch.setenv("SMGPU_BATCH_CAND", str(ncand))
         try:
@@ -86,8 +87,10 @@ def test_batch_matvec_every_launch_shape(lib, mixed_batch, monkeypatch):
         for p, ref in enumerate(refs):
             scale = max(np.abs(ref).max(), 1e-30)
             assert np.abs(w[p] - ref).max() <= MATVEC_MIXED_RTOL * scale, (ncand, p)
+        n_staged += G.stats()["hv_staged"]
         ncand += 1
     assert ncand >= 5
+    assert n_staged >= 1  # the staged pn row body ran on the batch
 
 
 def test_batch_solve_vs_oracle(lib, mixed_batch):
