@@ -197,7 +197,7 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
     if (r >= nr) break;
     const int g = pst + p0 + r;
     const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
-#pragma unroll 2
+#pragma unroll 8
     for (int k = kb; k < ke; ++k) {
       const float pv = a.c.pp_val[k];
       const float* __restrict__ src = v + blk + (int64_t)t.pp_col[k] * stride + tid;
@@ -212,7 +212,7 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
     const int W = tt.nnell_w[b];
     const int* __restrict__ ecol = tt.nnell_col + tt.nnell_off[b] + tid;
     const float* __restrict__ eval = tt.nnell_val + tt.nnell_off[b] + tid;
-#pragma unroll 2
+#pragma unroll 8
     for (int k = 0; k < W; ++k) {
 #pragma unroll
       for (int q = 0; q < QM; ++q) {
