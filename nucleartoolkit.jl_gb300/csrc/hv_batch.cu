@@ -1,8 +1,10 @@
 // Batched H·v: one launch over the row tiles of every problem of a batch
 // (operate_H!, src/ShellModel/lanczos_methods.jl:153-248, for many problems
 // at once).  Each CTA takes one task (problem, block, first row, α slot) from
-// a list sorted by estimated work, largest first, and runs the row-tile body
-// of hv.cu on that problem's tables and vector segment (FP32-mixed).  The
+// a list sorted by estimated work, largest first, and runs either the
+// row-tile body of hv.cu or the staged pn body of hv_staged.cu on that
+// problem's tables and vector segment (FP32-mixed; the autotuner picks the
+// launch shape, staged shapes only where every problem fits them).  The
 // per-problem tables are read through a reference into a device array, so a
 // CTA touches only the fields its rows use.
 #include "batch.cuh"
@@ -58,6 +60,8 @@ __global__ void __launch_bounds__(NT, MINB) hv_batch_staged_kernel(const BatchPr
                                      e.alpha_part != nullptr ? e.alpha_part + tk.w : nullptr);
 }
 
+// {threads, rows, min CTAs per SM, staged}; launch_hv_batch and staged_case
+// map each index to its template instance.
 constexpr BatchHvConfig kBatchCand[] = {
     {32, 4, 1, 0},  {64, 2, 1, 0},  {64, 4, 1, 0},  {128, 1, 1, 0}, {128, 2, 1, 0}, {128, 4, 1, 0},
     {128, 2, 6, 0}, {256, 2, 1, 0}, {64, 1, 8, 1},  {128, 1, 4, 1}, {128, 1, 5, 1}, {128, 2, 3, 1},
