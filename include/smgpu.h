@@ -43,9 +43,17 @@ enum smgpu_status_code {
 
 /* Arithmetic of the H·v and of the Krylov basis storage. */
 enum smgpu_precision {
-  SMGPU_FP64 = 0,   /* plain form: everything FP64 */
-  SMGPU_MIXED = 1   /* H·v and Krylov storage FP32 with compensated sums; recurrences,
-                       re-orthogonalisation, tridiagonal solves and Ritz vectors FP64 */
+  SMGPU_FP64 = 0,     /* plain form: everything FP64 */
+  SMGPU_MIXED = 1,    /* H·v and Krylov storage FP32 (FP32 products and partial sums, the
+                         partial sums of a row combined with Kahan compensation); the Lanczos
+                         residual, α/β, both re-orthogonalisation passes, the restart's
+                         tridiagonal/arrowhead eigensolve, its Gram matrix, Cholesky factor and
+                         basis update, and the Ritz vectors FP64.  The restart's basis rotation
+                         (whose result is stored in FP32) runs in compensated FP32. */
+  SMGPU_MIXED_DF = 2  /* as SMGPU_MIXED, except that the residual, the re-orthogonalisation,
+                         the restart eigensolve, Gram matrix and Cholesky factor run in
+                         double-float arithmetic (pairs of FP32 numbers, about 48 significant
+                         bits) on the FP32 pipe instead of FP64 */
 };
 
 /* Orbits are given as in an snt file: n, l, 2j, 2tz (tz = -1 proton, +1 neutron). */
@@ -217,6 +225,13 @@ int smgpu_timings(const smgpu_problem* h, double* times_out);
  * ms_out: mean milliseconds per launch. */
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
+/* Read bandwidth (GB/s) of a device buffer of `bytes` (1 MB .. 1 GB) that
+ * stays resident in the L2 cache: `reps` passes of the library's own read
+ * kernel over the buffer, CUDA events, after one untimed pass.  No
+ * counterpart in the reference: the ceiling against which the H·v kernels,
+ * whose tables and vectors fit in L2, are measured. */
+int smgpu_l2_read_bandwidth(long long bytes, int reps, double* gbs_out);
+
 /* The H·v autotuner's measurements for this handle (no counterpart in the
  * reference, whose operate_H! has one form): *count = number of candidate
  * launch shapes timed when the handle was created (0 when the shape came
@@ -234,11 +249,11 @@ int smgpu_tune_report(const smgpu_problem* h, int max, int* shapes, double* ms, 
 int smgpu_stats(const smgpu_problem* h, long long* stats_out);
 
 /* H·v that allocates nothing.  No counterpart in the reference: it exists for
- * callers that cannot have the library allocate device memory while they run
- * — code recording a CUDA stream capture (allocation is not capturable) and
- * hosts whose device memory is owned by their own pool allocator (a Julia
- * CuArray pool, a PyTorch caching allocator), which must not see cudaMalloc
- * or cudaFree from a library in the middle of a step.
+ * callers whose device memory is owned by their own pool allocator (a Julia
+ * CuArray pool, PyTorch's caching allocator).  Such a pool usually holds most
+ * of the device's memory, so a library's cudaMalloc in the middle of a step
+ * can fail or force the pool to release its cache, and a cudaFree
+ * synchronizes the whole device, stalling the host's queued work.
  *   v, w : caller-owned DEVICE buffers of mdim doubles in the reference's
  *          basis order (the layout of smgpu_matvec's host vectors);
  *          w = H v is overwritten, the FP64 form is used;
@@ -246,11 +261,14 @@ int smgpu_stats(const smgpu_problem* h, long long* stats_out);
  * The only scratch, the per-CTA partial sums of <v|H|v>, is a file-scope
  * device array of 65,536 doubles (512 KB) that every GPU loading the library
  * holds until exit; problems whose H·v launch has more CTAs than that, and
- * handles created with SMGPU_MIXED, are rejected (SMGPU_ERR_LIMIT /
+ * handles created with a mixed precision, are rejected (SMGPU_ERR_LIMIT /
  * SMGPU_ERR_ARG).  The first call on a device looks up the array's device
- * address; make that first call before any stream capture.  All calls share
- * the array (each call rewrites every entry it reads), so calls that overlap
- * on the GPU race; the call returns when w and *vhv are ready. */
+ * address and caches it for the process (cudaDeviceReset between calls is
+ * not supported).  The kernels run on the handle's own stream, which is not
+ * ordered with the caller's streams: all device work writing v must be
+ * finished before the call (e.g. by a stream or device synchronize); the call
+ * returns when w and *vhv are ready.  All calls share the array (each call
+ * rewrites every entry it reads), so calls that overlap on the GPU race. */
 int smgpu_matvec_noalloc(smgpu_problem* h, const double* v, double* w, double* vhv);
 
 /* ------------------------------------------------------------------------

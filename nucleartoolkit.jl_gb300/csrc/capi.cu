@@ -76,7 +76,8 @@ void tune_file_store() {
 }  // namespace
 
 void smgpu_problem::autotune() {
-  ShapeKey key{precision, T.Lp, T.Ln, vp, vn, mtot2};
+  // both FP32-mixed forms run the same H·v kernels: one cache entry
+  ShapeKey key{precision == SMGPU_FP64 ? SMGPU_FP64 : SMGPU_MIXED, T.Lp, T.Ln, vp, vn, mtot2};
   // SMGPU_HV_SHAPE="threads,rows,min_ctas,staged" selects one candidate
   // launch shape outright (for tests that run every shape); unknown or
   // non-fitting shapes are an error.
@@ -205,7 +206,8 @@ int guarded(smgpu_problem* h, F&& f) {
 }
 
 int create_common(const Interaction& I, int vp, int vn, int mtot2, int precision, smgpu_problem** out) {
-  if (precision != SMGPU_FP64 && precision != SMGPU_MIXED) throw SetupError{SMGPU_ERR_ARG, "unknown precision"};
+  if (precision != SMGPU_FP64 && precision != SMGPU_MIXED && precision != SMGPU_MIXED_DF)
+    throw SetupError{SMGPU_ERR_ARG, "unknown precision"};
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev == 0)
@@ -268,6 +270,11 @@ struct Solve {
   TX* U = nullptr;
   double* w = nullptr;
   long long launches_first = 0, launches_rest = 0;
+  // FP32 basis only: true runs the residual, re-orthogonalisation and the
+  // restart's small dense algebra in double-float (SMGPU_MIXED_DF), false in
+  // FP64 (SMGPU_MIXED)
+  bool df = false;
+  bool dfs() const { return sizeof(TX) == 4 && df; }
 
   void alloc(int lm, int ls, int num_ev, double tol) {
     DeviceArena& A = P->solver;
@@ -299,13 +306,13 @@ struct Solve {
     L.jacZ = A.alloc<double>((size_t)lm * lm);
     L.evals = A.alloc<double>(lm);
     L.Yf = A.alloc<float>((size_t)lm * ls);
-    L.wsplit = sizeof(TX) == 4 ? A.alloc<float>(2 * (size_t)L.len) : nullptr;
+    L.wsplit = dfs() ? A.alloc<float>(2 * (size_t)L.len) : nullptr;
     L.gram = A.alloc<double>(P_gram);
     L.X = A.alloc<double>((size_t)ls * ls);
     L.cvec = A.alloc<double>(ls);
     L.sc = A.alloc<LanczosScalars>(1);
     L.fl = A.alloc<LanczosFlags>(1);
-    L.alpha_df = sizeof(TX) == 4 ? 1 : 0;  // the FP32-mixed solve runs the double-float H·v epilogue
+    L.alpha_df = dfs() ? 1 : 0;  // the double-float solve runs the double-float H·v epilogue
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(TX) * (size_t)lm * L.len, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * L.len, P->st));
     // the padding slots of the double-float residual are never written by H·v
@@ -339,16 +346,17 @@ struct Solve {
       epi.beta = L.T + (size_t)(it0 - 1) * L.lm + it0;
     }
     if constexpr (sizeof(TX) == 4) {
-      // FP32 basis: the residual w stays a double-float pair (wsplit)
-      P->hv_df(vk, L.wsplit, L.wsplit + L.len, epi, s);
+      // FP32 basis: the residual w is FP64, or a double-float pair (wsplit)
+      if (df) P->hv_df(vk, L.wsplit, L.wsplit + L.len, epi, s);
+      else P->hv(vk, w, epi, s);
     } else {
       P->hv(vk, w, epi, s);
     }
     SMGPU_CUDA_TRY(cudaEventRecord(ev_fork, s));
     SMGPU_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
     launch_sturm(L, it, lock, s2);
-    if constexpr (sizeof(TX) == 4) {
-      launch_orth_iteration_df(L, V, L.wsplit, L.wsplit + L.len, it0, s);
+    if (dfs()) {
+      launch_orth_iteration_df(L, reinterpret_cast<float*>(V), L.wsplit, L.wsplit + L.len, it0, s);
     } else {
       launch_orth_iteration<TX>(L, V, w, it0, s);
     }
@@ -356,13 +364,13 @@ struct Solve {
 
   void restart(cudaStream_t s) {
     // ThickRestart (lanczos_methods.jl:260-307)
-    launch_jacobi(L, L.lm - 1, true, sizeof(TX) == 4, s);
+    launch_jacobi(L, L.lm - 1, true, dfs(), s);
     launch_restart_small(L, s);
     launch_restart_rotate<TX>(L, V, U, s);
-    launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, s);
-    launch_gram_reduce(L, sizeof(TX) == 4, s);
-    launch_chol(L, sizeof(TX) == 4, s);
-    launch_restart_apply<TX>(L, U, V, s);
+    launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, dfs(), s);
+    launch_gram_reduce(L, dfs(), s);
+    launch_chol(L, dfs(), s);
+    launch_restart_apply<TX>(L, U, V, dfs(), s);
   }
 
   cudaGraphExec_t capture_cycle(int kstart, int lock, long long* nkernels) {
@@ -613,7 +621,7 @@ struct Solve {
     if (evecs_out && elit > 0) {
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, sizeof(TX) == 4, s);
+      launch_jacobi(L, elit, false, dfs(), s);
       launch_ritz<TX>(L, V, elit, nev, R, s);
       for (int e = 0; e < nev; ++e) {
         double* r = R + (size_t)e * L.len;
@@ -711,7 +719,7 @@ struct Solve {
       // Ritz vectors (shellmodel_main.jl:208-224)
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, sizeof(TX) == 4, P->st);
+      launch_jacobi(L, elit, false, dfs(), P->st);
       launch_ritz<TX>(L, V, elit, nev, R, P->st);
       launches += 2;
       for (int e = 0; e < nev; ++e) {
@@ -1240,6 +1248,7 @@ int smgpu_solve(smgpu_problem* h, int num_ev, int lm, int ls, double tol, int ma
       return s.run(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
     }
     Solve<float> s{h};
+    s.df = h->precision == SMGPU_MIXED_DF;
     return s.run(num_ev, lm, ls, tol, max_restarts, v1, evals_out, evecs_out, stats_out);
   });
 }
@@ -1406,14 +1415,20 @@ int smgpu_stats(const smgpu_problem* h, long long* s) {
 // ===========================================================================
 // Allocation-free H·v (smgpu_matvec_noalloc).
 //
-// For callers that cannot allocate device memory while they run: code inside
-// a CUDA stream capture (allocation calls are not capturable), and hosts whose
-// device memory belongs to their own pool allocator (a Julia CuArray or
-// PyTorch caching pool) and must not see cudaMalloc/cudaFree from a library
-// in the middle of a step.  The only scratch this H·v needs — the per-CTA
-// partial sums of <v|H|v> — lives in the file-scope array below, so the call
-// allocates nothing.  Every GPU that loads the library holds this array
-// (512 KB) until the process exits.
+// For callers that cannot let a library allocate device memory while they
+// run: hosts whose device memory belongs to their own pool allocator (a Julia
+// CuArray pool, PyTorch's caching allocator).  Such a pool usually holds most
+// of the device's memory, so a library's cudaMalloc in the middle of a step
+// can fail or force the pool to release its cache, and a cudaFree
+// synchronizes the whole device, stalling the host's queued work.  The only
+// scratch this H·v needs — the per-CTA partial sums of <v|H|v> — lives in the
+// file-scope array below, so the call allocates nothing.  Every GPU that
+// loads the library holds this array (512 KB) until the process exits.
+//
+// Ordering: the kernels run on the handle's own stream, which does not
+// synchronize with the caller's streams or the legacy default stream, so the
+// caller must have finished all device work that writes v (or still reads
+// w) before the call; the call returns after w and *vhv are written.
 namespace {
 constexpr int kNoAllocMaxPartials = 1 << 16;  // CTAs of one H·v launch; 65,536 doubles = 512 KB
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxPartials];
@@ -1424,7 +1439,9 @@ double* g_noalloc_addr[kMaxDevices] = {nullptr};
 
 // Device address of g_noalloc_partials on the current device.  Host code only
 // holds a host-side stand-in for the symbol, so the address is looked up once
-// per device (with that device current) and cached.
+// per device (with that device current, on the first call there) and cached
+// for the life of the process: a cudaDeviceReset between calls would leave
+// the cached address stale and is not supported.
 double* noalloc_scratch() {
   int dev = -1;
   SMGPU_CUDA_TRY(cudaGetDevice(&dev));

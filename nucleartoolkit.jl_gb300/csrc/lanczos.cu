@@ -822,8 +822,9 @@ __global__ void __launch_bounds__(kNT) k_gram_reduce_f(const double* __restrict_
 
 // Gram matrix of U (upper triangle, packed row by row) and U_k·v_last.
 // Entry order: pairs (k,l) with k <= l in row-major order, then g_k.
-// FP64 for FP64 vectors; double-float for FP32 vectors (mixed form).
-template <class TX>
+// FP64 for FP64 vectors; for FP32 vectors FP64 (F64, the FP32-mixed form) or
+// double-float (the double-float form when ls exceeds the register kernels).
+template <class TX, bool F64>
 __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX* __restrict__ vl, int ls,
                                               int64_t len, double* __restrict__ partials, int G,
                                               const LanczosFlags* __restrict__ fl) {
@@ -854,11 +855,12 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
       if (pr >= P) break;
       int k, l;
       gram_pair(pr, ls, k, l);
-      if constexpr (sizeof(TX) == 4) {
+      if constexpr (sizeof(TX) == 4 && !F64) {
         for (int x = 0; x < cnt; ++x) dacc[q].add_prod(tl[k * TS + x], tl[l * TS + x]);
       } else {
+        // (the product of two FP32 numbers is exact in FP64)
         double s = acc[q];
-        for (int x = 0; x < cnt; ++x) s = fma((double)tl[k * TS + x], (double)tl[l * TS + x], s);
+        for (int x = 0; x < cnt; ++x) s = fma(widen(tl[k * TS + x]), widen(tl[l * TS + x]), s);
         acc[q] = s;
       }
     }
@@ -867,7 +869,7 @@ __global__ void __launch_bounds__(kNT) k_gram(const TX* __restrict__ U, const TX
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     int pr = threadIdx.x + q * kNT;
-    if (pr < P) partials[(int64_t)pr * G + blockIdx.x] = (sizeof(TX) == 4) ? dacc[q].get() : acc[q];
+    if (pr < P) partials[(int64_t)pr * G + blockIdx.x] = (sizeof(TX) == 4 && !F64) ? dacc[q].get() : acc[q];
   }
 }
 
@@ -930,7 +932,9 @@ __global__ void __launch_bounds__(32) k_chol_df(const double* __restrict__ gram,
 }
 
 // V_k = Σ_{j<=k} X[j,k] U_j (k < ls);  V_ls = V_{lm-1} - Σ_k c_k V_k.
-template <class TX>
+// FP64 sums, except for FP32 vectors with !F64 (the double-float form when ls
+// exceeds the register kernels): FP32 products with Kahan sums.
+template <class TX, bool F64>
 __global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U, TX* __restrict__ V,
                                                        const double* __restrict__ X, const double* __restrict__ cvec,
                                                        int ls, int lm, int64_t len,
@@ -948,8 +952,8 @@ __global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U,
   }
   __syncthreads();
   for (int64_t i = blockIdx.x * (int64_t)kNT + threadIdx.x; i < len; i += (int64_t)gridDim.x * kNT) {
-    if constexpr (sizeof(TX) == 4) {
-      // mixed form: X is the identity up to O(1e-7); FP32 products, Kahan sums
+    if constexpr (sizeof(TX) == 4 && !F64) {
+      // X is the identity up to O(1e-7); FP32 products, Kahan sums
       KahanF last;
       last.init();
       last.add((float)V[(int64_t)(lm - 1) * len + i]);
@@ -963,10 +967,10 @@ __global__ void __launch_bounds__(kNT) k_restart_apply(const TX* __restrict__ U,
       }
       V[(int64_t)ls * len + i] = (TX)last.get();
     } else {
-      double last = (double)V[(int64_t)(lm - 1) * len + i];
+      double last = widen(V[(int64_t)(lm - 1) * len + i]);
       for (int k = 0; k < ls; ++k) {
         double q = 0.0;
-        for (int j = 0; j <= k; ++j) q = fma(xs[k * ls + j], (double)U[(int64_t)j * len + i], q);
+        for (int j = 0; j <= k; ++j) q = fma(xs[k * ls + j], widen(U[(int64_t)j * len + i]), q);
         V[(int64_t)k * len + i] = (TX)q;
         last = fma(-xs[ls * ls + k], q, last);
       }
@@ -1115,14 +1119,19 @@ void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t
   k_restart_rotate<TX><<<grid_for(L.len), kNT, 0, st>>>(V, U, L.jacA, L.Yf, m, L.ls, L.len, L.fl);
 }
 template <class TX>
-void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st) {
+void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, bool df, cudaStream_t st) {
   if constexpr (sizeof(TX) == 4) {
-    if (L.ls <= kRLS && L.ls * (L.ls + 1) / 2 + L.ls <= kNT) {
+    if (df && L.ls <= kRLS && L.ls * (L.ls + 1) / 2 + L.ls <= kNT) {
       k_gram_f<<<L.G, kNT, sizeof(float) * 2 * (L.ls + 1) * 129, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
       return;
     }
+    if (df) {
+      k_gram<TX, false><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 65, st>>>(U, vlast, L.ls, L.len, L.partials, L.G,
+                                                                            L.fl);
+      return;
+    }
   }
-  k_gram<TX><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 65, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
+  k_gram<TX, true><<<L.G, kNT, sizeof(double) * (L.ls + 1) * 65, st>>>(U, vlast, L.ls, L.len, L.partials, L.G, L.fl);
 }
 void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st) {
   const int P = L.ls * (L.ls + 1) / 2 + L.ls;
@@ -1134,16 +1143,19 @@ void launch_chol(const LanczosDev& L, bool df, cudaStream_t st) {
   else k_chol<<<1, 32, sizeof(double) * L.ls * L.ls, st>>>(L.gram, L.ls, L.X, L.cvec, L.fl);
 }
 template <class TX>
-void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st) {
+void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, bool df, cudaStream_t st) {
+  const size_t shm = (sizeof(double) + sizeof(float)) * (L.ls * L.ls + L.ls);
   if constexpr (sizeof(TX) == 4) {
-    if (L.ls <= kRLS) {
+    if (df && L.ls <= kRLS) {
       k_restart_apply_f<<<grid_for(L.len), kNT, 0, st>>>(U, V, L.X, L.cvec, L.ls, L.lm, L.len, L.fl);
       return;
     }
+    if (df) {
+      k_restart_apply<TX, false><<<grid_for(L.len), kNT, shm, st>>>(U, V, L.X, L.cvec, L.ls, L.lm, L.len, L.fl);
+      return;
+    }
   }
-  k_restart_apply<TX><<<grid_for(L.len), kNT, (sizeof(double) + sizeof(float)) * (L.ls * L.ls + L.ls), st>>>(
-      U, V, L.X, L.cvec, L.ls,
-                                                                                             L.lm, L.len, L.fl);
+  k_restart_apply<TX, true><<<grid_for(L.len), kNT, shm, st>>>(U, V, L.X, L.cvec, L.ls, L.lm, L.len, L.fl);
 }
 template <class TX>
 void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R, cudaStream_t st) {
@@ -1176,8 +1188,8 @@ void launch_small_eig(const double* T, int n, double* A, double* Z, double* eval
   template void launch_scale_store<TX>(const LanczosDev&, const double*, TX*, const double*, cudaStream_t);   \
   template void launch_orth_iteration<TX>(const LanczosDev&, TX*, double*, int, cudaStream_t);               \
   template void launch_restart_rotate<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                  \
-  template void launch_gram<TX>(const LanczosDev&, const TX*, const TX*, cudaStream_t);                      \
-  template void launch_restart_apply<TX>(const LanczosDev&, const TX*, TX*, cudaStream_t);                   \
+  template void launch_gram<TX>(const LanczosDev&, const TX*, const TX*, bool, cudaStream_t);                \
+  template void launch_restart_apply<TX>(const LanczosDev&, const TX*, TX*, bool, cudaStream_t);             \
   template void launch_ritz<TX>(const LanczosDev&, const TX*, int, int, double*, cudaStream_t);               \
   template void launch_widen<TX>(const TX*, double*, int64_t, cudaStream_t);                                 \
   template void launch_narrow<TX>(const double*, TX*, int64_t, cudaStream_t);                                \

@@ -62,14 +62,16 @@ void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaS
 void launch_restart_small(const LanczosDev& L, cudaStream_t st);
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st);
+// df: FP32 vectors summed in double-float (SMGPU_MIXED_DF); otherwise FP64
 template <class TX>
-void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, cudaStream_t st);
+void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, bool df, cudaStream_t st);
 // df: the partials of the FP32-basis Gram kernel ((hi, lo) pairs)
 void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st);
 // df: the double-float form on one warp (FP32-mixed solves, ls <= 32)
 void launch_chol(const LanczosDev& L, bool df, cudaStream_t st);
+// df: FP32 vectors combined in compensated FP32 (SMGPU_MIXED_DF); otherwise FP64
 template <class TX>
-void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, cudaStream_t st);
+void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, bool df, cudaStream_t st);
 template <class TX>
 void launch_ritz(const LanczosDev& L, const TX* V, int elit, int nev, double* R, cudaStream_t st);
 // J-projected Lanczos helpers: FP64 copies, y -= Σ h_j X_j, out = Σ c_j Q_j,

@@ -22,7 +22,8 @@ ERR_EMPTY = -9
 ERR_DEVICE = -10
 
 FP64 = 0
-MIXED = 1
+MIXED = 1      # FP32 H·v and Krylov storage, FP64 Lanczos arithmetic
+MIXED_DF = 2   # as MIXED, with the residual and re-orthogonalisation in double-float
 
 # Every symbol include/smgpu.h declares, with its ctypes signature.
 _vp = C.c_void_p
@@ -52,6 +53,7 @@ SIGNATURES = {
     "smgpu_time_matvec": (C.c_int, [_vp, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "smgpu_tune_report": (C.c_int, [_vp, C.c_int, _vp, _vp, C.POINTER(C.c_int)]),
     "smgpu_matvec_noalloc": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "smgpu_l2_read_bandwidth": (C.c_int, [C.c_longlong, C.c_int, C.POINTER(C.c_double)]),
     "smgpu_write_wav": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, C.c_int, _vp, _vp, _vp]),
     "smgpu_read_wav_header": (C.c_int, [C.c_char_p, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "smgpu_read_wav": (C.c_int, [C.c_char_p, C.c_longlong, C.c_int, _vp, _vp, _vp]),

@@ -32,7 +32,7 @@ VALENCE = {"sd2p2n": ("sd", 2, 2, "Ne20"), "sd4p4n": ("sd", 4, 4, "Mg24"), "pf4p
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="pf4p4n", choices=sorted(VALENCE))
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed", "mixed_df"])
     ap.add_argument("--samples", type=int, default=0, help="interaction samples sharing the basis (multi-sample H·V)")
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--no-flush", action="store_true")
@@ -55,7 +55,7 @@ def main():
         out.update(precision="mixed", samples=a.samples)
     else:
         snt, nuc = synth.config_snt(d, a.workload)
-        prec = smgpu.MIXED if a.precision == "mixed" else smgpu.FP64
+        prec = {"mixed": smgpu.MIXED, "mixed_df": smgpu.MIXED_DF, "fp64": smgpu.FP64}[a.precision]
         P = smgpu.ShellModelProblem(snt, nuc, prec)
         out.update(precision=a.precision)
     ms = P.time_matvec(reps=a.reps, flush_l2=not a.no_flush)
@@ -69,7 +69,7 @@ def main():
         elif a.samples:
             b = a.nnz * (4 + a.samples * 4) + 2 * a.samples * P.mdim * 4
         else:
-            s = 4 if a.precision == "mixed" else 8
+            s = 8 if a.precision == "fp64" else 4
             b = a.nnz * (s + 4) + 4 * (P.mdim + 1) + 2 * P.mdim * s
         out["csr_equiv_GBs"] = b / (ms * 1e-3) / 1e9
     if a.solve:

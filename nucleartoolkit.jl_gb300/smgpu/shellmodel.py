@@ -344,6 +344,14 @@ class BatchProblem:
                     n_second_pass=per[:, 2].astype(int), status=rc)
 
 
+def l2_read_bandwidth(nbytes=32 << 20, reps=50):
+    """GB/s of the library's read kernel on an L2-resident device buffer of
+    nbytes (the ceiling of the L2-resident H·v kernels)."""
+    g = C.c_double()
+    check(load().smgpu_l2_read_bandwidth(int(nbytes), int(reps), C.byref(g)), None)
+    return float(g.value)
+
+
 def J_from_JJ1(JJ, tol=1.0e-6):
     """J from <J^2> = J(J+1) (shellmodel_main.jl:1105-1113): the first
     half-integer J in 0..50 within tol, else -1."""

@@ -1,7 +1,11 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run once in a container where the NuclearToolkit.jl sources are mounted
-(default /root/reference, or the path given as the first argument).  Copies
+Run once where the NuclearToolkit.jl sources are available, with the path of
+that checkout as the only argument:
+
+    python tests/golden/make_golden.py <NuclearToolkit.jl checkout>
+
+Copies
 the interaction files the reference's own ShellModel tests use and records the
 reference's known-answer values next to them (golden.json).  Tests read only
 the files written here, never the reference tree.
@@ -14,7 +18,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref="/root/reference"):
+def main(ref):
     src = os.path.join(ref, "test", "interaction_file")
     for f in ("ckpot.snt", "usdb.snt"):
         shutil.copyfile(os.path.join(src, f), os.path.join(HERE, f))
@@ -34,4 +38,6 @@ def main(ref="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <NuclearToolkit.jl checkout>")
+    main(sys.argv[1])

@@ -207,8 +207,11 @@ def test_matvec_every_launch_shape(lib, snt_dir, case, monkeypatch):
         tol = MATVEC_FP64_RTOL if prec == 0 else MATVEC_MIXED_RTOL
         assert np.abs(G.matvec(v) - ref).max() <= tol * scale, sh
         if ro is not None and sh[3] == 1:
-            rm = G.solve(5, lm=30, ls=15, tol=1e-8)
-            assert rm["converged"] and np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, sh
+            # both epilogues of the staged kernel: FP64 residual (MIXED) and
+            # double-float residual (MIXED_DF)
+            for H in (G, _gpu(snt, nuc, 2)):
+                rm = H.solve(5, lm=30, ls=15, tol=1e-8)
+                assert rm["converged"] and np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, sh
     monkeypatch.setenv("SMGPU_HV_SHAPE", "999,1,1,1")
     with pytest.raises(Exception):
         _gpu(snt, nuc, 1)
@@ -235,9 +238,27 @@ def test_eigenvalues_vs_oracle(lib, snt_dir, case, nev, lm, ls):
     rg = G.solve(nev, lm=lm, ls=ls, tol=1e-8)
     assert rg["converged"]
     assert np.allclose(rg["evals"], ro["evals"], rtol=EIG_FP64_RTOL, atol=0)
-    M = _gpu(snt, nuc, 1)
-    rm = M.solve(nev, lm=lm, ls=ls, tol=1e-8)
-    assert np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL
+    for prec in (1, 2):  # FP32-mixed with FP64 / double-float Lanczos arithmetic
+        M = _gpu(snt, nuc, prec)
+        rm = M.solve(nev, lm=lm, ls=ls, tol=1e-8)
+        assert rm["converged"], prec
+        assert np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, prec
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_ritz_vectors_mixed(lib, snt_dir, prec):
+    """Ritz vectors of both FP32-mixed forms (FP64 or double-float Lanczos
+    arithmetic): unit norm, small residual, overlap with the oracle's."""
+    snt, nuc = snt_dir["sd4p4n"]
+    M = _gpu(snt, nuc, prec)
+    r = M.solve(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    O = _oracle(snt, nuc)
+    ro = O.trl(3, lm=40, ls=15, tol=1e-10, want_vecs=True)
+    for k in range(3):
+        x = r["evecs"][k]
+        assert abs(np.linalg.norm(x) - 1) < 1e-10
+        assert np.linalg.norm(O.operate_H(x) - r["evals"][k] * x) < 1e-2
+        assert abs(abs(x @ ro["evecs"][k]) - 1.0) < 1e-5
 
 
 def test_ritz_vectors(lib, snt_dir):
