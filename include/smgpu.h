@@ -47,9 +47,10 @@ enum smgpu_precision {
   SMGPU_MIXED = 1,    /* H·v and Krylov storage FP32 (FP32 products and partial sums, the
                          partial sums of a row combined with Kahan compensation); the Lanczos
                          residual, α/β, both re-orthogonalisation passes, the restart's
-                         tridiagonal/arrowhead eigensolve, its Gram matrix, Cholesky factor and
-                         basis update, and the Ritz vectors FP64.  The restart's basis rotation
-                         (whose result is stored in FP32) runs in compensated FP32. */
+                         tridiagonal/arrowhead eigensolve (FP64 Jacobi started from an FP32
+                         Jacobi's eigenbasis), its Gram matrix and Cholesky factor, and the
+                         Ritz vectors FP64.  The restart's basis rotation and update (whose
+                         results are stored in FP32) run in compensated FP32. */
   SMGPU_MIXED_DF = 2  /* as SMGPU_MIXED, except that the residual, the re-orthogonalisation,
                          the restart eigensolve, Gram matrix and Cholesky factor run in
                          double-float arithmetic (pairs of FP32 numbers, about 48 significant
@@ -226,8 +227,9 @@ int smgpu_timings(const smgpu_problem* h, double* times_out);
 int smgpu_time_matvec(smgpu_problem* h, int reps, int flush_l2, double* ms_out);
 
 /* Read bandwidth (GB/s) of a device buffer of `bytes` (1 MB .. 1 GB) that
- * stays resident in the L2 cache: `reps` passes of the library's own read
- * kernel over the buffer, CUDA events, after one untimed pass.  No
+ * stays resident in the L2 cache: `reps` launches of the library's own read
+ * kernel, 16 sweeps over the buffer each, timed with CUDA events after one
+ * untimed sweep.  No
  * counterpart in the reference: the ceiling against which the H·v kernels,
  * whose tables and vectors fit in L2, are measured. */
 int smgpu_l2_read_bandwidth(long long bytes, int reps, double* gbs_out);

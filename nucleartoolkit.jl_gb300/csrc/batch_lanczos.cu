@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const flo
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
   __shared__ double red[kNT / 32];
+  __shared__ double red8[(kNT / 32) * 8];
   const int m = it0 + 1;
   if (!b_need_second(B, P, m, red)) return;
   const float* __restrict__ Vb = V + P.voff;
@@ -260,12 +261,8 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const flo
           for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
         }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q >= m) break;
-      const double s = block_sum_all<kNT>(acc[q], red);
-      if (threadIdx.x == 0) B.pdot2[(int64_t)(j0 + q) * B.nchunks + c] = s;
-    }
+    const double s = block_sum8<kNT>(acc, red8);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m) B.pdot2[(int64_t)(j0 + threadIdx.x) * B.nchunks + c] = s;
   }
 }
 

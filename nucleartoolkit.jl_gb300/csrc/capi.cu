@@ -275,6 +275,9 @@ struct Solve {
   // FP64 (SMGPU_MIXED)
   bool df = false;
   bool dfs() const { return sizeof(TX) == 4 && df; }
+  // FP32 basis, FP64 arithmetic: the restart and Ritz eigenproblems by the
+  // FP64 Jacobi started from an FP32 Jacobi's eigenbasis
+  bool refj() const { return sizeof(TX) == 4 && !df; }
 
   void alloc(int lm, int ls, int num_ev, double tol) {
     DeviceArena& A = P->solver;
@@ -364,13 +367,15 @@ struct Solve {
 
   void restart(cudaStream_t s) {
     // ThickRestart (lanczos_methods.jl:260-307)
-    launch_jacobi(L, L.lm - 1, true, dfs(), s);
+    launch_jacobi(L, L.lm - 1, true, dfs(), refj(), s);
     launch_restart_small(L, s);
     launch_restart_rotate<TX>(L, V, U, s);
     launch_gram<TX>(L, U, V + (size_t)(L.lm - 1) * L.len, dfs(), s);
     launch_gram_reduce(L, dfs(), s);
     launch_chol(L, dfs(), s);
-    launch_restart_apply<TX>(L, U, V, dfs(), s);
+    // the updated basis is stored in FP32: for an FP32 basis the update runs
+    // in compensated FP32, as the rotation does
+    launch_restart_apply<TX>(L, U, V, sizeof(TX) == 4, s);
   }
 
   cudaGraphExec_t capture_cycle(int kstart, int lock, long long* nkernels) {
@@ -621,7 +626,7 @@ struct Solve {
     if (evecs_out && elit > 0) {
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, dfs(), s);
+      launch_jacobi(L, elit, false, dfs(), refj(), s);
       launch_ritz<TX>(L, V, elit, nev, R, s);
       for (int e = 0; e < nev; ++e) {
         double* r = R + (size_t)e * L.len;
@@ -719,7 +724,7 @@ struct Solve {
       // Ritz vectors (shellmodel_main.jl:208-224)
       double* R = P->solver.alloc<double>((size_t)nev * L.len);
       double* tmp = P->solver.alloc<double>(mdim);
-      launch_jacobi(L, elit, false, dfs(), P->st);
+      launch_jacobi(L, elit, false, dfs(), refj(), P->st);
       launch_ritz<TX>(L, V, elit, nev, R, P->st);
       launches += 2;
       for (int e = 0; e < nev; ++e) {

@@ -99,6 +99,14 @@ struct TileTables {
   const int* nnell_w;        // per block: longest list
   const int* nnell_col;
   const float* nnell_val;
+  // two-body pass of the staged form (hv_2b.cu): the pp and nn terms of
+  // every element, computed over row and column tiles of each block and left
+  // in s2b for the staged kernel's epilogue
+  const int4* pp_tasks;  // (block, first row, first of 32 columns, rows)
+  const int4* nn_tasks;  // (block, first of 32 rows, first column, columns)
+  int n_pp_tasks, n_nn_tasks;
+  float* s2b;            // 2 x len_pad: pp sums, then nn sums
+  int npmax;             // largest np[b]
   int ymax;     // floats of one row's slot buffer: max over links of (longest pull list) * nn[b]
   int nnmax;    // largest nn[b], rounded up to 4
   int nbmax;    // largest neutron-operator count nB of a link
@@ -230,7 +238,9 @@ void launch_hv_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig
 // one-time set-up of that shared-memory size (call before graph capture).
 const HvConfig* hv_staged_candidates(int* count);
 bool hv_staged_fits(const HvConfig& cfg, const TileTables& tt, int nnmax_raw);
-size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt);
+// ext: the single-problem form, whose pp and nn sums come from the two-body
+// pass; otherwise the batched body that computes them itself
+size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt, bool ext = false);
 void hv_staged_prepare(const HvConfig& cfg, const TileTables& tt);
 void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
                             const double* en, const CoefTables<float>& c, const float* v, double* w,
@@ -238,6 +248,16 @@ void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvCo
 void launch_hv_staged_mixed_df(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const float2* ep2,
                                const float2* en2, const CoefTables<float>& c, const float* v, float* wh, float* wl,
                                const HvEpilogue<float>& epi, cudaStream_t st);
+// The two-body pass of the staged form (hv_2b.cu): pp and nn sums of every
+// element into tt.s2b.  Tile sizes, the shared memory of its two kernels, and
+// their one-time set-up (call before graph capture).
+constexpr int kPPRows = 128;  // rows of a pp task (its 32 columns are the lanes of a warp), <= 32 per warp
+constexpr int kNNCols = 256;  // columns of an nn task (its 32 rows are the lanes of a warp)
+size_t hv_2b_nn_smem(const TileTables& tt);
+size_t hv_2b_pp_smem(const TileTables& tt);
+void hv_2b_prepare(const TileTables& tt);
+void launch_hv_2b(const DevTables& t, const TileTables& tt, const CoefTables<float>& c, const float* v,
+                  const LanczosFlags* fl, cudaStream_t st);
 // Multi-sample H·V (hv_multi.cu).  S in {4, 8, 16}; tt1 = one-row tasks
 // (ntasks of them); v/w interleaved; cand = index into hv_multi_candidates().
 struct MultiHvConfig {

@@ -24,9 +24,12 @@
 //
 // Every update is still one FP32 multiply-add, in the order of the proton
 // entries; the partial sums are FP32 per (row, link, neutron entry), combined
-// with Kahan compensation per (row, link) as in the row-tile kernel.  The nn
-// term gathers from the CTA's rows of v staged in shared memory; pp, the
-// one-body term and the Lanczos epilogue are those of hv_tile.cuh.
+// with Kahan compensation per (row, link) as in the row-tile kernel.  The pp
+// and nn terms come from the two-body pass (hv_2b.cu), launched just before
+// on the same stream, which leaves them per element in tt.s2b; the one-body
+// term and the Lanczos epilogue are those of hv_tile.cuh.  (The batched
+// kernel, hv_batch.cu, runs the same row body with the pp and nn terms
+// computed in the kernel.)
 
 #include "device.cuh"
 #include "hv_staged.cuh"
@@ -41,8 +44,8 @@ __global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float,
   if (a.fl != nullptr && cta_gate(threadIdx.x == 0 && (a.fl->done || a.fl->exhausted))) return;
   const int task = blockIdx.x;
   const double beta = (a.vprev != nullptr) ? *a.beta : 0.0;
-  hv_staged_rows<NT, R, QM, DF>(a, a.v, a.w, a.vprev, beta, a.tt.task_b[task], a.tt.task_p0[task],
-                                a.alpha_part != nullptr ? a.alpha_part + task : nullptr);
+  hv_staged_rows<NT, R, QM, DF, true>(a, a.v, a.w, a.vprev, beta, a.tt.task_b[task], a.tt.task_p0[task],
+                                      a.alpha_part != nullptr ? a.alpha_part + task : nullptr);
 }
 
 // {threads, rows, -, min CTAs per SM, staged}; a thread owns up to
@@ -84,23 +87,25 @@ const HvConfig* hv_staged_candidates(int* count) {
   return kStagedCand;
 }
 
-size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt) {
+size_t hv_staged_smem(const HvConfig& cfg, const TileTables& tt, bool ext) {
   const size_t R = (size_t)cfg.rows;
-  return sizeof(float) * R * ((size_t)tt.ymax + (size_t)tt.nbmax * tt.astride + (size_t)tt.nnmax) +
+  return sizeof(float) * R * ((size_t)tt.ymax + (size_t)tt.nbmax * tt.astride + (ext ? 0 : (size_t)tt.nnmax)) +
          sizeof(int) * R * (size_t)tt.kpad;
 }
 
 bool hv_staged_fits(const HvConfig& cfg, const TileTables& tt, int nnmax_raw) {
-  if (tt.push_ent == nullptr) return false;
+  if (tt.push_ent == nullptr || tt.s2b == nullptr) return false;
   if (nnmax_raw > cfg.nt * qm_for(cfg.nt)) return false;
-  return hv_staged_smem(cfg, tt) <= 200 * 1024;
+  return hv_staged_smem(cfg, tt, true) <= 200 * 1024 && hv_2b_nn_smem(tt) <= 200 * 1024 &&
+         hv_2b_pp_smem(tt) <= 200 * 1024;
 }
 
 void hv_staged_prepare(const HvConfig& cfg, const TileTables& tt) {
-  const size_t smem = hv_staged_smem(cfg, tt);
+  const size_t smem = hv_staged_smem(cfg, tt, true);
   HvArgs<float, float> a{};
   dispatch<false>(cfg, a, smem, nullptr, true);
   dispatch<true>(cfg, a, smem, nullptr, true);
+  hv_2b_prepare(tt);
 }
 
 void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvConfig& cfg, const double* ep,
@@ -108,7 +113,8 @@ void launch_hv_staged_mixed(const DevTables& t, const TileTables& tt, const HvCo
                             const HvEpilogue<float>& epi, cudaStream_t st) {
   HvArgs<float, float> a{t, tt, c, ep, en, v, w, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
                          nullptr, nullptr, nullptr, nullptr};
-  if (!dispatch<false>(cfg, a, hv_staged_smem(cfg, tt), st, false))
+  launch_hv_2b(t, tt, c, v, epi.fl, st);
+  if (!dispatch<false>(cfg, a, hv_staged_smem(cfg, tt, true), st, false))
     throw CudaError{cudaErrorInvalidConfiguration, "staged H·v launch shape", __FILE__, __LINE__};
 }
 
@@ -117,7 +123,8 @@ void launch_hv_staged_mixed_df(const DevTables& t, const TileTables& tt, const H
                                const HvEpilogue<float>& epi, cudaStream_t st) {
   HvArgs<float, float> a{t, tt, c, nullptr, nullptr, v, nullptr, epi.fl, epi.vprev, epi.beta, epi.alpha_part,
                          wh, wl, ep2, en2};
-  if (!dispatch<true>(cfg, a, hv_staged_smem(cfg, tt), st, false))
+  launch_hv_2b(t, tt, c, v, epi.fl, st);
+  if (!dispatch<true>(cfg, a, hv_staged_smem(cfg, tt, true), st, false))
     throw CudaError{cudaErrorInvalidConfiguration, "staged H·v launch shape", __FILE__, __LINE__};
 }
 

@@ -12,7 +12,9 @@ namespace smgpu {
 // arguments).  vprev: three-term correction w -= beta*vprev (null: none);
 // alpha_out: where the CTA's partial of v·Hv goes (null: none; DF: a (hi, lo)
 // float pair in the FP64 slot).  DF: the epilogue writes w as (a.wh, a.wl).
-template <int NT, int R, int QM, bool DF>
+// EXT: the pp and nn sums of every element come from the two-body pass
+// (hv_2b.cu, in a.tt.s2b) instead of being computed here.
+template <int NT, int R, int QM, bool DF, bool EXT = false>
 __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, const float* __restrict__ v_in,
                                                double* w_out, const float* vprev, const double beta, const int b,
                                                const int p0, double* alpha_out) {
@@ -21,8 +23,8 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
   extern __shared__ float4 sm4[];
   float* Y = reinterpret_cast<float*>(sm4);          // [R][ymax] slots
   float* A = Y + R * tt.ymax;                        // [R][nbmax][astride] coefficients
-  float* vrow = A + R * tt.nbmax * tt.astride;       // [R][nnmax] the CTA's rows of v
-  int* so = reinterpret_cast<int*>(vrow + R * tt.nnmax);  // [R][kpad] source-row offsets into v
+  float* vrow = A + R * tt.nbmax * tt.astride;       // [R][nnmax] the CTA's rows of v (not with EXT)
+  int* so = reinterpret_cast<int*>(vrow + (EXT ? 0 : R * tt.nnmax));  // [R][kpad] source-row offsets into v
   const int tid = threadIdx.x;
   const int np = t.np[b];
   const int nr = min(R, np - p0);
@@ -36,9 +38,11 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
   const float* __restrict__ v = v_in;
   const int as = tt.astride, kpad = tt.kpad;
 
-  for (int idx = tid; idx < nr * nn; idx += NT) {
-    const int r = idx / nn, n = idx - r * nn;
-    vrow[r * tt.nnmax + n] = v[blk + (int64_t)(p0 + r) * stride + n];
+  if constexpr (!EXT) {
+    for (int idx = tid; idx < nr * nn; idx += NT) {
+      const int r = idx / nn, n = idx - r * nn;
+      vrow[r * tt.nnmax + n] = v[blk + (int64_t)(p0 + r) * stride + n];
+    }
   }
 
   AccKahan pn[R][QM];
@@ -75,15 +79,26 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
     for (int r = 0; r < R; ++r) {
       if (r >= nr || kr[r] == 0) continue;
       float* Ar = A + r * tt.nbmax * as;
-      for (int idx = tid; idx < nB * kp; idx += NT) {
-        const int ib = idx / kp, jj = idx - ib * kp;
-        float val = 0.f;
-        if (jj < kr[r]) {
-          const uint32_t meta = t.ppn_meta[eb[r] + jj];
-          val = vt[(int)((meta >> 1) & 0x7fffu) * nB + ib];
-          if (meta & 1u) val = -val;
+      // one thread per row ib: the proton entries' metadata are uniform
+      // (broadcast) loads, V[ia][ib] coalesced over ib, and the row goes out
+      // as 16-byte stores (row stride = 4 mod 8 floats: no bank conflicts)
+      for (int ib = tid; ib < nB; ib += NT) {
+        float4* row = reinterpret_cast<float4*>(Ar + ib * as);
+        for (int j4 = 0; j4 < kp; j4 += 4) {
+          float x4[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int jj = j4 + u;
+            float val = 0.f;
+            if (jj < kr[r]) {
+              const uint32_t meta = t.ppn_meta[eb[r] + jj];
+              val = vt[(int)((meta >> 1) & 0x7fffu) * nB + ib];
+              if (meta & 1u) val = -val;
+            }
+            x4[u] = val;
+          }
+          row[j4 >> 2] = make_float4(x4[0], x4[1], x4[2], x4[3]);
         }
-        Ar[ib * as + jj] = val;
       }
       for (int jj = tid; jj < kr[r]; jj += NT) so[r * kpad + jj] = (int)(soff + (int64_t)t.ppn_src[eb[r] + jj] * sstride);
     }
@@ -102,9 +117,17 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
         const int ne = max(0, min(16, cnt - ec));
         const int kw = (int)__reduce_max_sync(0xffffffffu, (unsigned)ne);
         if (kw == 0) break;
+        // the lane's entries, in groups of four up to the warp's longest list
         uint32_t ent[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) ent[k] = (k < ne) ? pell[(int64_t)(ec + k) * nns + i] : 0u;
+        for (int k0 = 0; k0 < 16; k0 += 4) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) ent[k0 + u] = 0u;
+          if (k0 >= kw) continue;
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (k0 + u < ne) ent[k0 + u] = pell[(int64_t)(ec + k0 + u) * nns + i];
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           if (r >= nr || kr[r] == 0) continue;
@@ -114,9 +137,17 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
           // proton entries in blocks of 16: v[s,p'_j,n'] of the block in registers
           for (int j0 = 0; j0 < kr[r]; j0 += 16) {
             const int kq = min(16, kr[r] - j0);
+            // kq is uniform over the CTA: groups of four past it are skipped
             float x[16];
 #pragma unroll
-            for (int jj = 0; jj < 16; ++jj) x[jj] = (jj < kq) ? v[sor[j0 + jj] + n] : 0.f;
+            for (int jc = 0; jc < 16; jc += 4) {
+#pragma unroll
+              for (int u = 0; u < 4; ++u) x[jc + u] = 0.f;
+              if (jc >= kq) continue;
+#pragma unroll
+              for (int u = 0; u < 4; ++u)
+                if (jc + u < kq) x[jc + u] = v[sor[j0 + jc + u] + n];
+            }
             // four entries at a time, branch-free inside a group (entries past
             // the lane's list read row 0 of A and are not stored)
 #pragma unroll
@@ -191,10 +222,24 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
       sp[r][q] = 0.f;
       sn[r][q] = 0.f;
     }
+  if constexpr (EXT) {
+    // the two-body pass has left them in s2b
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (r >= nr) break;
+#pragma unroll
+      for (int q = 0; q < QM; ++q)
+        if (tid + q * NT < nn) {
+          const int64_t o = blk + (int64_t)(p0 + r) * stride + tid + q * NT;
+          sp[r][q] = tt.s2b[o];
+          sn[r][q] = tt.s2b[t.len_pad + o];
+        }
+    }
+  }
   // pp: other proton rows of the block, same neutron column (coalesced)
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    if (r >= nr) break;
+    if (EXT || r >= nr) break;
     const int g = pst + p0 + r;
     const int kb = t.pp_ptr[g], ke = t.pp_ptr[g + 1];
 #pragma unroll 8
@@ -208,7 +253,7 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
   }
   // nn: same proton row, other neutron columns (ELL lists [k][n], rows of v
   // in shared memory)
-  {
+  if constexpr (!EXT) {
     const int W = tt.nnell_w[b];
     const int* __restrict__ ecol = tt.nnell_col + tt.nnell_off[b] + tid;
     const float* __restrict__ eval = tt.nnell_val + tt.nnell_off[b] + tid;
@@ -244,7 +289,7 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
       for (int r = 0; r < R; ++r) {
         if (r >= nr) break;
         const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
-        const float x = vrow[r * tt.nnmax + n];
+        const float x = EXT ? v[o] : vrow[r * tt.nnmax + n];
         float hh, hl;
         fast_two_sum(acc[r].s, -acc[r].c, hh, hl);
         const float2 ep2 = a.ep2[pst + p0 + r];
@@ -269,10 +314,10 @@ __device__ __forceinline__ void hv_staged_rows(const HvArgs<float, float>& a, co
       for (int r = 0; r < R; ++r) {
         if (r >= nr) break;
         const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
-        const double x = (double)vrow[r * tt.nnmax + n];
-        double hv = acc[r].result() + (a.ep[pst + p0 + r] + enn) * x;
+        const double x = widen(EXT ? v[o] : vrow[r * tt.nnmax + n]);
+        double hv = fma(a.ep[pst + p0 + r] + enn, x, acc[r].result());
         apart = fma(x, hv, apart);
-        if (vprev != nullptr) hv = fma(-beta, (double)vprev[o], hv);
+        if (vprev != nullptr) hv = fma(-beta, widen(vprev[o]), hv);
         w_out[o] = hv;
       }
     }

@@ -23,7 +23,9 @@ struct AccKahan {
     c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
   }
-  __device__ __forceinline__ double result() const { return (double)s - (double)c; }
+  // (widened with integer instructions: conversions on this GPU share the
+  // scarce FP64 pipe)
+  __device__ __forceinline__ double result() const { return widen(s) - widen(c); }
 };
 
 template <class TV, class TC>
@@ -213,10 +215,10 @@ __device__ __forceinline__ void hv_tile_rows(const HvArgs<TV, TC>& a, const TV* 
       for (int r = 0; r < R; ++r) {
         if (r >= nr) break;
         const int64_t o = blk + (int64_t)(p0 + r) * stride + n;
-        const double x = (double)v[o];
-        double hv = acc[r].result() + (a.ep[pst + p0 + r] + enn) * x;
+        const double x = widen(v[o]);
+        double hv = fma(a.ep[pst + p0 + r] + enn, x, acc[r].result());
         apart = fma(x, hv, apart);
-        if (vprev != nullptr) hv = fma(-beta, (double)vprev[o], hv);
+        if (vprev != nullptr) hv = fma(-beta, widen(vprev[o]), hv);
         w[o] = hv;
       }
     }

@@ -78,7 +78,7 @@ template <class TX>
 __global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int64_t ld, int m,
                                                   const double* __restrict__ y, int64_t len, int self,
                                                   double* __restrict__ partials, int G) {
-  __shared__ double red[kNT / 32];
+  __shared__ double red8[(kNT / 32) * 8];
   int64_t cb, ce;
   chunk_of(len, G, cb, ce);
   const int mt = m + (self ? 1 : 0);
@@ -95,12 +95,8 @@ __global__ void __launch_bounds__(kNT) k_multidot(const TX* __restrict__ X, int6
         else if (j == m && self) acc[q] = fma(yi, yi, acc[q]);
       }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q >= mt) break;
-      double s = block_sum_all<kNT>(acc[q], red);
-      if (threadIdx.x == 0) partials[(int64_t)(j0 + q) * G + blockIdx.x] = s;
-    }
+    const double s = block_sum8<kNT>(acc, red8);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < mt) partials[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
   }
 }
 
@@ -131,6 +127,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
                                                   double* __restrict__ pdot, int G, const LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
+  __shared__ double red8[(kNT / 32) * 8];
   const double alpha = sum_partials<kNT>(alpha_part + (int64_t)it0 * nalpha, nalpha, red);
   const TX* __restrict__ vk = V + (int64_t)it0 * ld;
   const int m = it0 + 1;
@@ -164,12 +161,8 @@ __global__ void __launch_bounds__(kNT) k_orth_dot(const TX* __restrict__ V, int6
         }
       }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q > m) break;
-      double s = block_sum_all<kNT>(acc[q], red);
-      if (threadIdx.x == 0) pdot[(int64_t)(j0 + q) * G + blockIdx.x] = s;
-    }
+    const double s = block_sum8<kNT>(acc, red8);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m) pdot[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
   }
 }
 
@@ -224,6 +217,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
                                                    int G, const LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   __shared__ double red[kNT / 32];
+  __shared__ double red8[(kNT / 32) * 8];
   const int m = it0 + 1;
   if (!need_second(pdot, pn1, m, G, red)) return;
   int64_t cb, ce;
@@ -244,12 +238,8 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
           for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
         }
     }
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      if (j0 + q >= m) break;
-      double s = block_sum_all<kNT>(acc[q], red);
-      if (threadIdx.x == 0) pdot2[(int64_t)(j0 + q) * G + blockIdx.x] = s;
-    }
+    const double s = block_sum8<kNT>(acc, red8);
+    if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m) pdot2[(int64_t)(j0 + threadIdx.x) * G + blockIdx.x] = s;
   }
 }
 
@@ -577,6 +567,12 @@ __global__ void __launch_bounds__(NT) k_jacobi(const double* __restrict__ T, int
                                                double* evals, const LanczosFlags* fl, int gate) {
   if (gate && stopped(fl)) return;
   jacobi_eig<NT>(T, ldt, n, A, Z, evals);
+}
+template <int NT>
+__global__ void __launch_bounds__(NT) k_jacobi_refined(const double* __restrict__ T, int ldt, int n, double* A,
+                                                       double* evals, const LanczosFlags* fl, int gate) {
+  if (gate && stopped(fl)) return;
+  jacobi_eig_refined<NT>(T, ldt, n, A, evals);
 }
 template <int NT>
 __global__ void __launch_bounds__(NT) k_jacobi_df(const double* __restrict__ T, int ldt, int n, double* A,
@@ -1097,10 +1093,13 @@ void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st) {
   k_sturm<<<1, threads, shm, st>>>(L.T, L.lm, it, lock, L.num_ev, L.en, L.nh, L.tol, L.mdim, L.alpha_part, L.nalpha,
                                    L.alpha_df, L.fl);
 }
-void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaStream_t st) {
+void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, bool refined, cudaStream_t st) {
   const size_t shm = jacobi_smem_bytes(n);
   if (df && n <= kJacobiSmemN)
     k_jacobi_df<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.evals, L.fl, gate_on_done ? 1 : 0);
+  else if (refined && n <= kJacobiRefineN)
+    k_jacobi_refined<256><<<1, 256, jacobi_refined_smem_bytes(n), st>>>(L.T, L.lm, n, L.jacA, L.evals, L.fl,
+                                                                       gate_on_done ? 1 : 0);
   else
     k_jacobi<256><<<1, 256, shm, st>>>(L.T, L.lm, n, L.jacA, L.jacZ, L.evals, L.fl, gate_on_done ? 1 : 0);
 }

@@ -57,8 +57,10 @@ void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaS
 // The same for an FP32 basis with the residual kept in double-float, w = wh + wl.
 void launch_orth_iteration_df(const LanczosDev& L, float* V, float* wh, float* wl, int it0, cudaStream_t st);
 void launch_sturm(const LanczosDev& L, int it, int lock, cudaStream_t st);
-// df: the double-float Jacobi (FP32-mixed solves; orders above kJacobiSmemN use FP64)
-void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, cudaStream_t st);
+// df: the double-float Jacobi (orders above kJacobiSmemN use FP64); refined:
+// the FP64 Jacobi started from an FP32 Jacobi's eigenbasis (FP32-mixed
+// solves, orders up to kJacobiRefineN); otherwise the plain FP64 Jacobi.
+void launch_jacobi(const LanczosDev& L, int n, bool gate_on_done, bool df, bool refined, cudaStream_t st);
 void launch_restart_small(const LanczosDev& L, cudaStream_t st);
 template <class TX>
 void launch_restart_rotate(const LanczosDev& L, const TX* V, TX* U, cudaStream_t st);
@@ -69,7 +71,8 @@ void launch_gram(const LanczosDev& L, const TX* U, const TX* vlast, bool df, cud
 void launch_gram_reduce(const LanczosDev& L, bool df, cudaStream_t st);
 // df: the double-float form on one warp (FP32-mixed solves, ls <= 32)
 void launch_chol(const LanczosDev& L, bool df, cudaStream_t st);
-// df: FP32 vectors combined in compensated FP32 (SMGPU_MIXED_DF); otherwise FP64
+// df: FP32 vectors combined in compensated FP32 (the FP32-mixed solves, whose
+// updated basis is stored in FP32); otherwise FP64
 template <class TX>
 void launch_restart_apply(const LanczosDev& L, const TX* U, TX* V, bool df, cudaStream_t st);
 template <class TX>

@@ -19,17 +19,62 @@ __device__ __forceinline__ double warp_sum(double x) {
   return x;
 }
 
-// Deterministic block sum, result returned to every thread.
+// Deterministic block sum, result returned to every thread.  The warps'
+// sums are added by one thread and broadcast: on this GPU FP64 adds are
+// scarce, and letting every thread add them up costs NT/32 times as many.
 template <int NT>
 __device__ __forceinline__ double block_sum_all(double x, double* red) {
+  __shared__ double s_bcast;
   x = warp_sum(x);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) red[wid] = x;
   __syncthreads();
-  double s = 0.0;
+  if (threadIdx.x == 0) {
+    double s = 0.0;
 #pragma unroll
-  for (int k = 0; k < NT / 32; ++k) s += red[k];
+    for (int k = 0; k < NT / 32; ++k) s += red[k];
+    s_bcast = s;
+  }
+  __syncthreads();
+  return s_bcast;
+}
+
+// Eight deterministic block sums at once (a[q] per thread, q < 8); the sum of
+// value q is returned in thread q, other threads get an unspecified value.
+// The warp stage is a reduce-scatter: each of three halving exchanges keeps
+// half of the values, so a lane does 9 FP64 adds for all eight sums instead
+// of 40 (5 per value), then lane l holds the warp's sum of value l >> 2.
+// red: (NT/32) x 8 doubles of shared memory.
+template <int NT>
+__device__ __forceinline__ double block_sum8(const double (&a)[8], double* red) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  double h[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const double keep = b4 ? a[4 + q] : a[q];
+    const double give = b4 ? a[q] : a[4 + q];
+    h[q] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+  }
+  double g[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const double keep = b3 ? h[2 + q] : h[q];
+    const double give = b3 ? h[q] : h[2 + q];
+    g[q] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+  }
+  double u = (b2 ? g[1] : g[0]) + __shfl_xor_sync(0xffffffffu, b2 ? g[0] : g[1], 4);
+  u += __shfl_xor_sync(0xffffffffu, u, 2);
+  u += __shfl_xor_sync(0xffffffffu, u, 1);
+  __syncthreads();
+  if ((lane & 3) == 0) red[wid * 8 + (lane >> 2)] = u;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x < 8) {
+#pragma unroll
+    for (int k = 0; k < NT / 32; ++k) s += red[k * 8 + threadIdx.x];
+  }
   return s;
 }
 
@@ -358,6 +403,197 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
       if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
     evals[rank] = d;
     for (int r = 0; r < n; ++r) A[(int64_t)rank * n + r] = Z_[(int64_t)i * n + r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 Jacobi preconditioned by an FP32 one (the FP32-mixed solve's restart
+// and Ritz eigenproblems, order n <= kJacobiRefineN).  One SM's FP64 pipe runs
+// a from-scratch FP64 Jacobi of order ~30 for most of a millisecond on this
+// GPU; most of that goes into the early sweeps, whose rotations an FP32
+// Jacobi does on the FP32 pipe.  So:
+//   1. FP32 Jacobi sweeps on T give an approximate eigenbasis Z0 (~1e-6);
+//   2. Q = Z0 made orthonormal in FP64 by two Newton-Schulz steps
+//      Q <- Q (3I - QᵀQ) / 2 (orthonormal to FP64 rounding);
+//   3. A1 = Qᵀ T Q in FP64 — an FP64 similarity transform of T, nearly
+//      diagonal;
+//   4. FP64 Jacobi sweeps on A1 (a pair is rotated while
+//      a_pq² > 1e-34 ||A1||_F², as jacobi_eig's stopping test);
+//   5. eigenvectors Q Z1 in FP64, eigenvalues diag(A1) ascending.
+// The result is an FP64 Jacobi eigendecomposition of T.
+constexpr int kJacobiRefineN = 32;
+__host__ __device__ inline size_t jacobi_refined_smem_bytes(int n) {
+  const int N = n + (n & 1);
+  return sizeof(double) * (4 * (size_t)n * n + N + N) + sizeof(float) * (2 * (size_t)n * n + N) +
+         sizeof(int) * (size_t)N + 64;
+}
+
+// Parallel cyclic Jacobi sweeps (round-robin pairing, n/2 disjoint rotations
+// per round) on the symmetric matrix A_ (n x n, column-major, shared memory),
+// accumulating the rotations into Z_.  A pair is rotated while a_pq² > thr;
+// the sweeps stop when a sweep starts with no such pair, or after maxsweep.
+template <int NT, class R>
+__device__ void jacobi_sweeps(R* A_, R* Z_, int n, R thr, int maxsweep, R* cc, R* ss, int* pp, int* qq) {
+  const int N = n + (n & 1);
+  const int npair = N / 2;
+  const int tid = threadIdx.x;
+  for (int sweep = 0; sweep < maxsweep; ++sweep) {
+    int above = 0;
+    for (int idx = tid; idx < n * n; idx += NT) {
+      const int i = idx % n, j = idx / n;
+      const R a = A_[idx];
+      if (i < j && a * a > thr) above = 1;
+    }
+    if (!__syncthreads_or(above)) break;
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = tid; k < npair; k += NT) {
+        int p, q;
+        if (k == 0) { p = N - 1; q = r; }
+        else { p = (r + k) % (N - 1); q = (r - k + (N - 1)) % (N - 1); }
+        if (p > q) { const int x = p; p = q; q = x; }
+        R c = R(1), sn = R(0);
+        if (q < n) {
+          const R apq = A_[(int64_t)q * n + p];
+          if (apq * apq > thr) {
+            const R app = A_[(int64_t)p * n + p], aqq = A_[(int64_t)q * n + q];
+            const R theta = (aqq - app) / (R(2) * apq);
+            const R t = (fabs(theta) > R(1e18)) ? R(0.5) / theta
+                                                 : (theta >= R(0) ? R(1) : R(-1)) / (fabs(theta) + sqrt(R(1) + theta * theta));
+            c = R(1) / sqrt(R(1) + t * t);
+            sn = t * c;
+          }
+        }
+        pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = sn;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        const int k = idx / n, i = idx % n;
+        const R sk = ss[k];
+        if (sk == R(0)) continue;
+        const int p = pp[k], q = qq[k];
+        const R ck = cc[k];
+        const R aip = A_[(int64_t)p * n + i], aiq = A_[(int64_t)q * n + i];
+        A_[(int64_t)p * n + i] = ck * aip - sk * aiq;
+        A_[(int64_t)q * n + i] = sk * aip + ck * aiq;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        const int k = idx / n, j = idx % n;
+        const R sk = ss[k];
+        if (sk == R(0)) continue;
+        const int p = pp[k], q = qq[k];
+        const R ck = cc[k];
+        const R apj = A_[(int64_t)j * n + p], aqj = A_[(int64_t)j * n + q];
+        A_[(int64_t)j * n + p] = ck * apj - sk * aqj;
+        A_[(int64_t)j * n + q] = sk * apj + ck * aqj;
+      }
+      __syncthreads();
+      for (int k = tid; k < npair; k += NT)
+        if (ss[k] != R(0)) {
+          A_[(int64_t)qq[k] * n + pp[k]] = R(0);
+          A_[(int64_t)pp[k] * n + qq[k]] = R(0);
+        }
+      for (int idx = tid; idx < npair * n; idx += NT) {
+        const int k = idx / n, i = idx % n;
+        const R sk = ss[k];
+        if (sk == R(0)) continue;
+        const int p = pp[k], q = qq[k];
+        const R ck = cc[k];
+        const R zip = Z_[(int64_t)p * n + i], ziq = Z_[(int64_t)q * n + i];
+        Z_[(int64_t)p * n + i] = ck * zip - sk * ziq;
+        Z_[(int64_t)q * n + i] = sk * zip + ck * ziq;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// out = op(X) Y for n x n column-major matrices in shared memory, FP64;
+// op(X) = Xᵀ when tx.  out must not alias X or Y.
+template <int NT>
+__device__ void small_matmul(const double* X, bool tx, const double* Y, double* out, int n) {
+  for (int idx = threadIdx.x; idx < n * n; idx += NT) {
+    const int i = idx % n, j = idx / n;
+    double acc = 0.0;
+    for (int k = 0; k < n; ++k) acc = fma(tx ? X[(int64_t)i * n + k] : X[(int64_t)k * n + i], Y[(int64_t)j * n + k], acc);
+    out[idx] = acc;
+  }
+  __syncthreads();
+}
+
+template <int NT>
+__device__ void jacobi_eig_refined(const double* __restrict__ T, int ldt, int n, double* A_out, double* evals) {
+  __shared__ double red[NT / 32];
+  extern __shared__ double shj[];
+  const int N = n + (n & 1);
+  const int npair = N / 2;
+  const int nn = n * n;
+  double* Ad = shj;           // T, then Qᵀ T Q
+  double* Q = Ad + nn;
+  double* W = Q + nn;
+  double* Zd = W + nn;
+  double* ccd = Zd + nn;
+  double* ssd = ccd + npair;
+  double* dg = ssd + npair;
+  float* Af = reinterpret_cast<float*>(dg + N);
+  float* Zf = Af + nn;
+  float* ccf = Zf + nn;
+  float* ssf = ccf + npair;
+  int* pp = reinterpret_cast<int*>(ssf + npair);
+  int* qq = pp + npair;
+  const int tid = threadIdx.x;
+  // 1. FP32 Jacobi on T
+  float frf = 0.f;
+  for (int idx = tid; idx < nn; idx += NT) {
+    const int i = idx % n, j = idx / n;
+    const double x = T[(int64_t)j * ldt + i];
+    Ad[idx] = x;
+    Af[idx] = (float)x;
+    Zf[idx] = (i == j) ? 1.f : 0.f;
+    frf += (float)x * (float)x;
+  }
+  frf = (float)block_sum_all<NT>((double)frf, red);  // also the barrier after the loads
+  jacobi_sweeps<NT, float>(Af, Zf, n, 1e-12f * frf, 12, ccf, ssf, pp, qq);
+  // 2. Q = Z0 made orthonormal in FP64 (Newton-Schulz, twice)
+  for (int idx = tid; idx < nn; idx += NT) Q[idx] = (double)Zf[idx];
+  __syncthreads();
+  for (int it = 0; it < 2; ++it) {
+    small_matmul<NT>(Q, true, Q, W, n);  // W = QᵀQ
+    for (int idx = tid; idx < nn; idx += NT) {
+      const int i = idx % n, j = idx / n;
+      W[idx] = 0.5 * ((i == j ? 3.0 : 0.0) - W[idx]);
+    }
+    __syncthreads();
+    small_matmul<NT>(Q, false, W, Zd, n);  // Zd = Q (3I - QᵀQ)/2
+    for (int idx = tid; idx < nn; idx += NT) Q[idx] = Zd[idx];
+    __syncthreads();
+  }
+  // 3. A1 = Qᵀ T Q, symmetrised
+  small_matmul<NT>(Ad, false, Q, W, n);  // W = T Q
+  small_matmul<NT>(Q, true, W, Zd, n);   // Zd = Qᵀ T Q
+  double fro = 0.0;
+  for (int idx = tid; idx < nn; idx += NT) {
+    const int i = idx % n, j = idx / n;
+    const double a = 0.5 * (Zd[idx] + Zd[(int64_t)i * n + j]);
+    Ad[idx] = a;
+    fro += a * a;
+  }
+  fro = block_sum_all<NT>(fro, red);
+  for (int idx = tid; idx < nn; idx += NT) Zd[idx] = (idx % n == idx / n) ? 1.0 : 0.0;
+  __syncthreads();
+  // 4. FP64 Jacobi sweeps
+  jacobi_sweeps<NT, double>(Ad, Zd, n, 1e-34 * fro, 64, ccd, ssd, pp, qq);
+  // 5. eigenvectors Q Z1, eigenvalues ascending
+  small_matmul<NT>(Q, false, Zd, W, n);
+  for (int i = tid; i < n; i += NT) dg[i] = Ad[(int64_t)i * n + i];
+  __syncthreads();
+  for (int i = tid; i < n; i += NT) {
+    const double d = dg[i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j)
+      if (dg[j] < d || (dg[j] == d && j < i)) ++rank;
+    evals[rank] = d;
+    for (int r = 0; r < n; ++r) A_out[(int64_t)rank * n + r] = W[(int64_t)i * n + r];
   }
 }
 

@@ -255,6 +255,45 @@ struct smgpu_problem {
     tt.nbmax = std::max(nbmax, 1);
     tt.kpad = std::max(4, (kmax + 3) & ~3);
     tt.astride = (tt.kpad % 8 == 0) ? tt.kpad + 4 : tt.kpad;
+    build_2b_tasks();
+  }
+
+  // Tasks of the two-body pass (hv_2b.cu), largest estimated work first:
+  // pp tasks of 32 columns x kPPRows rows, nn tasks of 32 rows x kNNCols
+  // columns, covering every element of every block; and its output array.
+  void build_2b_tasks() {
+    struct Item {
+      double cost;
+      int4 t;
+    };
+    std::vector<Item> pp, nn;
+    for (int b = 0; b < T.nb; ++b) {
+      const int npb = T.np[b], nnb = T.nn[b];
+      for (int r0 = 0; r0 < npb; r0 += kPPRows) {
+        const int nr = std::min(kPPRows, npb - r0);
+        const double e = (double)(T.pp_ptr[T.pstart[b] + r0 + nr] - T.pp_ptr[T.pstart[b] + r0]) + nr;
+        for (int n0 = 0; n0 < nnb; n0 += 32) pp.push_back({e, make_int4(b, r0, n0, nr)});
+      }
+      for (int c0 = 0; c0 < nnb; c0 += kNNCols) {
+        const int nc = std::min(kNNCols, nnb - c0);
+        const double e = (double)(T.nn_ptr[T.nstart[b] + c0 + nc] - T.nn_ptr[T.nstart[b] + c0]) + nc + nnb / 8.0;
+        for (int r0 = 0; r0 < npb; r0 += 32) nn.push_back({e, make_int4(b, r0, c0, nc)});
+      }
+    }
+    auto order = [](std::vector<Item>& v) {
+      std::stable_sort(v.begin(), v.end(), [](const Item& x, const Item& y) { return x.cost > y.cost; });
+      std::vector<int4> out(v.size());
+      for (size_t k = 0; k < v.size(); ++k) out[k] = v[k].t;
+      return out;
+    };
+    const std::vector<int4> ppt = order(pp), nnt = order(nn);
+    tt.pp_tasks = tables.upload(ppt);
+    tt.nn_tasks = tables.upload(nnt);
+    tt.n_pp_tasks = (int)ppt.size();
+    tt.n_nn_tasks = (int)nnt.size();
+    tt.npmax = 1;
+    for (int b = 0; b < T.nb; ++b) tt.npmax = std::max(tt.npmax, T.np[b]);
+    tt.s2b = tables.alloc<float>(2 * (size_t)T.len_pad);
   }
 
   // Device copies of the tables.  with_streams = false for problems that run

@@ -11,7 +11,7 @@ LIB = os.path.join(LIBDIR, "libsmgpu.so")
 INCLUDE = os.path.join(os.path.dirname(ROOT), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["hv.cu", "hv_staged.cu", "hv_multi.cu", "hv_batch.cu", "lanczos.cu", "multi_lanczos.cu", "batch_lanczos.cu", "enum.cu", "capi.cu",
+CU_SOURCES = ["hv.cu", "hv_staged.cu", "hv_2b.cu", "hv_multi.cu", "hv_batch.cu", "lanczos.cu", "multi_lanczos.cu", "batch_lanczos.cu", "enum.cu", "capi.cu",
               "multi.cu", "batch.cu", "obtr.cu", "ec.cu", "membw.cu"]
 CXX_SOURCES = ["setup.cpp", "wavio.cpp", "obtr.cpp"]
 
