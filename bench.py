@@ -318,6 +318,14 @@ def batch_leg(flush):
     flush()
     r = G.solve(NEV, lm=LM, ls=LS, tol=TOL)
     t_batch = G.timings()["lanczos"]
+    # the same solve in the graph form (per-phase launches captured per cycle)
+    os.environ["SMGPU_BATCH_PERSIST"] = "0"
+    try:
+        flush()
+        rg = G.solve(NEV, lm=LM, ls=LS, tol=TOL)
+        t_graph = G.timings()["lanczos"]
+    finally:
+        del os.environ["SMGPU_BATCH_PERSIST"]
     hv_ms = G.time_matvec(reps=10, flush_l2=True)
     st = G.stats()
     mdims = [int(x) for x in G.mdims]
@@ -347,6 +355,9 @@ def batch_leg(flush):
            "max_abs_dE_vs_oracle_MeV": max(dE_oracle) if dE_oracle else None,
            "n_matvec": r["n_matvec"], "n_restart": r["n_restart"], "converged": r["converged"],
            "kernel_launches": r["kernel_launches"], "create_s": t_create, "fp64_loop_create_s": t_loop_create,
+           "form": "persistent: one cooperative launch per restart cycle (H·v task queue, eigenvalue tests, "
+                   "re-orthogonalisation, grid barriers) + cycle end + 6 restart kernels",
+           "graph_form_s": t_graph, "graph_form_kernel_launches": rg["kernel_launches"],
            "hv_ms": hv_ms, "hv_launch_shape": [st["hv_threads"], st["hv_rows"], st["hv_min_ctas"]],
            "mdim_total": sum(mdims), "problem_matvecs_per_s": 128 * r["n_matvec"] / t_batch}
     if gb:
@@ -465,12 +476,12 @@ def run_gpu(args, dist, rank, local):
     t_e2e = max_over_ranks(dist, statistics.mean(e2e_times))
     cold = cold_e2e(snt, nuc) if rank == 0 else {}
 
-    # ---- roofline of the H·v kernel (FP32-mixed).  Its tables and vectors
-    # are L2-resident, so the bound is the L2 -> SM read rate: L2->L1 bytes
-    # per launch (ncu capture of this kernel) over the event-timed launch,
-    # against the library's own L2 read kernel measured here.  The physical
-    # DRAM figure and the CSR-equivalent figure of the explicit-SpMV model
-    # are reported beside it.
+    # ---- roofline of the FP32-mixed H·v.  Its tables and vectors are
+    # L2-resident, so the bound is the L2 -> SM read rate: the L2->L1 bytes of
+    # one H·v (ncu capture of its kernels: the two-body pass and the staged pn
+    # kernel) over the event-timed H·v, against the library's own L2 read
+    # kernel measured here.  The physical DRAM figure and the CSR-equivalent
+    # figure of the explicit-SpMV model are reported beside it.
     mdim = 1963461
     nnz = g["nnz"] if g else None
     peaks = load_json(os.path.join(ROOT, "MEASURED_PEAKS.json"))
@@ -478,22 +489,23 @@ def run_gpu(args, dist, rank, local):
     hbm_src = "measured" if peaks and peaks.get("hbm_gbs") else "fallback"
     prof = load_json(os.path.join(ROOT, "profiles", "hv_pf4p4n_traffic.json")) or {}
     staged = bool(st.get("hv_staged"))
-    kname = "hv_staged_kernel" if staged else "hv_tile_kernel"
-    kp = prof.get(kname) or {}
+    form = "hv_staged_form" if staged else "hv_tile_kernel"
+    kp = prof.get(form) or {}
     l2_gbs = smgpu.l2_read_bandwidth(32 << 20, 50)
     t_hv = hv_ms_mixed * 1e-3
-    dram = kp.get("mixed_bytes_per_launch")
-    l2b = kp.get("l2_to_l1_bytes_per_launch")
+    dram = kp.get("dram_bytes_per_hv")
+    l2b = kp.get("l2_to_l1_bytes_per_hv")
+    kernels = " + ".join(kp.get("kernels", [form]))
     roof = {"bound": "l2", "unit": "GB/s",
             "achieved": l2b / t_hv / 1e9 if l2b else None, "peak": l2_gbs,
             "frac": (l2b / t_hv / 1e9) / l2_gbs if l2b else None, "traffic": dram,
             "peak_source": "measured here: the library's L2-resident read kernel (smgpu_l2_read_bandwidth, 32 MB)",
-            "l2_to_l1_bytes_per_launch": l2b, "l1tex_wavefront_frac": kp.get("l1tex_wavefront_frac"),
+            "l2_to_l1_bytes_per_hv": l2b, "l1tex_wavefront_frac": kp.get("l1tex_wavefront_frac"),
             "profile": kp.get("source"),
-            "kernel": f"{kname} (FP32-mixed H·v, launch shape {st['hv_threads']}x{st['hv_rows']}"
+            "kernel": f"{kernels} (one FP32-mixed H·v; staged launch shape {st['hv_threads']}x{st['hv_rows']}"
                       f" min {st['hv_min_ctas']} CTAs/SM)", "hv_ms": hv_ms_mixed, "hv_fp64_ms": hv_ms_fp64,
             "hbm": {"achieved": dram / t_hv / 1e9 if dram else None, "peak": hbm, "peak_source": hbm_src,
-                    "frac": dram / t_hv / 1e9 / hbm if dram else None, "bytes_per_launch": dram}}
+                    "frac": dram / t_hv / 1e9 / hbm if dram else None, "bytes_per_hv": dram}}
     if nnz:
         b_alg = nnz * (4 + 4) + 4 * (mdim + 1) + 2 * 1 * mdim * 4
         roof["csr_equivalent"] = {

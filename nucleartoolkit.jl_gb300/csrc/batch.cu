@@ -28,7 +28,7 @@
 #include "setup.h"
 
 namespace {
-constexpr int kChunk = 8192;  // elements per streaming chunk (multiple of 4)
+constexpr int kChunk = 2048;  // elements per streaming chunk (multiple of 4)
 constexpr int kMaxBatch = 4096;
 }  // namespace
 
@@ -268,6 +268,8 @@ struct BatchSolve {
   float* U = nullptr;
   double* w = nullptr;
   int* hv_count = nullptr;
+  int* task_ctr = nullptr;  // persistent form: per-iteration H·v task queues
+  GridSync* gs = nullptr;   // persistent form: grid barrier
   long long launches_first = 0, launches_rest = 0;
 
   void alloc(int lm, int ls, int num_ev, double tol) {
@@ -304,6 +306,8 @@ struct BatchSolve {
     B.fl = A.alloc<LanczosFlags>(np);
     B.ctl = A.alloc<BatchCtl>(1);
     hv_count = A.alloc<int>(1);
+    task_ctr = A.alloc<int>(lm);
+    gs = A.alloc<GridSync>(1);
     cudaStream_t st = H->st;
     SMGPU_CUDA_TRY(cudaMemsetAsync(hv_count, 0, sizeof(int), st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(float) * (size_t)lm * B.LEN, st));
@@ -370,9 +374,20 @@ struct BatchSolve {
       v1dev = H->solver.alloc<double>(H->MTOT);
       SMGPU_CUDA_TRY(cudaMemcpyAsync(v1dev, v1, sizeof(double) * H->MTOT, cudaMemcpyHostToDevice, st));
     }
+    // the persistent form (one cooperative launch per restart cycle) when the
+    // H·v shape has one and the GPU runs it; SMGPU_BATCH_PERSIST=0 selects
+    // the graph form (one graph of per-phase launches per cycle)
+    const char* pe = std::getenv("SMGPU_BATCH_PERSIST");
+    const int pgrid = (pe && std::string(pe) == "0") ? 0 : persist_grid(H->cand, B, H->smem);
+    const bool persist = pgrid > 0;
+    long long spin_limit = 1ll << 24;  // barrier polls (~100 ns each) before a wait gives up
+    if (const char* sl = std::getenv("SMGPU_BATCH_SPIN_LIMIT")) spin_limit = std::max(1ll, std::atoll(sl));
     const double tc0 = now_s();
-    cudaGraphExec_t g_first = capture_cycle(1, 0, &launches_first);
-    cudaGraphExec_t g_rest = capture_cycle(ls + 1, ls, &launches_rest);
+    cudaGraphExec_t g_first = nullptr, g_rest = nullptr;
+    if (!persist) {
+      g_first = capture_cycle(1, 0, &launches_first);
+      g_rest = capture_cycle(ls + 1, ls, &launches_rest);
+    }
     H->times[3] = now_s() - tc0;
     cudaEvent_t e0, e1, e2;
     SMGPU_CUDA_TRY(cudaEventCreate(&e0));
@@ -385,19 +400,52 @@ struct BatchSolve {
     long long launches = 3;
     int n_restart = 0, status = SMGPU_OK;
     BatchCtl ctl{};
-    SMGPU_CUDA_TRY(cudaGraphLaunch(g_first, st));
-    launches += launches_first;
-    while (true) {
-      SMGPU_CUDA_TRY(cudaMemcpyAsync(&ctl, B.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, st));
-      SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
-      if (ctl.all_done) break;
-      ++n_restart;
-      if (n_restart > max_restarts) {
-        status = SMGPU_ERR_NOCONV;
-        break;
+    if (persist) {
+      BatchCycle C{};
+      const auto& tk = H->tasks[H->rows()];
+      C.tasks = tk.first;
+      C.ntasks = tk.second;
+      C.task_ctr = task_ctr;
+      C.hv_count = hv_count;
+      C.gs = gs;
+      C.spin_limit = spin_limit;
+      C.kstart = 1;
+      C.lock = 0;
+      while (true) {
+        SMGPU_CUDA_TRY(cudaMemsetAsync(task_ctr, 0, sizeof(int) * lm, st));
+        SMGPU_CUDA_TRY(cudaMemsetAsync(gs, 0, sizeof(GridSync), st));
+        launch_b_persist_cycle(H->cand, B, V, w, C, H->smem, pgrid, st);
+        launch_b_cycle_end(B, st);
+        launches += 2;
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(&ctl, B.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (ctl.sync_err) break;
+        if (ctl.all_done) break;
+        ++n_restart;
+        if (n_restart > max_restarts) {
+          status = SMGPU_ERR_NOCONV;
+          break;
+        }
+        launch_b_restart(B, V, U, st);
+        launches += 6;
+        C.kstart = ls + 1;
+        C.lock = ls;
       }
-      SMGPU_CUDA_TRY(cudaGraphLaunch(g_rest, st));
-      launches += launches_rest;
+    } else {
+      SMGPU_CUDA_TRY(cudaGraphLaunch(g_first, st));
+      launches += launches_first;
+      while (true) {
+        SMGPU_CUDA_TRY(cudaMemcpyAsync(&ctl, B.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, st));
+        SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
+        if (ctl.all_done) break;
+        ++n_restart;
+        if (n_restart > max_restarts) {
+          status = SMGPU_ERR_NOCONV;
+          break;
+        }
+        SMGPU_CUDA_TRY(cudaGraphLaunch(g_rest, st));
+        launches += launches_rest;
+      }
     }
     std::vector<double> en((size_t)np * B.nh * num_ev);
     std::vector<LanczosFlags> fl(np);
@@ -407,8 +455,11 @@ struct BatchSolve {
     SMGPU_CUDA_TRY(cudaMemcpyAsync(fl.data(), B.fl, sizeof(LanczosFlags) * np, cudaMemcpyDeviceToHost, st));
     SMGPU_CUDA_TRY(cudaEventRecord(e1, st));
     SMGPU_CUDA_TRY(cudaStreamSynchronize(st));
-    cudaGraphExecDestroy(g_first);
-    cudaGraphExecDestroy(g_rest);
+    if (g_first) cudaGraphExecDestroy(g_first);
+    if (g_rest) cudaGraphExecDestroy(g_rest);
+    if (ctl.sync_err)
+      return fail(H, SMGPU_ERR_DEVICE,
+                  "a grid barrier of the persistent batch kernel ran out of its wait limit (SMGPU_BATCH_SPIN_LIMIT)");
     for (int p = 0; p < np; ++p) {
       const int nev = (int)std::min<int64_t>(num_ev, H->P[p]->T.mdim);
       for (int j = 0; j < num_ev; ++j)

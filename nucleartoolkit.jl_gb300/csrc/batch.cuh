@@ -27,7 +27,29 @@ struct BatchProblemDev {
 struct BatchCtl {
   int all_done;  // every problem has converged
   int ndone;
-  int pad0, pad1;
+  int sync_err;  // a grid barrier of the persistent cycle kernel ran out of its wait limit
+  int pad1;
+};
+
+// Grid barrier state of the persistent cycle kernel (zeroed once per solve).
+struct GridSync {
+  unsigned count;
+  unsigned gen;
+};
+
+// One restart cycle of the batched Lanczos as one persistent (cooperative)
+// launch: iterations kstart .. lm-1, each phase of an iteration (H·v over
+// a device task queue with the previous iteration's eigenvalue tests, the
+// re-orthogonalisation passes, β and the next vector) separated by a grid
+// barrier, and the last eigenvalue test.
+struct BatchCycle {
+  const int4* tasks;    // H·v tasks (problem, block, first row, α slot), largest first
+  int ntasks;
+  int* task_ctr;        // lm counters: the H·v task queue of each iteration (zeroed before the launch)
+  int* hv_count;        // batched H·v iterations executed
+  GridSync* gs;
+  long long spin_limit; // polls of a barrier wait before it gives up (sync_err)
+  int kstart, lock;
 };
 
 struct BatchDev {
@@ -69,6 +91,8 @@ struct BatchEpi {
   int* count;                // incremented once per launch while some problem runs (null: none)
 };
 
+constexpr int kBatchQM = 3;  // output columns per thread of the staged batch H·v bodies
+
 struct BatchHvConfig {
   int nt, rows, minb;
   int staged;  // 1: the staged pn row body (hv_staged.cuh); 0: the row-tile body
@@ -91,6 +115,14 @@ void launch_b_init(const BatchDev& B, const double* w, float* V0, cudaStream_t s
 void launch_b_sturm(const BatchDev& B, int k, int lock, cudaStream_t st);
 void launch_b_orth(const BatchDev& B, float* V, double* w, int it0, cudaStream_t st);
 void launch_b_cycle_end(const BatchDev& B, cudaStream_t st);
+// The persistent cycle kernel for the H·v launch shape `cand` (of
+// hv_batch_candidates) with dynamic shared memory smem_hv for its H·v body.
+// persist_supported: whether that shape has a persistent form.
+bool persist_supported(int cand);
+// Grid size (co-resident CTAs) of the persistent kernel, 0 when it cannot run.
+int persist_grid(int cand, const BatchDev& B, size_t smem_hv);
+void launch_b_persist_cycle(int cand, const BatchDev& B, float* V, double* w, const BatchCycle& C, size_t smem_hv,
+                            int grid, cudaStream_t st);
 void launch_b_restart(const BatchDev& B, float* V, float* U, cudaStream_t st);
 // Ritz vectors of problem p: Jacobi of its T[0:n,0:n], then R (nev x len, FP64, padded)
 void launch_b_jacobi_one(const BatchDev& B, int p, int n, cudaStream_t st);

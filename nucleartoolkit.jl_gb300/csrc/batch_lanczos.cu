@@ -12,7 +12,11 @@
 // FP32 Krylov vectors, FP64 dot products, recurrences and small
 // eigenproblems; FP32 Kahan sums for the restart rotation (the mixed form of
 // lanczos.cu).
+#include <algorithm>
+
 #include "batch.cuh"
+#include "hv_staged.cuh"
+#include "hv_tile.cuh"
 #include "lanczos_dev.cuh"
 
 namespace smgpu {
@@ -107,15 +111,14 @@ __global__ void __launch_bounds__(kNT) k_b_init_scale(const BatchDev B, const do
 // ------------------------------------------------------------ one iteration
 // α (from the H·v partials of the problem), w' = w − α v_k, partials of
 // v_j·w' (j <= it0) and of ||w'||² (slot it0+1).
-__global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const float* __restrict__ V, double* w,
-                                                    int it0) {
-  const int c = blockIdx.x;
+template <int NT>
+__device__ void b_orth_dot_body(const BatchDev& B, const int c, const float* __restrict__ V, double* w, int it0) {
   const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
-  __shared__ double red[kNT / 32];
-  __shared__ double red8[(kNT / 32) * 8];
-  const double alpha = sum_partials_d2<kNT>(B.alpha_part + (int64_t)it0 * B.nslots + P.slot0, P.nslots, red);
+  __shared__ double red[NT / 32];
+  __shared__ double red8[(NT / 32) * 8];
+  const double alpha = sum_partials_d2<NT>(B.alpha_part + (int64_t)it0 * B.nslots + P.slot0, P.nslots, red);
   const float* __restrict__ Vb = V + P.voff;
   const float* __restrict__ vk = Vb + (int64_t)it0 * B.LEN;
   double* wb = w + P.voff;
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
     float acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.f;
-    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
       float h[4], l[4];
       if (j0 == 0) {
         double wv[4], x[4];
@@ -171,25 +174,27 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const floa
       dacc[q].lo = 0.f;
     }
     float2 s;
-    block_sum_df<kNT, 8>(dacc, red8, s);
+    block_sum_df<NT, 8>(dacc, red8, s);
     if (threadIdx.x < 8 && j0 + (int)threadIdx.x <= m)
       B.pdot[(int64_t)(j0 + threadIdx.x) * B.nchunks + c] = (double)s.x + (double)s.y;
   }
 }
 
 // Second-pass decision of the problem, identical in all its CTAs.
+template <int NT>
 __device__ __forceinline__ bool b_need_second(const BatchDev& B, const BatchProblemDev& P, int m, double* red) {
-  const double n0 = sum_partials_d2<kNT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
-  const double n1 = sum_partials_d2<kNT>(B.pn1 + P.chunk0, P.nchunks, red);
+  const double n0 = sum_partials_d2<NT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
+  const double n1 = sum_partials_d2<NT>(B.pn1 + P.chunk0, P.nchunks, red);
   return n1 < 0.5 * n0;
 }
 
 // w -= Σ_j h_j V_j over the chunk; pout[c] = ||w chunk||².
-__device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblemDev& P, const int4 ch,
+template <int NT>
+__device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblemDev& P, const int c, const int4 ch,
                                            const float* __restrict__ V, double* w, int m,
                                            const double* __restrict__ ph, double* __restrict__ pout, double* hs,
                                            double* red) {
-  sum_many_strided<kNT>(ph + P.chunk0, B.nchunks, P.nchunks, m, hs);
+  sum_many_strided<NT>(ph + P.chunk0, B.nchunks, P.nchunks, m, hs);
   const float* __restrict__ Vb = V + P.voff;
   double* wb = w + P.voff;
   double nrm = 0.0;
@@ -197,9 +202,9 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
   // subtraction per element
   float* hh = reinterpret_cast<float*>(hs + m);
   float* hl = hh + m;
-  for (int j = threadIdx.x; j < m; j += kNT) df_split(hs[j], hh[j], hl[j]);
+  for (int j = threadIdx.x; j < m; j += NT) df_split(hs[j], hh[j], hl[j]);
   __syncthreads();
-  for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+  for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
     DFAcc s4[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) s4[u].init();
@@ -220,36 +225,36 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
     }
     store4(wb + i, t);
   }
-  const double s = block_sum_d2<kNT>(nrm, red);
-  if (threadIdx.x == 0) pout[blockIdx.x] = s;
+  const double s = block_sum_d2<NT>(nrm, red);
+  if (threadIdx.x == 0) pout[c] = s;
 }
 
-__global__ void __launch_bounds__(kNT) k_b_orth_axpy(const BatchDev B, const float* __restrict__ V, double* w,
-                                                     int it0) {
-  const int4 ch = B.chunks[blockIdx.x];
+template <int NT>
+__device__ void b_orth_axpy_body(const BatchDev& B, const int c, const float* __restrict__ V, double* w, int it0) {
+  const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   extern __shared__ double hs[];
-  __shared__ double red[kNT / 32];
-  b_subtract(B, B.probs[ch.x], ch, V, w, it0 + 1, B.pdot, B.pn1, hs, red);
+  __shared__ double red[NT / 32];
+  b_subtract<NT>(B, B.probs[ch.x], c, ch, V, w, it0 + 1, B.pdot, B.pn1, hs, red);
 }
 
-__global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const float* __restrict__ V,
-                                                     const double* __restrict__ w, int it0) {
-  const int c = blockIdx.x;
+template <int NT>
+__device__ void b_orth_dot2_body(const BatchDev& B, const int c, const float* __restrict__ V,
+                                 const double* __restrict__ w, int it0) {
   const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
-  __shared__ double red[kNT / 32];
-  __shared__ double red8[(kNT / 32) * 8];
+  __shared__ double red[NT / 32];
+  __shared__ double red8[(NT / 32) * 8];
   const int m = it0 + 1;
-  if (!b_need_second(B, P, m, red)) return;
+  if (!b_need_second<NT>(B, P, m, red)) return;
   const float* __restrict__ Vb = V + P.voff;
   const double* wb = w + P.voff;
   for (int j0 = 0; j0 < m; j0 += 8) {
     double acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.0;
-    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * kNT) {
+    for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
       double wv[4];
       load4(wb + i, wv);
 #pragma unroll
@@ -261,35 +266,34 @@ __global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const flo
           for (int u = 0; u < 4; ++u) acc[q] = fma(x[u], wv[u], acc[q]);
         }
     }
-    const double s = block_sum8<kNT>(acc, red8);
+    const double s = block_sum8<NT>(acc, red8);
     if (threadIdx.x < 8 && j0 + (int)threadIdx.x < m) B.pdot2[(int64_t)(j0 + threadIdx.x) * B.nchunks + c] = s;
   }
 }
 
-__global__ void __launch_bounds__(kNT) k_b_orth_axpy2(const BatchDev B, const float* __restrict__ V, double* w,
-                                                      int it0) {
-  const int4 ch = B.chunks[blockIdx.x];
+template <int NT>
+__device__ void b_orth_axpy2_body(const BatchDev& B, const int c, const float* __restrict__ V, double* w, int it0) {
+  const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
   extern __shared__ double hs[];
-  __shared__ double red[kNT / 32];
+  __shared__ double red[NT / 32];
   const int m = it0 + 1;
-  if (!b_need_second(B, P, m, red)) return;
-  b_subtract(B, P, ch, V, w, m, B.pdot2, B.pn2, hs, red);
+  if (!b_need_second<NT>(B, P, m, red)) return;
+  b_subtract<NT>(B, P, c, ch, V, w, m, B.pdot2, B.pn2, hs, red);
 }
 
 // β = ||w||, T entries (by the problem's first CTA), v_{it0+1} = w/β.
-__global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V, const double* __restrict__ w,
-                                                      int it0) {
-  const int c = blockIdx.x;
+template <int NT>
+__device__ void b_orth_scale_body(const BatchDev& B, const int c, float* V, const double* __restrict__ w, int it0) {
   const int4 ch = B.chunks[c];
   LanczosFlags* f = B.fl + ch.x;
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(f)))) return;
   const BatchProblemDev& P = B.probs[ch.x];
-  __shared__ double red[kNT / 32];
+  __shared__ double red[NT / 32];
   const int m = it0 + 1;
-  const bool second = b_need_second(B, P, m, red);
-  const double nrm = sum_partials_d2<kNT>((second ? B.pn2 : B.pn1) + P.chunk0, P.nchunks, red);
+  const bool second = b_need_second<NT>(B, P, m, red);
+  const double nrm = sum_partials_d2<NT>((second ? B.pn2 : B.pn1) + P.chunk0, P.nchunks, red);
   const double beta = sqrt(nrm);
   const bool ok = (beta > 0.0) && (beta < INFINITY);
   if (c == P.chunk0 && threadIdx.x == 0) {
@@ -308,13 +312,32 @@ __global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V
   const double inv = 1.0 / beta;
   float* vn = V + (int64_t)(it0 + 1) * B.LEN + P.voff;
   const double* wb = w + P.voff;
-  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += kNT) vn[i] = (float)(wb[i] * inv);
+  for (int64_t i = ch.y + threadIdx.x; i < ch.z; i += NT) vn[i] = (float)(wb[i] * inv);
+}
+
+// The chunk kernels of one iteration: one CTA per chunk.
+__global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const float* __restrict__ V, double* w, int it0) {
+  b_orth_dot_body<kNT>(B, blockIdx.x, V, w, it0);
+}
+__global__ void __launch_bounds__(kNT) k_b_orth_axpy(const BatchDev B, const float* __restrict__ V, double* w, int it0) {
+  b_orth_axpy_body<kNT>(B, blockIdx.x, V, w, it0);
+}
+__global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const float* __restrict__ V,
+                                                     const double* __restrict__ w, int it0) {
+  b_orth_dot2_body<kNT>(B, blockIdx.x, V, w, it0);
+}
+__global__ void __launch_bounds__(kNT) k_b_orth_axpy2(const BatchDev B, const float* __restrict__ V, double* w,
+                                                      int it0) {
+  b_orth_axpy2_body<kNT>(B, blockIdx.x, V, w, it0);
+}
+__global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V, const double* __restrict__ w,
+                                                      int it0) {
+  b_orth_scale_body<kNT>(B, blockIdx.x, V, w, it0);
 }
 
 // Eigenvalue test of every problem (one CTA each): α from the H·v partials,
 // then sturm_step.
-__global__ void k_b_sturm(const BatchDev B, int k, int lock) {
-  const int p = blockIdx.x;
+__device__ void b_sturm_body(const BatchDev& B, const int p, int k, int lock) {
   LanczosFlags* f = B.fl + p;
   if (cta_gate(threadIdx.x == 0 && f->done)) return;
   if (cta_gate(threadIdx.x == 0 && f->exhausted && k > f->exh_k)) {
@@ -345,6 +368,7 @@ __global__ void k_b_sturm(const BatchDev B, int k, int lock) {
   sturm_step(T, B.lm, k, lock, B.num_ev, B.en + (int64_t)p * B.nh * B.num_ev, B.nh, B.tol, P.mdim, f);
   if (threadIdx.x == 0 && f->done) problem_finished(B.ctl, B.nprob);
 }
+__global__ void k_b_sturm(const BatchDev B, int k, int lock) { b_sturm_body(B, blockIdx.x, k, lock); }
 
 __global__ void k_b_cycle_end(const BatchDev B) {
   for (int p = threadIdx.x; p < B.nprob; p += blockDim.x) {
@@ -771,7 +795,161 @@ __global__ void __launch_bounds__(kNT) k_b_ritz(const BatchDev B, const float* _
 }
 
 size_t jacobi_smem(int n) { return jacobi_smem_bytes(n); }
+
+// ------------------------------------------------------- persistent cycle
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid barrier of the cooperative cycle kernel.  Thread 0 of each CTA
+// arrives on a counter; the last arriver resets it and advances the
+// generation the others poll.  Every wait is bounded: after
+// C.spin_limit polls the CTA records sync_err and the kernel unwinds (every
+// CTA leaves at its next barrier), so a lost CTA costs an error status, not
+// a hang.  Returns false when the kernel is to stop.
+__device__ bool grid_sync(const BatchCycle& C, BatchCtl* ctl) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned g = ld_acquire_u32(&C.gs->gen);
+    __threadfence();
+    if (atomicAdd(&C.gs->count, 1u) == gridDim.x - 1) {
+      atomicExch(&C.gs->count, 0u);
+      __threadfence();
+      atomicAdd(&C.gs->gen, 1u);
+    } else {
+      long long polls = 0;
+      while (ld_acquire_u32(&C.gs->gen) == g) {
+        if (++polls > C.spin_limit) {
+          ok = 0;
+          atomicExch(&ctl->sync_err, 1);
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    if (*(volatile int*)&ctl->sync_err) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// One H·v task (the body of hv_batch_staged_kernel / hv_batch_kernel).
+template <int NT, int R, bool STAGED>
+__device__ __forceinline__ void b_hv_task(const BatchDev& B, const int4 tk, const float* v, double* w,
+                                          const float* vprev_all, int it0, double* alpha_part) {
+  if (cta_gate(threadIdx.x == 0 && (B.fl[tk.x].done || B.fl[tk.x].exhausted))) return;
+  const BatchProblemDev& P = B.probs[tk.x];
+  const int64_t off = P.voff;
+  double beta = 0.0;
+  const float* vprev = nullptr;
+  if (vprev_all != nullptr) {
+    vprev = vprev_all + off;
+    beta = B.T[(int64_t)tk.x * B.lm * B.lm + (int64_t)(it0 - 1) * B.lm + it0];
+  }
+  if constexpr (STAGED)
+    hv_staged_rows<NT, R, kBatchQM, false>(P.a, v + off, w + off, vprev, beta, tk.y, tk.z, alpha_part + tk.w);
+  else
+    hv_tile_rows<float, float, AccKahan, NT, R>(P.a, v + off, w + off, vprev, tk.y, tk.z, beta, alpha_part + tk.w);
+}
+
+// Registers capped as the H·v shapes of the graph form (64 threads: 8 CTAs
+// per SM; 128 threads: 4).
+template <int NT, int R, bool STAGED>
+__global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, float* V, double* w, const BatchCycle C) {
+  __shared__ int s_task;
+  const int nb = gridDim.x;
+  for (int it = C.kstart; it <= B.lm - 1; ++it) {
+    const int it0 = it - 1;
+    // phase A: the previous iteration's eigenvalue tests (one CTA per
+    // problem), then the H·v row tasks from this iteration's queue
+    if (it > C.kstart)
+      for (int p = blockIdx.x; p < B.nprob; p += nb) b_sturm_body(B, p, it - 1, C.lock);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !*(volatile int*)&B.ctl->all_done) atomicAdd(C.hv_count, 1);
+    const float* vprev = (it0 > C.lock) ? V + (int64_t)(it0 - 1) * B.LEN : nullptr;
+    double* ap = B.alpha_part + (int64_t)it0 * B.nslots;
+    while (true) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_task = atomicAdd(C.task_ctr + it0, 1);
+      __syncthreads();
+      const int task = s_task;
+      if (task >= C.ntasks) break;
+      b_hv_task<NT, R, STAGED>(B, C.tasks[task], V + (int64_t)it0 * B.LEN, w, vprev, it0, ap);
+    }
+    if (!grid_sync(C, B.ctl)) return;
+    if (*(volatile int*)&B.ctl->all_done) return;  // set only in phase A: the same for every CTA
+    // the re-orthogonalisation passes, β and the next vector (chunk phases)
+    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_dot_body<NT>(B, c, V, w, it0);
+    if (!grid_sync(C, B.ctl)) return;
+    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy_body<NT>(B, c, V, w, it0);
+    if (!grid_sync(C, B.ctl)) return;
+    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_dot2_body<NT>(B, c, V, w, it0);
+    if (!grid_sync(C, B.ctl)) return;
+    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy2_body<NT>(B, c, V, w, it0);
+    if (!grid_sync(C, B.ctl)) return;
+    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_scale_body<NT>(B, c, V, w, it0);
+    if (!grid_sync(C, B.ctl)) return;
+  }
+  for (int p = blockIdx.x; p < B.nprob; p += nb) b_sturm_body(B, p, B.lm - 1, C.lock);
+}
+
+// cand (index into hv_batch_candidates) -> persistent instance
+template <int NT, int R, bool STAGED>
+struct PersistKernel {
+  static void* fn() { return (void*)k_b_cycle<NT, R, STAGED>; }
+};
+void* persist_fn(int cand) {
+  switch (cand) {
+    case 3: return PersistKernel<128, 1, false>::fn();
+    case 4: return PersistKernel<128, 2, false>::fn();
+    case 6: return PersistKernel<128, 2, false>::fn();
+    case 8: return PersistKernel<64, 1, true>::fn();
+    case 9: return PersistKernel<128, 1, true>::fn();
+    case 10: return PersistKernel<128, 1, true>::fn();
+    default: return nullptr;
+  }
+}
+int persist_nt(int cand) { return cand == 8 ? 64 : 128; }
+size_t persist_smem(const BatchDev& B, size_t smem_hv) {
+  size_t m = smem_hv;
+  m = std::max(m, sizeof(double) * (3 * (size_t)B.lm + B.num_ev));  // eigenvalue test
+  m = std::max(m, 2 * sizeof(double) * (size_t)(B.lm + 1));         // h_j and their splits
+  return m;
+}
 }  // namespace
+
+bool persist_supported(int cand) { return persist_fn(cand) != nullptr; }
+
+int persist_grid(int cand, const BatchDev& B, size_t smem_hv) {
+  void* f = persist_fn(cand);
+  if (!f) return 0;
+  const size_t smem = persist_smem(B, smem_hv);
+  int dev = 0, sms = 0, coop = 0, per_sm = 0;
+  SMGPU_CUDA_TRY(cudaGetDevice(&dev));
+  SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+  if (!coop) return 0;
+  SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  SMGPU_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  SMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, persist_nt(cand), smem));
+  return per_sm * sms;
+}
+
+void launch_b_persist_cycle(int cand, const BatchDev& B, float* V, double* w, const BatchCycle& C, size_t smem_hv,
+                            int grid, cudaStream_t st) {
+  void* f = persist_fn(cand);
+  if (!f || grid <= 0) throw CudaError{cudaErrorInvalidConfiguration, "persistent cycle kernel", __FILE__, __LINE__};
+  BatchDev b = B;
+  float* v = V;
+  double* ww = w;
+  BatchCycle c = C;
+  void* args[] = {&b, &v, &ww, &c};
+  SMGPU_CUDA_TRY(cudaLaunchCooperativeKernel(f, dim3(grid), dim3(persist_nt(cand)), args, persist_smem(B, smem_hv), st));
+}
 
 // ------------------------------------------------------------------ launchers
 void launch_b_start(const BatchDev& B, uint64_t seed, double* w, cudaStream_t st) {

@@ -37,7 +37,6 @@ __global__ void __launch_bounds__(NT, MINB) hv_batch_kernel(const BatchProblemDe
 }
 
 // The staged pn row body (hv_staged.cuh) on the batch's tasks.
-constexpr int kBQM = 3;  // output columns per thread of the staged batch shapes
 template <int NT, int R, int MINB>
 __global__ void __launch_bounds__(NT, MINB) hv_batch_staged_kernel(const BatchProblemDev* __restrict__ probs,
                                                                    const int4* __restrict__ tasks, const float* v,
@@ -56,7 +55,7 @@ __global__ void __launch_bounds__(NT, MINB) hv_batch_staged_kernel(const BatchPr
     vprev = e.vprev + off;
     beta = e.T[(int64_t)tk.x * e.lm * e.lm + (int64_t)(e.it0 - 1) * e.lm + e.it0];
   }
-  hv_staged_rows<NT, R, kBQM, false>(P.a, v + off, w + off, vprev, beta, tk.y, tk.z,
+  hv_staged_rows<NT, R, kBatchQM, false>(P.a, v + off, w + off, vprev, beta, tk.y, tk.z,
                                      e.alpha_part != nullptr ? e.alpha_part + tk.w : nullptr);
 }
 
@@ -96,7 +95,7 @@ const BatchHvConfig* hv_batch_candidates(int* count) {
   return kBatchCand;
 }
 
-int hv_batch_staged_cols(const BatchHvConfig& c) { return c.nt * kBQM; }
+int hv_batch_staged_cols(const BatchHvConfig& c) { return c.nt * kBatchQM; }
 
 void hv_batch_prepare(int cand, size_t smem) {
   if (kBatchCand[cand].staged) staged_case(cand, nullptr, nullptr, 0, nullptr, nullptr, BatchEpi{}, smem, true, nullptr);

@@ -155,3 +155,51 @@ def test_batch_noconv_and_error_paths(lib, mixed_batch, tmp_path):
     with pytest.raises(SmgpuError) as e:
         _batch([(CKPOT, "Be8"), (CKPOT, "He3")])
     assert e.value.code == L.ERR_NUCLEUS
+
+
+PERSIST_CANDS = (3, 4, 6, 8, 9, 10)  # batched H·v shapes that have a persistent cycle kernel
+
+
+def test_batch_persistent_cycle_every_shape(lib, mixed_batch, monkeypatch):
+    """The persistent form (one cooperative launch per restart cycle: H·v over
+    a device task queue, eigenvalue tests, re-orthogonalisation passes, each
+    phase behind a grid barrier) for every H·v shape that has one, against
+    the oracle and against the graph form; far fewer launches."""
+    probs = mixed_batch[:10]
+    refs = []
+    for snt, nuc in probs:
+        ro = _oracle(snt, nuc).trl(5, lm=30, ls=15, tol=1e-8)
+        refs.append(ro["evals"])
+    for cand in PERSIST_CANDS:
+        monkeypatch.setenv("SMGPU_BATCH_CAND", str(cand))
+        G = _batch(probs)
+        monkeypatch.setenv("SMGPU_BATCH_PERSIST", "0")
+        rg = G.solve(5, lm=30, ls=15, tol=1e-8)
+        monkeypatch.delenv("SMGPU_BATCH_PERSIST")
+        rp = G.solve(5, lm=30, ls=15, tol=1e-8)
+        assert rp["converged"] and rp["problem_converged"].all(), cand
+        for p, ref in enumerate(refs):
+            nev = len(ref)
+            assert np.abs(rp["evals"][p, :nev] - ref).max() <= EIG_MIXED_ATOL, (cand, p)
+            assert np.abs(rp["evals"][p, :nev] - rg["evals"][p, :nev]).max() <= EIG_MIXED_ATOL, (cand, p)
+        # persistent: per cycle the cycle kernel, the cycle end and 6 restart kernels
+        assert rp["kernel_launches"] <= 8 * (rp["n_restart"] + 1) + 3, (cand, rp["kernel_launches"])
+        assert rp["kernel_launches"] * 5 < rg["kernel_launches"], cand
+
+
+def test_batch_persistent_barrier_wait_limit(lib, mixed_batch, monkeypatch):
+    """Every grid-barrier wait of the persistent kernel is bounded: with a
+    wait limit of one poll the kernel gives up at its first barrier, the solve
+    reports SMGPU_ERR_DEVICE, and the handle solves normally afterwards."""
+    from smgpu import SmgpuError
+    from smgpu import _lib as L
+    G = _batch(mixed_batch[:6])
+    r0 = G.solve(5, lm=30, ls=15, tol=1e-8)
+    monkeypatch.setenv("SMGPU_BATCH_SPIN_LIMIT", "1")
+    with pytest.raises(SmgpuError) as e:
+        G.solve(5, lm=30, ls=15, tol=1e-8)
+    assert e.value.code == L.ERR_DEVICE and "wait limit" in str(e.value)
+    monkeypatch.delenv("SMGPU_BATCH_SPIN_LIMIT")
+    r1 = G.solve(5, lm=30, ls=15, tol=1e-8)
+    assert r1["converged"]
+    assert np.array_equal(np.nan_to_num(r1["evals"]), np.nan_to_num(r0["evals"]))
