@@ -31,10 +31,17 @@ struct BatchCtl {
   int pad1;
 };
 
-// Grid barrier state of the persistent cycle kernel (zeroed once per solve).
+// Grid barrier state of the persistent cycle kernel (zeroed before each
+// launch): CTAs arrive in groups of kSyncGroup on their own counters (one
+// 128-byte line each, so the groups' atomics go to different L2 slices), the
+// last arriver of a group on the top counter.
+constexpr int kSyncGroup = 32;
+constexpr int kSyncMaxGroups = 256;  // up to 8,192 CTAs
 struct GridSync {
-  unsigned count;
-  unsigned gen;
+  unsigned count;  // top counter: groups arrived
+  unsigned gen;    // generation, advanced when every group has arrived
+  unsigned pad[30];
+  unsigned group[kSyncMaxGroups][32];  // per-group counter in word 0 of its line
 };
 
 // One restart cycle of the batched Lanczos as one persistent (cooperative)

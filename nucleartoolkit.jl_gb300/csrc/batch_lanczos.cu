@@ -797,32 +797,49 @@ __global__ void __launch_bounds__(kNT) k_b_ritz(const BatchDev B, const float* _
 size_t jacobi_smem(int n) { return jacobi_smem_bytes(n); }
 
 // ------------------------------------------------------- persistent cycle
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+// A gpu-scope load that sees the L2 value without acquire semantics: the
+// barrier polls with it, so a waiting CTA does not invalidate the L1 cache
+// its SM's other CTAs are still working from; one fence after the wait
+// gives the acquire.
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
   unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
 // Grid barrier of the cooperative cycle kernel.  Thread 0 of each CTA
-// arrives on a counter; the last arriver resets it and advances the
-// generation the others poll.  Every wait is bounded: after
-// C.spin_limit polls the CTA records sync_err and the kernel unwinds (every
-// CTA leaves at its next barrier), so a lost CTA costs an error status, not
-// a hang.  Returns false when the kernel is to stop.
+// arrives on its group's counter; the last arriver of a group resets that
+// counter and arrives on the top counter; the last group to arrive resets
+// the top counter and advances the generation the others poll.  (Arrivals
+// are spread over many counters: a thousand CTAs on one address serialise
+// for tens of microseconds.)  Every wait is bounded: after C.spin_limit polls
+// the CTA records sync_err and the kernel unwinds (every CTA leaves at its
+// next barrier), so a lost CTA costs an error status, not a hang.  Returns
+// false when the kernel is to stop.
 __device__ bool grid_sync(const BatchCycle& C, BatchCtl* ctl) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned g = ld_acquire_u32(&C.gs->gen);
+    const unsigned g = ld_relaxed_u32(&C.gs->gen);
     __threadfence();
-    if (atomicAdd(&C.gs->count, 1u) == gridDim.x - 1) {
+    const unsigned grp = blockIdx.x / kSyncGroup;
+    const unsigned ngroups = (gridDim.x + kSyncGroup - 1) / kSyncGroup;
+    const unsigned in_grp = min((unsigned)kSyncGroup, gridDim.x - grp * kSyncGroup);
+    bool last = false;
+    if (atomicAdd(&C.gs->group[grp][0], 1u) == in_grp - 1) {
+      __threadfence();  // the group's writes, seen through its counter, before the top arrival
+      atomicExch(&C.gs->group[grp][0], 0u);
+      last = atomicAdd(&C.gs->count, 1u) == ngroups - 1;
+      if (last) __threadfence();
+    }
+    if (last) {
       atomicExch(&C.gs->count, 0u);
       __threadfence();
       atomicAdd(&C.gs->gen, 1u);
     } else {
       long long polls = 0;
-      while (ld_acquire_u32(&C.gs->gen) == g) {
+      while (ld_relaxed_u32(&C.gs->gen) == g) {
         if (++polls > C.spin_limit) {
           ok = 0;
           atomicExch(&ctl->sync_err, 1);
@@ -837,6 +854,41 @@ __device__ bool grid_sync(const BatchCycle& C, BatchCtl* ctl) {
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// The eigenvalue tests of iteration k, problem p by CTA floor(p·nb/nprob):
+// spread over the grid (the tests are FP64-heavy, and CTAs of adjacent
+// indices may share an SM).
+__device__ void b_sturm_spread(const BatchDev& B, int nb, int k, int lock) {
+  const int c = blockIdx.x;
+  const int pb = (int)(((long long)c * B.nprob + nb - 1) / nb), pe = (int)(((long long)(c + 1) * B.nprob + nb - 1) / nb);
+  for (int p = pb; p < pe; ++p) b_sturm_body(B, p, k, lock);
+}
+
+// Whether some running problem may take the second Gram-Schmidt pass at
+// this iteration (b_need_second's test of each problem, from the completed
+// partials, with a margin for the different summation order; the chunk
+// kernels then decide per problem exactly).
+template <int NT>
+__device__ bool any_second(const BatchDev& B, int m) {
+  __shared__ int s_any;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int p = threadIdx.x; p < B.nprob; p += NT) {
+    const LanczosFlags* f = B.fl + p;
+    if (*(volatile int*)&f->done || *(volatile int*)&f->exhausted) continue;
+    const BatchProblemDev& P = B.probs[p];
+    double n0 = 0.0, n1 = 0.0;
+    for (int q = 0; q < P.nchunks; ++q) {
+      n0 += B.pdot[(int64_t)m * B.nchunks + P.chunk0 + q];
+      n1 += B.pn1[P.chunk0 + q];
+    }
+    if (n1 < 0.5 * n0 * (1.0 + 1e-6)) s_any = 1;  // conservative: the chunk kernels decide exactly
+  }
+  __syncthreads();
+  const bool any = s_any != 0;
+  __syncthreads();
+  return any;
 }
 
 // One H·v task (the body of hv_batch_staged_kernel / hv_batch_kernel).
@@ -868,18 +920,22 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, floa
     const int it0 = it - 1;
     // phase A: the previous iteration's eigenvalue tests (one CTA per
     // problem), then the H·v row tasks from this iteration's queue
-    if (it > C.kstart)
-      for (int p = blockIdx.x; p < B.nprob; p += nb) b_sturm_body(B, p, it - 1, C.lock);
+    if (it > C.kstart) b_sturm_spread(B, nb, it - 1, C.lock);
     if (blockIdx.x == 0 && threadIdx.x == 0 && !*(volatile int*)&B.ctl->all_done) atomicAdd(C.hv_count, 1);
     const float* vprev = (it0 > C.lock) ? V + (int64_t)(it0 - 1) * B.LEN : nullptr;
     double* ap = B.alpha_part + (int64_t)it0 * B.nslots;
+    // tasks are taken kGrab at a time: one atomic per kGrab tasks keeps
+    // the queue counter off the critical path
+    constexpr int kGrab = 8;
     while (true) {
       __syncthreads();
-      if (threadIdx.x == 0) s_task = atomicAdd(C.task_ctr + it0, 1);
+      if (threadIdx.x == 0) s_task = atomicAdd(C.task_ctr + it0, kGrab);
       __syncthreads();
-      const int task = s_task;
-      if (task >= C.ntasks) break;
-      b_hv_task<NT, R, STAGED>(B, C.tasks[task], V + (int64_t)it0 * B.LEN, w, vprev, it0, ap);
+      const int t0 = s_task;
+      if (t0 >= C.ntasks) break;
+      const int t1 = min(C.ntasks, t0 + kGrab);
+      for (int task = t0; task < t1; ++task)
+        b_hv_task<NT, R, STAGED>(B, C.tasks[task], V + (int64_t)it0 * B.LEN, w, vprev, it0, ap);
     }
     if (!grid_sync(C, B.ctl)) return;
     if (*(volatile int*)&B.ctl->all_done) return;  // set only in phase A: the same for every CTA
@@ -888,14 +944,18 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, floa
     if (!grid_sync(C, B.ctl)) return;
     for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy_body<NT>(B, c, V, w, it0);
     if (!grid_sync(C, B.ctl)) return;
-    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_dot2_body<NT>(B, c, V, w, it0);
-    if (!grid_sync(C, B.ctl)) return;
-    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy2_body<NT>(B, c, V, w, it0);
-    if (!grid_sync(C, B.ctl)) return;
+    // the second pass only when some running problem needs it (the same
+    // decision in every CTA: it reads the same completed partials)
+    if (any_second<NT>(B, it0 + 1)) {
+      for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_dot2_body<NT>(B, c, V, w, it0);
+      if (!grid_sync(C, B.ctl)) return;
+      for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy2_body<NT>(B, c, V, w, it0);
+      if (!grid_sync(C, B.ctl)) return;
+    }
     for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_scale_body<NT>(B, c, V, w, it0);
     if (!grid_sync(C, B.ctl)) return;
   }
-  for (int p = blockIdx.x; p < B.nprob; p += nb) b_sturm_body(B, p, B.lm - 1, C.lock);
+  b_sturm_spread(B, nb, B.lm - 1, C.lock);
 }
 
 // cand (index into hv_batch_candidates) -> persistent instance
@@ -936,7 +996,7 @@ int persist_grid(int cand, const BatchDev& B, size_t smem_hv) {
   SMGPU_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   SMGPU_CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   SMGPU_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, persist_nt(cand), smem));
-  return per_sm * sms;
+  return std::min(per_sm * sms, kSyncGroup * kSyncMaxGroups);
 }
 
 void launch_b_persist_cycle(int cand, const BatchDev& B, float* V, double* w, const BatchCycle& C, size_t smem_hv,

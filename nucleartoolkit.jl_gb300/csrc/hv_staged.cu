@@ -51,7 +51,8 @@ __global__ void __launch_bounds__(NT, MINB) hv_staged_kernel(const HvArgs<float,
 // {threads, rows, -, min CTAs per SM, staged}; a thread owns up to
 // qm_for(threads) output columns.
 constexpr int qm_for(int nt) { return nt <= 128 ? 5 : 3; }
-constexpr HvConfig kStagedCand[] = {{128, 1, 0, 1, 1}, {128, 1, 0, 4, 1}, {128, 1, 0, 5, 1}, {128, 2, 0, 3, 1},
+constexpr HvConfig kStagedCand[] = {{128, 1, 0, 1, 1}, {128, 1, 0, 4, 1}, {128, 1, 0, 5, 1}, {128, 1, 0, 6, 1},
+                                    {128, 2, 0, 3, 1},
                                     {192, 1, 0, 2, 1}, {192, 2, 0, 2, 1}, {256, 1, 0, 1, 1}, {256, 1, 0, 2, 1},
                                     {256, 2, 0, 2, 1}};
 
@@ -70,6 +71,7 @@ bool dispatch(const HvConfig& cfg, const HvArgs<float, float>& a, size_t smem, c
   SMGPU_ST_CASE(128, 1, 1)
   SMGPU_ST_CASE(128, 1, 4)
   SMGPU_ST_CASE(128, 1, 5)
+  SMGPU_ST_CASE(128, 1, 6)
   SMGPU_ST_CASE(128, 2, 3)
   SMGPU_ST_CASE(192, 1, 2)
   SMGPU_ST_CASE(192, 2, 2)

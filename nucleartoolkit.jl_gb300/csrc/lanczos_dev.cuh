@@ -256,6 +256,28 @@ __device__ inline void sturm_step(double* __restrict__ T, int lm, int k, int loc
     const int e = e0 + grp;
     const bool live = e < n;
     double lo = s_lo, hi = s_hi;
+    // Warm start.  T_k grows from T_{k-1} by a row and a column (and after a
+    // restart its leading block holds the kept Ritz values, the previous
+    // test's eigenvalues), so by Cauchy interlacing λ_e(T_k) <= λ_e(T_{k-1})
+    // = en[e]; the new eigenvalue is expected within a few times its last
+    // change below that.  The bracket [l, h] around that guess is taken only
+    // when two Sturm counts (two lanes of the group, in parallel) confirm it
+    // holds λ_e: count(l) <= e < count(h); otherwise the Gershgorin bracket
+    // stays.  The bisection then runs to the same final width as before.
+    {
+      const double prev = live ? en[e] : 0.0, prev2 = live ? en[num_ev + e] : 0.0;
+      const bool warm = live && prev < hi && prev > lo;
+      const double h = prev + 8.0 * DBL_EPSILON * fabs(prev) + 1e-300;
+      const double l = h - fmax(4.0 * fabs(prev2 - prev), 64.0 * DBL_EPSILON * fabs(prev) + 1e-300);
+      int cnt = -1;
+      if (warm && l > lo && h < hi && sub < 2) cnt = sturm_count(a, c2, b2, lock, k, sub == 0 ? l : h, s_piv);
+      const int base = lane & ~(kLPE - 1);
+      const int cl = __shfl_sync(0xffffffffu, cnt, base), ch = __shfl_sync(0xffffffffu, cnt, base + 1);
+      if (warm && cl >= 0 && ch >= 0 && cl <= e && ch >= e + 1) {
+        lo = l;
+        hi = h;
+      }
+    }
     for (int step = 0; step < 200; ++step) {
       const double sigma = lo + (hi - lo) * (double)(sub + 1) * (1.0 / (kLPE + 1));
       const int cnt = live ? sturm_count(a, c2, b2, lock, k, sigma, s_piv) : 0;
