@@ -380,7 +380,7 @@ struct BatchSolve {
     const char* pe = std::getenv("SMGPU_BATCH_PERSIST");
     const int pgrid = (pe && std::string(pe) == "0") ? 0 : persist_grid(H->cand, B, H->smem);
     const bool persist = pgrid > 0;
-    long long spin_limit = 1ll << 24;  // barrier polls (~100 ns each) before a wait gives up
+    long long spin_limit = 1ll << 24;  // barrier polls (each at least 32 ns) before a wait gives up
     if (const char* sl = std::getenv("SMGPU_BATCH_SPIN_LIMIT")) spin_limit = std::max(1ll, std::atoll(sl));
     const double tc0 = now_s();
     cudaGraphExec_t g_first = nullptr, g_rest = nullptr;

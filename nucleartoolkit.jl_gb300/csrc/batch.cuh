@@ -32,16 +32,17 @@ struct BatchCtl {
 };
 
 // Grid barrier state of the persistent cycle kernel (zeroed before each
-// launch): CTAs arrive in groups of kSyncGroup on their own counters (one
-// 128-byte line each, so the groups' atomics go to different L2 slices), the
-// last arriver of a group on the top counter.
+// launch): CTAs arrive in groups of kSyncGroup on their own counters, the
+// last arriver of a group on the top counter, and each group polls its own
+// release word; every counter and release word has a 128-byte line to
+// itself, so arrivals and polls spread over the L2 slices.
 constexpr int kSyncGroup = 32;
 constexpr int kSyncMaxGroups = 256;  // up to 8,192 CTAs
 struct GridSync {
   unsigned count;  // top counter: groups arrived
-  unsigned gen;    // generation, advanced when every group has arrived
-  unsigned pad[30];
-  unsigned group[kSyncMaxGroups][32];  // per-group counter in word 0 of its line
+  unsigned pad[31];
+  unsigned group[kSyncMaxGroups][32];  // per-group arrival counter in word 0 of its line
+  unsigned rel[kSyncMaxGroups][32];    // per-group release generation in word 0 of its line
 };
 
 // One restart cycle of the batched Lanczos as one persistent (cooperative)

@@ -810,42 +810,46 @@ __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
 // Grid barrier of the cooperative cycle kernel.  Thread 0 of each CTA
 // arrives on its group's counter; the last arriver of a group resets that
 // counter and arrives on the top counter; the last group to arrive resets
-// the top counter and advances the generation the others poll.  (Arrivals
-// are spread over many counters: a thousand CTAs on one address serialise
-// for tens of microseconds.)  Every wait is bounded: after C.spin_limit polls
-// the CTA records sync_err and the kernel unwinds (every CTA leaves at its
-// next barrier), so a lost CTA costs an error status, not a hang.  Returns
-// false when the kernel is to stop.
+// the top counter and writes the next generation into every group's release
+// word, which the group's CTAs poll.  (A thousand CTAs arriving on, and
+// polling, one address serialise for tens of microseconds.)  Every wait is
+// bounded: after C.spin_limit polls the CTA records sync_err and the kernel
+// unwinds (every CTA leaves at its next barrier), so a lost CTA costs an
+// error status, not a hang.  Returns false when the kernel is to stop.
+__device__ __forceinline__ void st_relaxed_u32(unsigned* p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 __device__ bool grid_sync(const BatchCycle& C, BatchCtl* ctl) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned g = ld_relaxed_u32(&C.gs->gen);
-    __threadfence();
     const unsigned grp = blockIdx.x / kSyncGroup;
     const unsigned ngroups = (gridDim.x + kSyncGroup - 1) / kSyncGroup;
     const unsigned in_grp = min((unsigned)kSyncGroup, gridDim.x - grp * kSyncGroup);
+    // the group's release word cannot advance before this CTA arrives
+    const unsigned g = ld_relaxed_u32(&C.gs->rel[grp][0]);
+    __threadfence();
     bool last = false;
     if (atomicAdd(&C.gs->group[grp][0], 1u) == in_grp - 1) {
       __threadfence();  // the group's writes, seen through its counter, before the top arrival
       atomicExch(&C.gs->group[grp][0], 0u);
       last = atomicAdd(&C.gs->count, 1u) == ngroups - 1;
-      if (last) __threadfence();
     }
     if (last) {
+      __threadfence();
       atomicExch(&C.gs->count, 0u);
       __threadfence();
-      atomicAdd(&C.gs->gen, 1u);
+      for (unsigned q = 0; q < ngroups; ++q) st_relaxed_u32(&C.gs->rel[q][0], g + 1u);
     } else {
       long long polls = 0;
-      while (ld_relaxed_u32(&C.gs->gen) == g) {
+      while (ld_relaxed_u32(&C.gs->rel[grp][0]) == g) {
         if (++polls > C.spin_limit) {
           ok = 0;
           atomicExch(&ctl->sync_err, 1);
           break;
         }
-        __nanosleep(100);
+        __nanosleep(32);
       }
     }
     __threadfence();
