@@ -28,6 +28,8 @@
 // sums per list, added at its end); the staged kernel adds them to its
 // Kahan-compensated pn sum.  Every element of every block is written (zero
 // when its list is empty).
+#include <algorithm>
+
 #include "device.cuh"
 
 namespace smgpu {
@@ -127,13 +129,10 @@ __device__ __forceinline__ void stream_lists(const int* __restrict__ col, const 
   }
 }
 
-__global__ void __launch_bounds__(kNT2) k_hv_pp(const DevTables t, const int4* __restrict__ tasks,
-                                                const float* __restrict__ pp_val, const float* __restrict__ v,
-                                                float* __restrict__ s_pp, const LanczosFlags* fl) {
-  if (fl != nullptr && cta_gate(threadIdx.x == 0 && (fl->done || fl->exhausted))) return;
-  extern __shared__ float sm[];
-  __shared__ int2 ebuf[kW2][64];
-  const int4 tk = tasks[blockIdx.x];
+// pp task tk = (block, first row, first column, rows).
+__device__ __forceinline__ void pp_task(const DevTables& t, const int4 tk, const float* __restrict__ pp_val,
+                                        const float* __restrict__ v, float* __restrict__ s_pp, float* sm,
+                                        int2 (*ebuf)[64]) {
   const int b = tk.x, r0 = tk.y, n0 = tk.z, nr = tk.w;
   const int np = t.np[b], nn = t.nn[b], stride = t.stride[b];
   const int64_t blk = t.off_pad[b];
@@ -164,13 +163,10 @@ __global__ void __launch_bounds__(kNT2) k_hv_pp(const DevTables t, const int4* _
   });
 }
 
-__global__ void __launch_bounds__(kNT2) k_hv_nn(const DevTables t, const int4* __restrict__ tasks,
-                                                const float* __restrict__ nn_val, const float* __restrict__ v,
-                                                float* __restrict__ s_nn, const LanczosFlags* fl) {
-  if (fl != nullptr && cta_gate(threadIdx.x == 0 && (fl->done || fl->exhausted))) return;
-  extern __shared__ float sm[];
-  __shared__ int2 ebuf[kW2][64];
-  const int4 tk = tasks[blockIdx.x];
+// nn task tk = (block, first row, first column, columns).
+__device__ __forceinline__ void nn_task(const DevTables& t, const int4 tk, const float* __restrict__ nn_val,
+                                        const float* __restrict__ v, float* __restrict__ s_nn, float* sm,
+                                        int2 (*ebuf)[64]) {
   const int b = tk.x, r0 = tk.y, c0 = tk.z, nc = tk.w;
   const int np = t.np[b], nn = t.nn[b], stride = t.stride[b];
   const int nr = min(32, np - r0);
@@ -198,25 +194,39 @@ __global__ void __launch_bounds__(kNT2) k_hv_nn(const DevTables t, const int4* _
   }
 }
 
+// One launch for both terms: CTAs [0, n_nn) take the nn tasks, the rest the
+// pp tasks (each list largest first), so the short pp tasks fill the tail
+// of the nn ones.
+__global__ void __launch_bounds__(kNT2) k_hv_2b(const DevTables t, const int4* __restrict__ nn_tasks, int n_nn,
+                                                const int4* __restrict__ pp_tasks, const float* __restrict__ nn_val,
+                                                const float* __restrict__ pp_val, const float* __restrict__ v,
+                                                float* __restrict__ s2b, const LanczosFlags* fl) {
+  if (fl != nullptr && cta_gate(threadIdx.x == 0 && (fl->done || fl->exhausted))) return;
+  extern __shared__ float sm[];
+  __shared__ int2 ebuf[kW2][64];
+  const int c = blockIdx.x;
+  if (c < n_nn) nn_task(t, nn_tasks[c], nn_val, v, s2b + t.len_pad, sm, ebuf);
+  else pp_task(t, pp_tasks[c - n_nn], pp_val, v, s2b, sm, ebuf);
+}
+
 }  // namespace
 
 size_t hv_2b_nn_smem(const TileTables& tt) { return sizeof(float) * (size_t)32 * (size_t)((tt.nnmax) | 1); }
 
 size_t hv_2b_pp_smem(const TileTables& tt) { return sizeof(float) * 32 * (size_t)tt.npmax; }
 
+static size_t hv_2b_smem(const TileTables& tt) { return std::max(hv_2b_nn_smem(tt), hv_2b_pp_smem(tt)); }
+
 void hv_2b_prepare(const TileTables& tt) {
-  SMGPU_CUDA_TRY(
-      cudaFuncSetAttribute(k_hv_nn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hv_2b_nn_smem(tt)));
-  SMGPU_CUDA_TRY(
-      cudaFuncSetAttribute(k_hv_pp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hv_2b_pp_smem(tt)));
+  SMGPU_CUDA_TRY(cudaFuncSetAttribute(k_hv_2b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hv_2b_smem(tt)));
 }
 
 void launch_hv_2b(const DevTables& t, const TileTables& tt, const CoefTables<float>& c, const float* v,
                   const LanczosFlags* fl, cudaStream_t st) {
-  if (tt.n_pp_tasks > 0)
-    k_hv_pp<<<tt.n_pp_tasks, kNT2, hv_2b_pp_smem(tt), st>>>(t, tt.pp_tasks, c.pp_val, v, tt.s2b, fl);
-  if (tt.n_nn_tasks > 0)
-    k_hv_nn<<<tt.n_nn_tasks, kNT2, hv_2b_nn_smem(tt), st>>>(t, tt.nn_tasks, c.nn_val, v, tt.s2b + t.len_pad, fl);
+  const int n = tt.n_nn_tasks + tt.n_pp_tasks;
+  if (n > 0)
+    k_hv_2b<<<n, kNT2, hv_2b_smem(tt), st>>>(t, tt.nn_tasks, tt.n_nn_tasks, tt.pp_tasks, c.nn_val, c.pp_val, v,
+                                             tt.s2b, fl);
 }
 
 }  // namespace smgpu
