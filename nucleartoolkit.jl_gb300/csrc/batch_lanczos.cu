@@ -135,6 +135,7 @@ __device__ void b_orth_dot_body(const BatchDev& B, const int c, const float* __r
     float acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+    #pragma unroll(NT <= 64 ? 2 : 1)  // 64-thread CTAs (persistent cycle): two trips' loads in flight
     for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
       float h[4], l[4];
       if (j0 == 0) {
@@ -208,6 +209,7 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
     DFAcc s4[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) s4[u].init();
+#pragma unroll(NT <= 64 ? 4 : 1)
     for (int j = 0; j < m; ++j) {
       const float4 x = *reinterpret_cast<const float4*>(Vb + (int64_t)j * B.LEN + i);
       const float a = hh[j], b = hl[j];
@@ -254,6 +256,7 @@ __device__ void b_orth_dot2_body(const BatchDev& B, const int c, const float* __
     double acc[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+    #pragma unroll(NT <= 64 ? 2 : 1)  // 64-thread CTAs (persistent cycle): two trips' loads in flight
     for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
       double wv[4];
       load4(wb + i, wv);
@@ -313,6 +316,7 @@ __device__ void b_orth_scale_body(const BatchDev& B, const int c, float* V, cons
   float* vn = V + (int64_t)(it0 + 1) * B.LEN + P.voff;
   const double* wb = w + P.voff;
   // four elements per thread and trip (chunk bounds are multiples of 4)
+  #pragma unroll(NT <= 64 ? 4 : 1)
   for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
     double t[4];
     load4(wb + i, t);
@@ -345,8 +349,10 @@ __global__ void __launch_bounds__(kNT) k_b_orth_scale(const BatchDev B, float* V
 // then sturm_step.
 __device__ void b_sturm_body(const BatchDev& B, const int p, int k, int lock) {
   LanczosFlags* f = B.fl + p;
-  if (cta_gate(threadIdx.x == 0 && f->done)) return;
-  if (cta_gate(threadIdx.x == 0 && f->exhausted && k > f->exh_k)) {
+  // flags through L2 (in the persistent kernel other CTAs set them)
+  volatile const LanczosFlags* vf = f;
+  if (cta_gate(threadIdx.x == 0 && vf->done)) return;
+  if (cta_gate(threadIdx.x == 0 && vf->exhausted && k > vf->exh_k)) {
     if (threadIdx.x == 0) {
       f->done = 1;
       f->elit = f->exh_k;

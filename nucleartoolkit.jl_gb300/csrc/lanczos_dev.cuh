@@ -11,7 +11,11 @@ namespace dev {
 
 constexpr int kNT = 256;  // threads of the streaming kernels
 
-__device__ __forceinline__ bool stopped(const LanczosFlags* fl) { return fl->done || fl->exhausted; }
+// (volatile: the persistent batch kernel reads flags that other CTAs of the
+// same launch set, so they must come from L2, not from a line in L1)
+__device__ __forceinline__ bool stopped(const LanczosFlags* fl) {
+  return *(volatile const int*)&fl->done || *(volatile const int*)&fl->exhausted;
+}
 
 __device__ __forceinline__ double warp_sum(double x) {
 #pragma unroll
