@@ -190,12 +190,13 @@ __device__ __forceinline__ bool b_need_second(const BatchDev& B, const BatchProb
 }
 
 // w -= Σ_j h_j V_j over the chunk; pout[c] = ||w chunk||².
+// (sum_h: form h_j = Σ ph[j][chunks of P] into hs first; else hs holds them)
 template <int NT>
 __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblemDev& P, const int c, const int4 ch,
                                            const float* __restrict__ V, double* w, int m,
                                            const double* __restrict__ ph, double* __restrict__ pout, double* hs,
-                                           double* red) {
-  sum_many_strided<NT>(ph + P.chunk0, B.nchunks, P.nchunks, m, hs);
+                                           double* red, bool sum_h = true) {
+  if (sum_h) sum_many_strided<NT>(ph + P.chunk0, B.nchunks, P.nchunks, m, hs);
   const float* __restrict__ Vb = V + P.voff;
   double* wb = w + P.voff;
   double nrm = 0.0;
@@ -231,13 +232,86 @@ __device__ __forceinline__ void b_subtract(const BatchDev& B, const BatchProblem
   if (threadIdx.x == 0) pout[c] = s;
 }
 
+// The fast form of the first subtraction (h_j in hs): v_next = (w' -
+// Σ_j h_j V_j) * inv over the chunk; the residual itself is not stored
+// (the next H·v overwrites it).
 template <int NT>
-__device__ void b_orth_axpy_body(const BatchDev& B, const int c, const float* __restrict__ V, double* w, int it0) {
+__device__ __forceinline__ void b_subtract_scale(const BatchDev& B, const BatchProblemDev& P, const int4 ch,
+                                                 const float* __restrict__ V, const double* w, int m, double* hs,
+                                                 const double inv, float* __restrict__ vn) {
+  const float* __restrict__ Vb = V + P.voff;
+  const double* wb = w + P.voff;
+  float* hh = reinterpret_cast<float*>(hs + m);
+  float* hl = hh + m;
+  for (int j = threadIdx.x; j < m; j += NT) df_split(hs[j], hh[j], hl[j]);
+  __syncthreads();
+  for (int64_t i = ch.y + 4 * threadIdx.x; i < ch.z; i += 4 * NT) {
+    DFAcc s4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s4[u].init();
+#pragma unroll(NT <= 64 ? 4 : 1)
+    for (int j = 0; j < m; ++j) {
+      const float4 x = *reinterpret_cast<const float4*>(Vb + (int64_t)j * B.LEN + i);
+      const float a = hh[j], b = hl[j];
+      s4[0].add_prod2(x.x, a, b);
+      s4[1].add_prod2(x.y, a, b);
+      s4[2].add_prod2(x.z, a, b);
+      s4[3].add_prod2(x.w, a, b);
+    }
+    double t[4];
+    load4(wb + i, t);
+    *reinterpret_cast<float4*>(vn + i) =
+        make_float4((float)((t[0] - s4[0].get()) * inv), (float)((t[1] - s4[1].get()) * inv),
+                    (float)((t[2] - s4[2].get()) * inv), (float)((t[3] - s4[3].get()) * inv));
+  }
+}
+
+// β from the norm before the subtraction: with V orthonormal up to its
+// FP32 rounding E, ||w' - Σ h_j v_j||² = ||w'||² - Σ h_j² + hᵀE h, and when
+// Σ h_j² <= kFastNorm ||w'||² the last term is below 1e-15 of the result.
+// Then the subtraction pass also forms β and the next basis vector, and the
+// problem skips the second-pass test and the scaling pass (it cannot need
+// the second pass: ||w''||² >= (1 - kFastNorm) ||w'||²).
+constexpr double kFastNorm = 1e-8;
+
+// w' -= Σ_j h_j V_j over the chunk (first pass).  Every CTA of the problem
+// takes the same fast/slow decision from the same partial sums; the
+// problem's first chunk records it (fastnorm) with β or exhaustion.
+template <int NT>
+__device__ void b_orth_axpy_body(const BatchDev& B, const int c, float* V, double* w, int it0) {
   const int4 ch = B.chunks[c];
-  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  LanczosFlags* f = B.fl + ch.x;
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(f)))) return;
   extern __shared__ double hs[];
   __shared__ double red[NT / 32];
-  b_subtract<NT>(B, B.probs[ch.x], c, ch, V, w, it0 + 1, B.pdot, B.pn1, hs, red);
+  const BatchProblemDev& P = B.probs[ch.x];
+  const int m = it0 + 1;
+  const double n0 = sum_partials_d2<NT>(B.pdot + (int64_t)m * B.nchunks + P.chunk0, P.nchunks, red);
+  sum_many_strided<NT>(B.pdot + P.chunk0, B.nchunks, P.nchunks, m, hs);
+  double hsq = 0.0;
+  for (int j = 0; j < m; ++j) hsq = fma(hs[j], hs[j], hsq);
+  const bool fast = n0 > 0.0 && hsq <= kFastNorm * n0;
+  if (!fast) {
+    if (c == P.chunk0 && threadIdx.x == 0) f->fastnorm = 0;
+    b_subtract<NT>(B, P, c, ch, V, w, m, B.pdot, B.pn1, hs, red, false);
+    return;
+  }
+  const double beta = sqrt(n0 - hsq);
+  const bool ok = beta < INFINITY;
+  if (c == P.chunk0 && threadIdx.x == 0) {
+    f->fastnorm = 1;
+    double* T = B.T + (int64_t)ch.x * B.lm * B.lm;
+    if (ok) {
+      T[(int64_t)it0 * B.lm + it0 + 1] = beta;
+      T[(int64_t)(it0 + 1) * B.lm + it0] = beta;
+      f->second = 0;
+    } else {
+      f->exh_k = it0 + 1;
+      f->exhausted = 1;
+    }
+  }
+  if (!ok) return;
+  b_subtract_scale<NT>(B, P, ch, V, w, m, hs, 1.0 / beta, V + (int64_t)(it0 + 1) * B.LEN + P.voff);
 }
 
 template <int NT>
@@ -245,6 +319,7 @@ __device__ void b_orth_dot2_body(const BatchDev& B, const int c, const float* __
                                  const double* __restrict__ w, int it0) {
   const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  if (cta_gate(threadIdx.x == 0 && *(volatile const int*)&B.fl[ch.x].fastnorm)) return;  // β already taken
   const BatchProblemDev& P = B.probs[ch.x];
   __shared__ double red[NT / 32];
   __shared__ double red8[(NT / 32) * 8];
@@ -278,6 +353,7 @@ template <int NT>
 __device__ void b_orth_axpy2_body(const BatchDev& B, const int c, const float* __restrict__ V, double* w, int it0) {
   const int4 ch = B.chunks[c];
   if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(B.fl + ch.x)))) return;
+  if (cta_gate(threadIdx.x == 0 && *(volatile const int*)&B.fl[ch.x].fastnorm)) return;  // β already taken
   const BatchProblemDev& P = B.probs[ch.x];
   extern __shared__ double hs[];
   __shared__ double red[NT / 32];
@@ -291,7 +367,7 @@ template <int NT>
 __device__ void b_orth_scale_body(const BatchDev& B, const int c, float* V, const double* __restrict__ w, int it0) {
   const int4 ch = B.chunks[c];
   LanczosFlags* f = B.fl + ch.x;
-  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(f)))) return;
+  if (cta_gate(threadIdx.x == 0 && (B.ctl->all_done || stopped(f) || *(volatile const int*)&f->fastnorm))) return;
   const BatchProblemDev& P = B.probs[ch.x];
   __shared__ double red[NT / 32];
   const int m = it0 + 1;
@@ -329,7 +405,7 @@ __device__ void b_orth_scale_body(const BatchDev& B, const int c, float* V, cons
 __global__ void __launch_bounds__(kNT) k_b_orth_dot(const BatchDev B, const float* __restrict__ V, double* w, int it0) {
   b_orth_dot_body<kNT>(B, blockIdx.x, V, w, it0);
 }
-__global__ void __launch_bounds__(kNT) k_b_orth_axpy(const BatchDev B, const float* __restrict__ V, double* w, int it0) {
+__global__ void __launch_bounds__(kNT) k_b_orth_axpy(const BatchDev B, float* V, double* w, int it0) {
   b_orth_axpy_body<kNT>(B, blockIdx.x, V, w, it0);
 }
 __global__ void __launch_bounds__(kNT) k_b_orth_dot2(const BatchDev B, const float* __restrict__ V,
@@ -813,6 +889,11 @@ size_t jacobi_smem(int n) { return jacobi_smem_bytes(n); }
 // barrier polls with it, so a waiting CTA does not invalidate the L1 cache
 // its SM's other CTAs are still working from; one fence after the wait
 // gives the acquire.
+__device__ __forceinline__ int ld_relaxed_s32(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -881,30 +962,32 @@ __device__ void b_sturm_spread(const BatchDev& B, int nb, int k, int lock) {
   for (int p = pb; p < pe; ++p) b_sturm_body(B, p, k, lock);
 }
 
-// Whether some running problem may take the second Gram-Schmidt pass at
-// this iteration (b_need_second's test of each problem, from the completed
-// partials, with a margin for the different summation order; the chunk
-// kernels then decide per problem exactly).
+// Which passes after the subtraction this iteration needs, the same in every
+// CTA (it reads the flags and partials the subtraction pass completed):
+// bit 0, some running problem took the slow form (its β still to come, in
+// the scaling pass); bit 1, one of those may take the second Gram-Schmidt
+// pass (b_need_second's test with a margin for the summation order; the
+// chunk passes then decide per problem exactly).
 template <int NT>
-__device__ bool any_second(const BatchDev& B, int m) {
-  __shared__ int s_any;
-  if (threadIdx.x == 0) s_any = 0;
+__device__ int passes_needed(const BatchDev& B, int m) {
+  __shared__ int s_need;
+  if (threadIdx.x == 0) s_need = 0;
   __syncthreads();
   for (int p = threadIdx.x; p < B.nprob; p += NT) {
     const LanczosFlags* f = B.fl + p;
-    if (*(volatile int*)&f->done || *(volatile int*)&f->exhausted) continue;
+    if (stopped(f) || *(volatile const int*)&f->fastnorm) continue;
     const BatchProblemDev& P = B.probs[p];
     double n0 = 0.0, n1 = 0.0;
     for (int q = 0; q < P.nchunks; ++q) {
       n0 += B.pdot[(int64_t)m * B.nchunks + P.chunk0 + q];
       n1 += B.pn1[P.chunk0 + q];
     }
-    if (n1 < 0.5 * n0 * (1.0 + 1e-6)) s_any = 1;  // conservative: the chunk kernels decide exactly
+    atomicOr(&s_need, (n1 < 0.5 * n0 * (1.0 + 1e-6)) ? 3 : 1);
   }
   __syncthreads();
-  const bool any = s_any != 0;
+  const int need = s_need;
   __syncthreads();
-  return any;
+  return need;
 }
 
 // One H·v task (the body of hv_batch_staged_kernel / hv_batch_kernel).  Not
@@ -933,7 +1016,7 @@ __device__ __noinline__ void b_hv_task(const BatchDev& B, const int4 tk, const f
 // per SM; 128 threads: 4).
 template <int NT, int R, bool STAGED>
 __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, float* V, double* w, const BatchCycle C) {
-  __shared__ int s_task;
+  __shared__ int s_task, s_want;
   const int nb = gridDim.x;
   for (int it = C.kstart; it <= B.lm - 1; ++it) {
     const int it0 = it - 1;
@@ -943,16 +1026,22 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, floa
     if (blockIdx.x == 0 && threadIdx.x == 0 && !*(volatile int*)&B.ctl->all_done) atomicAdd(C.hv_count, 1);
     const float* vprev = (it0 > C.lock) ? V + (int64_t)(it0 - 1) * B.LEN : nullptr;
     double* ap = B.alpha_part + (int64_t)it0 * B.nslots;
-    // tasks are taken kGrab at a time: one atomic per kGrab tasks keeps
-    // the queue counter off the critical path
+    // tasks are taken kGrab at a time (one atomic per kGrab tasks keeps
+    // the queue counter off the critical path) until the last two tasks per
+    // CTA, then singly (a CTA holding kGrab of the last tasks would hold up
+    // the end of the phase)
     constexpr int kGrab = 8;
     while (true) {
       __syncthreads();
-      if (threadIdx.x == 0) s_task = atomicAdd(C.task_ctr + it0, kGrab);
+      if (threadIdx.x == 0) {
+        const int want = ld_relaxed_s32(C.task_ctr + it0) < C.ntasks - 2 * nb ? kGrab : 1;
+        s_task = atomicAdd(C.task_ctr + it0, want);
+        s_want = want;
+      }
       __syncthreads();
       const int t0 = s_task;
       if (t0 >= C.ntasks) break;
-      const int t1 = min(C.ntasks, t0 + kGrab);
+      const int t1 = min(C.ntasks, t0 + s_want);
       for (int task = t0; task < t1; ++task)
         b_hv_task<NT, R, STAGED>(B, C.tasks[task], V + (int64_t)it0 * B.LEN, w, vprev, it0, ap);
     }
@@ -963,16 +1052,19 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, floa
     if (!grid_sync(C, B.ctl)) return;
     for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy_body<NT>(B, c, V, w, it0);
     if (!grid_sync(C, B.ctl)) return;
-    // the second pass only when some running problem needs it (the same
-    // decision in every CTA: it reads the same completed partials)
-    if (any_second<NT>(B, it0 + 1)) {
+    // the second pass and the scaling pass only when some running problem
+    // needs them (the same decision in every CTA)
+    const int need = passes_needed<NT>(B, it0 + 1);
+    if (need & 2) {
       for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_dot2_body<NT>(B, c, V, w, it0);
       if (!grid_sync(C, B.ctl)) return;
       for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_axpy2_body<NT>(B, c, V, w, it0);
       if (!grid_sync(C, B.ctl)) return;
     }
-    for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_scale_body<NT>(B, c, V, w, it0);
-    if (!grid_sync(C, B.ctl)) return;
+    if (need & 1) {
+      for (int c = blockIdx.x; c < B.nchunks; c += nb) b_orth_scale_body<NT>(B, c, V, w, it0);
+      if (!grid_sync(C, B.ctl)) return;
+    }
   }
   b_sturm_spread(B, nb, B.lm - 1, C.lock);
 }

@@ -139,7 +139,7 @@ struct LanczosFlags {
   int bad;        // a device-side guard fired
   int exhausted;  // beta == 0: the Krylov space is exhausted
   int exh_k;      // size of T when that happened
-  int pad;
+  int fastnorm;   // batched form: this iteration's β was taken in the subtraction pass (no second pass)
 };
 
 template <class TV>
