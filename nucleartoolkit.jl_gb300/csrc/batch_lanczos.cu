@@ -1030,7 +1030,7 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_b_cycle(const BatchDev B, floa
     // the queue counter off the critical path) until the last two tasks per
     // CTA, then singly (a CTA holding kGrab of the last tasks would hold up
     // the end of the phase)
-    constexpr int kGrab = 8;
+    constexpr int kGrab = 4;
     while (true) {
       __syncthreads();
       if (threadIdx.x == 0) {
