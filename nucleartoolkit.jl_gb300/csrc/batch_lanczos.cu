@@ -266,14 +266,7 @@ __device__ __forceinline__ void b_subtract_scale(const BatchDev& B, const BatchP
   }
 }
 
-// β from the norm before the subtraction: with V orthonormal up to its
-// FP32 rounding E, ||w' - Σ h_j v_j||² = ||w'||² - Σ h_j² + hᵀE h, and when
-// Σ h_j² <= kFastNorm ||w'||² the last term is below 1e-15 of the result.
-// Then the subtraction pass also forms β and the next basis vector, and the
-// problem skips the second-pass test and the scaling pass (it cannot need
-// the second pass: ||w''||² >= (1 - kFastNorm) ||w'||²).
-constexpr double kFastNorm = 1e-8;
-
+// β from the norm before the subtraction (kFastNorm, lanczos_dev.cuh).
 // w' -= Σ_j h_j V_j over the chunk (first pass).  Every CTA of the problem
 // takes the same fast/slow decision from the same partial sums; the
 // problem's first chunk records it (fastnorm) with β or exhaustion.

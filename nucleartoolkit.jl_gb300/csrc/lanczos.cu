@@ -177,8 +177,8 @@ __device__ __forceinline__ bool need_second(const double* pdot, const double* pn
 template <class TX>
 __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t ld, int m, double* w,
                                               const double* __restrict__ ph, double* __restrict__ pout, int G,
-                                              double* hs, double* red) {
-  sum_partials_many<kNT>(ph, G, m, hs);
+                                              double* hs, double* red, bool sum_h = true) {
+  if (sum_h) sum_partials_many<kNT>(ph, G, m, hs);  // else hs holds the h_j
   int64_t cb, ce;
   chunk_of(ld, G, cb, ce);
   double nrm = 0.0;
@@ -200,14 +200,65 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
   if (threadIdx.x == 0) pout[blockIdx.x] = s;
 }
 
+// First subtraction.  FP32 basis: when the projections are small
+// (kFastNorm) β comes from the norm before the subtraction and this pass also
+// writes T's β, the scalars and v_{it0+1} (fastnorm = 1; the second-pass and
+// scaling kernels then return at once); every CTA takes the same decision
+// from the same partial sums.
 template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_axpy(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                    const double* __restrict__ pdot, double* __restrict__ pn1, int G,
-                                                   const LanczosFlags* fl) {
+                                                   TX* __restrict__ vnext, double* T, int lm, LanczosScalars* sc,
+                                                   LanczosFlags* fl) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   extern __shared__ double hs[];
   __shared__ double red[kNT / 32];
-  orth_subtract<TX>(V, ld, it0 + 1, w, pdot, pn1, G, hs, red);
+  const int m = it0 + 1;
+  if constexpr (sizeof(TX) == 4) {
+    const double n0 = sum_partials<kNT>(pdot + (int64_t)m * G, G, red);
+    sum_partials_many<kNT>(pdot, G, m, hs);
+    double hsq = 0.0;
+    for (int j = 0; j < m; ++j) hsq = fma(hs[j], hs[j], hsq);
+    const bool fast = n0 > 0.0 && hsq <= kFastNorm * n0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) fl->fastnorm = fast ? 1 : 0;
+    if (fast) {
+      const double beta = sqrt(n0 - hsq);
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        T[(int64_t)it0 * lm + it0 + 1] = beta;
+        T[(int64_t)(it0 + 1) * lm + it0] = beta;
+        sc->beta = beta;
+        sc->inv_beta = 1.0 / beta;
+        fl->second = 0;
+      }
+      const double inv = 1.0 / beta;
+      int64_t cb, ce;
+      chunk_of(ld, G, cb, ce);
+      for (int64_t i = cb + 4 * threadIdx.x; i < ce; i += 4 * kNT) {
+        double t[4];
+        load4(w + i, t);
+        for (int j = 0; j < m; ++j) {
+          double x[4];
+          load4(V + (int64_t)j * ld + i, x);
+          const double hj = hs[j];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) t[u] = fma(-hj, x[u], t[u]);
+        }
+        *reinterpret_cast<float4*>(vnext + i) =
+            make_float4((float)(t[0] * inv), (float)(t[1] * inv), (float)(t[2] * inv), (float)(t[3] * inv));
+      }
+      return;
+    }
+    orth_subtract<TX>(V, ld, m, w, pdot, pn1, G, hs, red, false);
+  } else {
+    orth_subtract<TX>(V, ld, m, w, pdot, pn1, G, hs, red);
+  }
+}
+
+// Whether the first subtraction already finished the iteration (FP32 basis).
+template <class TX>
+__device__ __forceinline__ bool took_fastnorm(const LanczosFlags* fl) {
+  if constexpr (sizeof(TX) == 4) return *(volatile const int*)&fl->fastnorm != 0;
+  return false;
 }
 
 template <class TX>
@@ -215,7 +266,7 @@ __global__ void __launch_bounds__(kNT) k_orth_dot2(const TX* __restrict__ V, int
                                                    const double* __restrict__ w, const double* __restrict__ pdot,
                                                    const double* __restrict__ pn1, double* __restrict__ pdot2,
                                                    int G, const LanczosFlags* fl) {
-  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  if (cta_gate(threadIdx.x == 0 && (stopped(fl) || took_fastnorm<TX>(fl)))) return;
   __shared__ double red[kNT / 32];
   __shared__ double red8[(kNT / 32) * 8];
   const int m = it0 + 1;
@@ -249,7 +300,7 @@ __global__ void __launch_bounds__(kNT) k_orth_axpy2(const TX* __restrict__ V, in
                                                     const double* __restrict__ pn1,
                                                     const double* __restrict__ pdot2, double* __restrict__ pn2,
                                                     int G, const LanczosFlags* fl) {
-  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  if (cta_gate(threadIdx.x == 0 && (stopped(fl) || took_fastnorm<TX>(fl)))) return;
   extern __shared__ double hs[];
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
@@ -265,7 +316,7 @@ __global__ void __launch_bounds__(kNT) k_orth_scale(const double* __restrict__ w
                                                     const double* __restrict__ pn1,
                                                     const double* __restrict__ pn2, int G, int it0, double* T,
                                                     int lm, int64_t len, LanczosScalars* sc, LanczosFlags* fl) {
-  if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
+  if (cta_gate(threadIdx.x == 0 && (stopped(fl) || took_fastnorm<TX>(fl)))) return;
   __shared__ double red[kNT / 32];
   const int m = it0 + 1;
   const bool second = need_second(pdot, pn1, m, G, red);
@@ -1066,7 +1117,8 @@ void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaS
   const int m = it0 + 1;
   const size_t hsh = sizeof(double) * (size_t)m;
   k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl);
-  k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, L.fl);
+  k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, V + (int64_t)(it0 + 1) * L.len, L.T,
+                                         L.lm, L.sc, L.fl);
   k_orth_dot2<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.G, L.fl);
   k_orth_axpy2<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.pn2, L.G, L.fl);
   k_orth_scale<TX><<<L.G, kNT, 0, st>>>(w, V + (int64_t)(it0 + 1) * L.len, L.pdot, L.pn1, L.pn2, L.G, it0, L.T,
