@@ -257,36 +257,94 @@ __global__ void __launch_bounds__(kT) k_2b_fill(const Op2* __restrict__ ops, con
 }
 
 // Per row: stable sort by column, then sum equal columns in list order.
-__global__ void __launch_bounds__(kT) k_2b_merge(int64_t nrow, const int64_t* __restrict__ off,
-                                                 const int* __restrict__ cnt, int* __restrict__ col,
-                                                 double* __restrict__ val, int* __restrict__ mcnt) {
-  for (int64_t g = blockIdx.x * (int64_t)kT + threadIdx.x; g < nrow; g += (int64_t)gridDim.x * kT) {
+// One warp per row: the row's entries go to shared memory, each lane ranks
+// its entries (entries with a smaller column, plus equal columns earlier in
+// the list: a stable order) and scatters them; then each group of equal
+// columns is summed left to right by one lane — the same additions in the
+// same order as the sequential merge.  Rows longer than kMergeMax entries
+// take the sequential merge in global memory (one lane).
+constexpr int kMergeWarps = 8;
+constexpr int kMergeMax = 512;
+size_t merge_smem() { return (size_t)kMergeWarps * kMergeMax * 2 * (sizeof(int) + sizeof(double)); }
+
+__device__ void merge_row_serial(int* c, double* v, int n, int* mout) {
+  for (int a = 1; a < n; ++a) {
+    const int kc = c[a];
+    const double kv = v[a];
+    int p = a - 1;
+    while (p >= 0 && c[p] > kc) {
+      c[p + 1] = c[p];
+      v[p + 1] = v[p];
+      --p;
+    }
+    c[p + 1] = kc;
+    v[p + 1] = kv;
+  }
+  int m = 0;
+  for (int a = 0; a < n; ++a) {
+    if (m > 0 && c[m - 1] == c[a]) {
+      v[m - 1] = __dadd_rn(v[m - 1], v[a]);
+    } else {
+      c[m] = c[a];
+      v[m] = v[a];
+      ++m;
+    }
+  }
+  *mout = m;
+}
+
+__global__ void __launch_bounds__(kMergeWarps * 32) k_2b_merge(int64_t nrow, const int64_t* __restrict__ off,
+                                                               const int* __restrict__ cnt, int* __restrict__ col,
+                                                               double* __restrict__ val, int* __restrict__ mcnt) {
+  extern __shared__ double msm[];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* vin = msm + (size_t)wid * kMergeMax * 2;
+  double* vs = vin + kMergeMax;
+  int* cin = reinterpret_cast<int*>(msm + (size_t)kMergeWarps * kMergeMax * 2) + (size_t)wid * kMergeMax * 2;
+  int* cs = cin + kMergeMax;
+  const unsigned full = 0xffffffffu;
+  for (int64_t g = blockIdx.x * (int64_t)kMergeWarps + wid; g < nrow; g += (int64_t)gridDim.x * kMergeWarps) {
     int* c = col + off[g];
     double* v = val + off[g];
     const int n = cnt[g];
-    for (int a = 1; a < n; ++a) {
-      const int kc = c[a];
-      const double kv = v[a];
-      int p = a - 1;
-      while (p >= 0 && c[p] > kc) {
-        c[p + 1] = c[p];
-        v[p + 1] = v[p];
-        --p;
-      }
-      c[p + 1] = kc;
-      v[p + 1] = kv;
+    if (n > kMergeMax) {
+      if (lane == 0) merge_row_serial(c, v, n, mcnt + g);
+      __syncwarp();
+      continue;
     }
-    int m = 0;
-    for (int a = 0; a < n; ++a) {
-      if (m > 0 && c[m - 1] == c[a]) {
-        v[m - 1] = __dadd_rn(v[m - 1], v[a]);
-      } else {
-        c[m] = c[a];
-        v[m] = v[a];
-        ++m;
-      }
+    for (int a = lane; a < n; a += 32) {
+      cin[a] = c[a];
+      vin[a] = v[a];
     }
-    mcnt[g] = m;
+    __syncwarp();
+    for (int a = lane; a < n; a += 32) {
+      const int ca = cin[a];
+      int r = 0;
+      for (int b = 0; b < n; ++b) {
+        const int cb = cin[b];
+        r += (cb < ca || (cb == ca && b < a)) ? 1 : 0;
+      }
+      cs[r] = ca;
+      vs[r] = vin[a];
+    }
+    __syncwarp();
+    // groups of equal columns: the lane at a group's first entry sums it
+    int base = 0;
+    for (int a0 = 0; a0 < n; a0 += 32) {
+      const int a = a0 + lane;
+      const bool start = a < n && (a == 0 || cs[a] != cs[a - 1]);
+      const unsigned bal = __ballot_sync(full, start);
+      if (start) {
+        const int m = base + __popc(bal & ((1u << lane) - 1u));
+        double s = vs[a];
+        for (int e = a + 1; e < n && cs[e] == cs[a]; ++e) s = __dadd_rn(s, vs[e]);
+        c[m] = cs[a];
+        v[m] = s;
+      }
+      base += __popc(bal);
+    }
+    if (lane == 0) mcnt[g] = base;
+    __syncwarp();
   }
 }
 
@@ -487,7 +545,12 @@ void build_2b_device(DeviceArena& A, const std::vector<Op2>& ops, const uint64_t
   int* mcnt = A.alloc<int>(nrow);
   int64_t* moff = A.alloc<int64_t>(nrow);
   k_2b_fill<<<gw, kT, 0, st>>>(d_ops, d_conj, nops, d_bits, d_start, nb, nrow, off, craw, vraw);
-  k_2b_merge<<<grid_for(nrow), kT, 0, st>>>(nrow, off, cnt, craw, vraw, mcnt);
+  {
+    SMGPU_CUDA_TRY(cudaFuncSetAttribute(k_2b_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)merge_smem()));
+    int64_t gm = (nrow + kMergeWarps - 1) / kMergeWarps;
+    if (gm > 152 * 8) gm = 152 * 8;
+    k_2b_merge<<<(int)(gm < 1 ? 1 : gm), kMergeWarps * 32, merge_smem(), st>>>(nrow, off, cnt, craw, vraw, mcnt);
+  }
   const int64_t total = scan_exclusive<int>(A, mcnt, nrow, moff, st);
   if (total >= (1ll << 31)) throw SetupError{SMGPU_ERR_LIMIT, "two-body jump table too large"};
   int* d_col = A.alloc<int>(total);

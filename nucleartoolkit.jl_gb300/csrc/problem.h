@@ -1,6 +1,7 @@
 // The problem handle behind the C ABI (shared by capi.cu and multi.cu).
 #pragma once
 #include <algorithm>
+#include <new>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -154,71 +155,100 @@ struct smgpu_problem {
     nnmax_raw = 0;
     for (int b = 0; b < T.nb; ++b) nnmax_raw = std::max(nnmax_raw, T.nn[b]);
     if (T.len_pad >= ((int64_t)1 << 31)) return;
+    // the links are independent: built in parallel into per-link arrays,
+    // then concatenated in link order (the same tables as a serial build)
+    struct LinkPush {
+      std::vector<uint32_t> ell;  // [k][position]
+      std::vector<int> info;      // per position: source column | count << 16
+      int64_t y = 0;              // slots of the link
+    };
+    std::vector<LinkPush> lp(nl);
+    int bad = 0, nomem = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : bad, nomem)
+    for (long lii = 0; lii < (long)nl; ++lii) {
+      if (bad || nomem) continue;
+      try {
+        const size_t li = (size_t)lii;
+        const auto& L = T.links[li];
+        const int nno = T.nn[L.b], nns = T.nn[L.s];
+        const int64_t* np_ = T.npn_ptr.data() + L.nptr_off;
+        std::vector<int64_t> cnt(nns + 1, 0);
+        int64_t kw = 0;
+        for (int n = 0; n < nno; ++n) {
+          kw = std::max(kw, np_[n + 1] - np_[n]);
+          for (int64_t g = np_[n]; g < np_[n + 1]; ++g) cnt[(T.npn_ent[g] >> 14) + 1]++;
+        }
+        if (kw * nno > 65536 || L.nB >= (1 << 15)) {
+          bad = 1;
+          continue;
+        }
+        lp[li].y = kw * nno;
+        // source columns in descending order of their entry counts within
+        // windows of 128 consecutive columns: the lanes of a warp carry lists
+        // of about the same length, and a warp's loads of v stay inside four
+        // 128-byte lines
+        std::vector<int> order(nns);
+        for (int n = 0; n < nns; ++n) order[n] = n;
+        for (int w0 = 0; w0 < nns; w0 += 128) {
+          std::stable_sort(order.begin() + w0, order.begin() + std::min(nns, w0 + 128),
+                           [&](int x, int y) { return cnt[x + 1] > cnt[y + 1]; });
+          // full windows: the four 32-column groups (longest first) rotate over
+          // the warps from window to window, so no warp always gets the longest
+          if (w0 + 128 <= nns) {
+            const int rot = (w0 / 128) % 4;
+            std::vector<int> win(order.begin() + w0, order.begin() + w0 + 128);
+            for (int g = 0; g < 4; ++g)
+              for (int l = 0; l < 32; ++l) order[w0 + ((g + rot) % 4) * 32 + l] = win[g * 32 + l];
+          }
+        }
+        std::vector<int64_t> start(nns + 1, 0);  // entry offset of each source column (position order)
+        std::vector<int> posof(nns);
+        for (int q = 0; q < nns; ++q) {
+          posof[order[q]] = q;
+          start[q + 1] = start[q] + cnt[order[q] + 1];
+        }
+        std::vector<uint32_t> pent(start[nns]);
+        std::vector<int64_t> pos(start.begin(), start.end() - 1);
+        for (int n = 0; n < nno; ++n)
+          for (int64_t g = np_[n]; g < np_[n + 1]; ++g) {
+            const uint32_t e = T.npn_ent[g];
+            const uint32_t src = e >> 14, ib = (e >> 1) & 0x1fffu, sg = e & 1u;
+            const uint32_t slot = (uint32_t)((g - np_[n]) * nno + n);
+            pent[pos[posof[src]]++] = slot | (ib << 16) | (sg << 31);
+          }
+        // each list by operator index: lanes at the same position then tend to
+        // read the same or neighbouring coefficient rows (fewer bank conflicts)
+        for (int q = 0; q < nns; ++q)
+          std::sort(pent.begin() + start[q], pent.begin() + start[q + 1],
+                    [](uint32_t x, uint32_t y) { return ((x >> 16) & 0x7fffu) < ((y >> 16) & 0x7fffu); });
+        // ELL [k][position] and the per-position descriptors
+        int64_t kwp = 0;
+        for (int q = 0; q < nns; ++q) kwp = std::max(kwp, start[q + 1] - start[q]);
+        if (nns >= 65536 || kwp >= 32768) {
+          bad = 1;
+          continue;
+        }
+        lp[li].ell.assign((size_t)kwp * nns, 0u);
+        lp[li].info.resize(nns);
+        for (int q = 0; q < nns; ++q) {
+          const int64_t c = start[q + 1] - start[q];
+          lp[li].info[q] = order[q] | (int)(c << 16);
+          for (int64_t k = 0; k < c; ++k) lp[li].ell[k * nns + q] = pent[start[q] + k];
+        }
+      } catch (const std::bad_alloc&) {
+        nomem = 1;
+      }
+    }
+    if (nomem) throw std::bad_alloc();
+    if (bad) return;
     for (size_t li = 0; li < nl; ++li) {
-      const auto& L = T.links[li];
-      const int nno = T.nn[L.b], nns = T.nn[L.s];
-      const int64_t* np_ = T.npn_ptr.data() + L.nptr_off;
-      std::vector<int64_t> cnt(nns + 1, 0);
-      int64_t kw = 0;
-      for (int n = 0; n < nno; ++n) {
-        kw = std::max(kw, np_[n + 1] - np_[n]);
-        for (int64_t g = np_[n]; g < np_[n + 1]; ++g) cnt[(T.npn_ent[g] >> 14) + 1]++;
-      }
-      if (kw * nno > 65536) return;
-      ymax = std::max(ymax, kw * nno);
-      nbmax = std::max(nbmax, L.nB);
-      if (L.nB >= (1 << 15)) return;
-      // source columns in descending order of their entry counts within
-      // windows of 128 consecutive columns: the lanes of a warp carry lists
-      // of about the same length, and a warp's loads of v stay inside four
-      // 128-byte lines
-      std::vector<int> order(nns);
-      for (int n = 0; n < nns; ++n) order[n] = n;
-      for (int w0 = 0; w0 < nns; w0 += 128) {
-        std::stable_sort(order.begin() + w0, order.begin() + std::min(nns, w0 + 128),
-                         [&](int x, int y) { return cnt[x + 1] > cnt[y + 1]; });
-        // full windows: the four 32-column groups (longest first) rotate over
-        // the warps from window to window, so no warp always gets the longest
-        if (w0 + 128 <= nns) {
-          const int rot = (w0 / 128) % 4;
-          std::vector<int> win(order.begin() + w0, order.begin() + w0 + 128);
-          for (int g = 0; g < 4; ++g)
-            for (int l = 0; l < 32; ++l) order[w0 + ((g + rot) % 4) * 32 + l] = win[g * 32 + l];
-        }
-      }
-      std::vector<int64_t> start(nns + 1, 0);  // entry offset of each source column (position order)
-      std::vector<int> posof(nns);
-      for (int i = 0; i < nns; ++i) {
-        posof[order[i]] = i;
-        start[i + 1] = start[i] + cnt[order[i] + 1];
-      }
-      const int64_t base = 0;
-      std::vector<uint32_t> pent(start[nns]);
-      std::vector<int64_t> pos(start.begin(), start.end() - 1);
-      for (int n = 0; n < nno; ++n)
-        for (int64_t g = np_[n]; g < np_[n + 1]; ++g) {
-          const uint32_t e = T.npn_ent[g];
-          const uint32_t src = e >> 14, ib = (e >> 1) & 0x1fffu, sg = e & 1u;
-          const uint32_t slot = (uint32_t)((g - np_[n]) * nno + n);
-          pent[base + pos[posof[src]]++] = slot | (ib << 16) | (sg << 31);
-        }
-      // each list by operator index: lanes at the same position then tend to
-      // read the same or neighbouring coefficient rows (fewer bank conflicts)
-      for (int i = 0; i < nns; ++i)
-        std::sort(pent.begin() + base + start[i], pent.begin() + base + start[i + 1],
-                  [](uint32_t x, uint32_t y) { return ((x >> 16) & 0x7fffu) < ((y >> 16) & 0x7fffu); });
-      // ELL [k][position] and the per-position descriptors
-      int64_t kwp = 0;
-      for (int i = 0; i < nns; ++i) kwp = std::max(kwp, start[i + 1] - start[i]);
-      if (nns >= 65536 || kwp >= 32768) return;
+      ymax = std::max(ymax, lp[li].y);
+      nbmax = std::max(nbmax, T.links[li].nB);
       poff[li] = (int64_t)pell.size();
       pioff[li] = (int64_t)pinfo.size();
-      pell.resize(pell.size() + (size_t)kwp * nns, 0u);
-      for (int i = 0; i < nns; ++i) {
-        const int64_t c = start[i + 1] - start[i];
-        pinfo.push_back(order[i] | (int)(c << 16));
-        for (int64_t k = 0; k < c; ++k) pell[poff[li] + k * nns + i] = pent[start[i] + k];
-      }
+      pell.insert(pell.end(), lp[li].ell.begin(), lp[li].ell.end());
+      pinfo.insert(pinfo.end(), lp[li].info.begin(), lp[li].info.end());
+      std::vector<uint32_t>().swap(lp[li].ell);
     }
     for (size_t k = 0; k + 1 < rl.size(); ++k) kmax = std::max(kmax, rl[k + 1] - rl[k]);
     // nn lists as ELL [k][n] per block
