@@ -14,18 +14,38 @@
 
 namespace smgpu {
 
+// Device allocations freed together.  Small requests are carved (256-byte
+// aligned) from slabs of doubling size, 1 MB .. 64 MB, so building a
+// problem's few dozen tables costs a handful of cudaMalloc calls; a request
+// that does not fit the next slab gets its own allocation.
 struct DeviceArena {
   std::vector<void*> ptrs;
   size_t bytes = 0;
-  template <class T>
-  T* alloc(size_t n) {
+  char* slab = nullptr;
+  size_t slab_left = 0, next_slab = (size_t)1 << 20;
+  static constexpr size_t kAlign = 256, kMaxSlab = (size_t)64 << 20;
+  void* raw(size_t b) {
     void* p = nullptr;
-    size_t b = sizeof(T) * (n > 0 ? n : 1);
     cudaError_t e = cudaMalloc(&p, b);
     if (e != cudaSuccess) throw CudaError{e, "cudaMalloc", __FILE__, __LINE__};
     ptrs.push_back(p);
+    return p;
+  }
+  template <class T>
+  T* alloc(size_t n) {
+    size_t b = sizeof(T) * (n > 0 ? n : 1);
+    b = (b + kAlign - 1) & ~(kAlign - 1);
     bytes += b;
-    return (T*)p;
+    if (b > slab_left) {
+      if (b > next_slab) return (T*)raw(b);
+      slab = (char*)raw(next_slab);
+      slab_left = next_slab;
+      next_slab = std::min(next_slab * 2, kMaxSlab);
+    }
+    T* p = (T*)slab;
+    slab += b;
+    slab_left -= b;
+    return p;
   }
   template <class T>
   T* upload(const std::vector<T>& v) {
@@ -37,6 +57,9 @@ struct DeviceArena {
     for (void* p : ptrs) cudaFree(p);
     ptrs.clear();
     bytes = 0;
+    slab = nullptr;
+    slab_left = 0;
+    next_slab = (size_t)1 << 20;
   }
 };
 
@@ -161,12 +184,12 @@ struct smgpu_problem {
       std::vector<uint32_t> ell;  // [k][position]
       std::vector<int> info;      // per position: source column | count << 16
       int64_t y = 0;              // slots of the link
+      int bad = 0;                // a packing limit is exceeded
+      int nomem = 0;
     };
     std::vector<LinkPush> lp(nl);
-    int bad = 0, nomem = 0;
-#pragma omp parallel for schedule(dynamic, 1) reduction(max : bad, nomem)
+#pragma omp parallel for schedule(dynamic, 1)
     for (long lii = 0; lii < (long)nl; ++lii) {
-      if (bad || nomem) continue;
       try {
         const size_t li = (size_t)lii;
         const auto& L = T.links[li];
@@ -179,7 +202,7 @@ struct smgpu_problem {
           for (int64_t g = np_[n]; g < np_[n + 1]; ++g) cnt[(T.npn_ent[g] >> 14) + 1]++;
         }
         if (kw * nno > 65536 || L.nB >= (1 << 15)) {
-          bad = 1;
+          lp[li].bad = 1;
           continue;
         }
         lp[li].y = kw * nno;
@@ -225,7 +248,7 @@ struct smgpu_problem {
         int64_t kwp = 0;
         for (int q = 0; q < nns; ++q) kwp = std::max(kwp, start[q + 1] - start[q]);
         if (nns >= 65536 || kwp >= 32768) {
-          bad = 1;
+          lp[li].bad = 1;
           continue;
         }
         lp[li].ell.assign((size_t)kwp * nns, 0u);
@@ -236,11 +259,17 @@ struct smgpu_problem {
           for (int64_t k = 0; k < c; ++k) lp[li].ell[k * nns + q] = pent[start[q] + k];
         }
       } catch (const std::bad_alloc&) {
-        nomem = 1;
+        lp[(size_t)lii].nomem = 1;
       }
     }
-    if (nomem) throw std::bad_alloc();
-    if (bad) return;
+    for (const LinkPush& x : lp)
+      if (x.nomem) throw std::bad_alloc();
+    for (const LinkPush& x : lp)
+      if (x.bad) return;
+    // every link's lists must be present before the kernels index them
+    for (size_t li = 0; li < nl; ++li)
+      if (lp[li].info.size() != (size_t)T.nn[T.links[li].s])
+        throw SetupError{SMGPU_ERR_LIMIT, "staged push lists incomplete"};
     for (size_t li = 0; li < nl; ++li) {
       ymax = std::max(ymax, lp[li].y);
       nbmax = std::max(nbmax, T.links[li].nB);
