@@ -281,6 +281,7 @@ struct BatchSolve {
     B.num_ev = num_ev;
     B.nh = 3;
     B.tol = tol;
+    B.fastnorm = fastnorm_threshold();
     B.nslots = H->ntasks();
     const int np = H->nprob, nch = B.nchunks;
     const int NP = ls * (ls + 1) / 2 + ls;

@@ -63,6 +63,7 @@ struct BatchCycle {
 struct BatchDev {
   int nprob, lm, ls, num_ev, nh;
   double tol;
+  double fastnorm;    // β from the norm before the subtraction when Σh² <= fastnorm ||w'||²
   int nchunks;        // chunks of the batch vector
   int nslots;         // H·v tasks
   int64_t LEN;        // batch vector length (slot stride of V and U)

@@ -266,7 +266,7 @@ __device__ __forceinline__ void b_subtract_scale(const BatchDev& B, const BatchP
   }
 }
 
-// β from the norm before the subtraction (kFastNorm, lanczos_dev.cuh).
+// β from the norm before the subtraction (B.fastnorm, normally kFastNorm, lanczos.cuh).
 // w' -= Σ_j h_j V_j over the chunk (first pass).  Every CTA of the problem
 // takes the same fast/slow decision from the same partial sums; the
 // problem's first chunk records it (fastnorm) with β or exhaustion.
@@ -283,7 +283,7 @@ __device__ void b_orth_axpy_body(const BatchDev& B, const int c, float* V, doubl
   sum_many_strided<NT>(B.pdot + P.chunk0, B.nchunks, P.nchunks, m, hs);
   double hsq = 0.0;
   for (int j = 0; j < m; ++j) hsq = fma(hs[j], hs[j], hsq);
-  const bool fast = n0 > 0.0 && hsq <= kFastNorm * n0;
+  const bool fast = n0 > 0.0 && hsq <= B.fastnorm * n0;
   if (!fast) {
     if (c == P.chunk0 && threadIdx.x == 0) f->fastnorm = 0;
     b_subtract<NT>(B, P, c, ch, V, w, m, B.pdot, B.pn1, hs, red, false);

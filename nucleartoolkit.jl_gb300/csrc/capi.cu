@@ -316,6 +316,7 @@ struct Solve {
     L.sc = A.alloc<LanczosScalars>(1);
     L.fl = A.alloc<LanczosFlags>(1);
     L.alpha_df = dfs() ? 1 : 0;  // the double-float solve runs the double-float H·v epilogue
+    L.fastnorm = fastnorm_threshold();
     SMGPU_CUDA_TRY(cudaMemsetAsync(V, 0, sizeof(TX) * (size_t)lm * L.len, P->st));
     SMGPU_CUDA_TRY(cudaMemsetAsync(w, 0, sizeof(double) * L.len, P->st));
     // the padding slots of the double-float residual are never written by H·v

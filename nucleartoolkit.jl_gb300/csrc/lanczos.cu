@@ -201,7 +201,7 @@ __device__ __forceinline__ void orth_subtract(const TX* __restrict__ V, int64_t 
 }
 
 // First subtraction.  FP32 basis: when the projections are small
-// (kFastNorm) β comes from the norm before the subtraction and this pass also
+// (L.fastnorm, normally kFastNorm) β comes from the norm before the subtraction and this pass also
 // writes T's β, the scalars and v_{it0+1} (fastnorm = 1; the second-pass and
 // scaling kernels then return at once); every CTA takes the same decision
 // from the same partial sums.
@@ -209,7 +209,7 @@ template <class TX>
 __global__ void __launch_bounds__(kNT) k_orth_axpy(const TX* __restrict__ V, int64_t ld, int it0, double* w,
                                                    const double* __restrict__ pdot, double* __restrict__ pn1, int G,
                                                    TX* __restrict__ vnext, double* T, int lm, LanczosScalars* sc,
-                                                   LanczosFlags* fl) {
+                                                   LanczosFlags* fl, double fastnorm) {
   if (cta_gate(threadIdx.x == 0 && stopped(fl))) return;
   extern __shared__ double hs[];
   __shared__ double red[kNT / 32];
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kNT) k_orth_axpy(const TX* __restrict__ V, int
     sum_partials_many<kNT>(pdot, G, m, hs);
     double hsq = 0.0;
     for (int j = 0; j < m; ++j) hsq = fma(hs[j], hs[j], hsq);
-    const bool fast = n0 > 0.0 && hsq <= kFastNorm * n0;
+    const bool fast = n0 > 0.0 && hsq <= fastnorm * n0;
     if (blockIdx.x == 0 && threadIdx.x == 0) fl->fastnorm = fast ? 1 : 0;
     if (fast) {
       const double beta = sqrt(n0 - hsq);
@@ -1118,7 +1118,7 @@ void launch_orth_iteration(const LanczosDev& L, TX* V, double* w, int it0, cudaS
   const size_t hsh = sizeof(double) * (size_t)m;
   k_orth_dot<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.alpha_part, L.nalpha, L.pdot, L.G, L.fl);
   k_orth_axpy<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.G, V + (int64_t)(it0 + 1) * L.len, L.T,
-                                         L.lm, L.sc, L.fl);
+                                         L.lm, L.sc, L.fl, L.fastnorm);
   k_orth_dot2<TX><<<L.G, kNT, 0, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.G, L.fl);
   k_orth_axpy2<TX><<<L.G, kNT, hsh, st>>>(V, L.len, it0, w, L.pdot, L.pn1, L.pdot2, L.pn2, L.G, L.fl);
   k_orth_scale<TX><<<L.G, kNT, 0, st>>>(w, V + (int64_t)(it0 + 1) * L.len, L.pdot, L.pn1, L.pn2, L.G, it0, L.T,

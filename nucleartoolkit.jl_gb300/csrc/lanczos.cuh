@@ -3,6 +3,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "device.cuh"
 
 namespace smgpu {
@@ -12,6 +14,21 @@ enum ReduceMode {
   RED_STORE = 0,    // out[j] = sum_j
   RED_INVNORM = 5   // out[j] = 1/sqrt(sum_j)
 };
+
+// β from the norm before the subtraction (FP32-mixed forms): with the FP32
+// basis V orthonormal up to its rounding E, ||w' - Σ h_j v_j||² = ||w'||² -
+// Σ h_j² + hᵀE h, and when Σ h_j² <= kFastNorm ||w'||² the last term is below
+// 1e-15 of the result.  Then the subtraction pass also forms β and the next
+// basis vector, and the second-pass test and the scaling pass are skipped
+// (no second pass can be needed: ||w''||² >= (1 - kFastNorm) ||w'||²).
+constexpr double kFastNorm = 1e-8;
+// The threshold a solve uses: kFastNorm, or -1 (never: every iteration takes
+// the norm after the subtraction) with SMGPU_FASTNORM=0, which the tests use
+// to cover both paths.
+inline double fastnorm_threshold() {
+  const char* e = std::getenv("SMGPU_FASTNORM");
+  return (e && e[0] == '0') ? -1.0 : kFastNorm;
+}
 
 struct LanczosDev {
   int G;                // CTAs of the streaming reduction kernels
@@ -40,6 +57,7 @@ struct LanczosDev {
   LanczosScalars* sc;
   LanczosFlags* fl;
   int alpha_df;         // 1: alpha_part holds double-float (hi, lo) float pairs (FP32-mixed H·v)
+  double fastnorm;      // β from the norm before the subtraction when Σh² <= fastnorm ||w'||² (FP32 basis)
 };
 
 void launch_start_vector(const DevTables& t, uint64_t seed, double* w, cudaStream_t st);

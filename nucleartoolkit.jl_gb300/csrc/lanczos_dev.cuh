@@ -11,14 +11,6 @@ namespace dev {
 
 constexpr int kNT = 256;  // threads of the streaming kernels
 
-// β from the norm before the subtraction (FP32-mixed forms): with the FP32
-// basis V orthonormal up to its rounding E, ||w' - Σ h_j v_j||² = ||w'||² -
-// Σ h_j² + hᵀE h, and when Σ h_j² <= kFastNorm ||w'||² the last term is below
-// 1e-15 of the result.  Then the subtraction pass also forms β and the next
-// basis vector, and the second-pass test and the scaling pass are skipped
-// (no second pass can be needed: ||w''||² >= (1 - kFastNorm) ||w'||²).
-constexpr double kFastNorm = 1e-8;
-
 // (volatile: the persistent batch kernel reads flags that other CTAs of the
 // same launch set, so they must come from L2, not from a line in L1)
 __device__ __forceinline__ bool stopped(const LanczosFlags* fl) {

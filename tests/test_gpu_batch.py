@@ -187,6 +187,27 @@ def test_batch_persistent_cycle_every_shape(lib, mixed_batch, monkeypatch):
         assert rp["kernel_launches"] * 5 < rg["kernel_launches"], cand
 
 
+def test_batch_beta_from_norm_before_subtraction_both_paths(lib, mixed_batch, monkeypatch):
+    """The batched solve takes β from the norm before the subtraction when a
+    problem's projections are small; SMGPU_FASTNORM=0 forces the norm after
+    the subtraction (and the scaling pass) in every iteration.  Both paths,
+    persistent and graph form, against the oracle."""
+    probs = mixed_batch[:8]
+    refs = [_oracle(snt, nuc).trl(5, lm=30, ls=15, tol=1e-8)["evals"] for snt, nuc in probs]
+    for mode in ("1", "0"):
+        monkeypatch.setenv("SMGPU_FASTNORM", mode)
+        G = _batch(probs)
+        for persist in ("1", "0"):
+            monkeypatch.setenv("SMGPU_BATCH_PERSIST", persist)
+            r = G.solve(5, lm=30, ls=15, tol=1e-8)
+            assert r["converged"] and r["problem_converged"].all(), (mode, persist)
+            for p, ref in enumerate(refs):
+                nev = len(ref)
+                assert np.abs(r["evals"][p, :nev] - ref).max() <= EIG_MIXED_ATOL, (mode, persist, p)
+    monkeypatch.delenv("SMGPU_BATCH_PERSIST")
+    monkeypatch.delenv("SMGPU_FASTNORM")
+
+
 def test_batch_persistent_barrier_wait_limit(lib, mixed_batch, monkeypatch):
     """Every grid-barrier wait of the persistent kernel is bounded: with a
     wait limit of one poll the kernel gives up at its first barrier, the solve

@@ -245,6 +245,26 @@ def test_eigenvalues_vs_oracle(lib, snt_dir, case, nev, lm, ls):
         assert np.abs(rm["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, prec
 
 
+@pytest.mark.parametrize("case", ["sd4p4n", "usdb_Na21"])
+def test_mixed_beta_from_norm_before_subtraction_both_paths(lib, snt_dir, case, monkeypatch):
+    """The FP32-mixed solve with FP64 re-orthogonalisation takes β from the
+    norm before the subtraction when the projections are small, and the norm
+    after the subtraction otherwise; SMGPU_FASTNORM=0 forces the latter in
+    every iteration.  Both paths against the oracle, with the same iteration
+    count."""
+    snt, nuc = _cases(snt_dir)[case]
+    ro = _oracle(snt, nuc).trl(5, lm=30, ls=15, tol=1e-8)
+    res = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("SMGPU_FASTNORM", mode)
+        r = _gpu(snt, nuc, 1).solve(5, lm=30, ls=15, tol=1e-8)
+        assert r["converged"], mode
+        assert np.abs(r["evals"] - ro["evals"]).max() <= EIG_MIXED_ATOL, mode
+        res[mode] = r
+    assert res["1"]["n_matvec"] == res["0"]["n_matvec"]
+    assert np.abs(res["1"]["evals"] - res["0"]["evals"]).max() <= 1e-6
+
+
 @pytest.mark.parametrize("prec", [1, 2])
 def test_ritz_vectors_mixed(lib, snt_dir, prec):
     """Ritz vectors of both FP32-mixed forms (FP64 or double-float Lanczos
