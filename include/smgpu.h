@@ -239,7 +239,10 @@ int smgpu_l2_read_bandwidth(long long bytes, int reps, double* gbs_out);
  * launch shapes timed when the handle was created (0 when the shape came
  * from the cache or SMGPU_AUTOTUNE=0); for the first min(max, *count) of
  * them, shapes[4k..4k+3] = (threads per CTA, rows per CTA, minimum CTAs per
- * SM, kernel form: 0 row-tile, 1 staged pn) and ms[k] = mean ms per launch. */
+ * SM, kernel form: 0 row-tile, 1 staged pn) and ms[k] = mean ms per launch
+ * (for a shape dropped because its warm-up launch took more than twice the
+ * best mean so far: that warm-up launch's time).  Staged shapes are timed
+ * first. */
 int smgpu_tune_report(const smgpu_problem* h, int max, int* shapes, double* ms, int* count);
 
 /* Structural statistics of the factorised H (12 entries): [updates per H·v

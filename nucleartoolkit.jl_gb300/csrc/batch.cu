@@ -224,13 +224,21 @@ void smgpu_batch::autotune() {
     SMGPU_CUDA_TRY(cudaEventCreate(&a));
     SMGPU_CUDA_TRY(cudaEventCreate(&b));
     int nc = 0;
-    hv_batch_candidates(&nc);
-    int best = cand;
+    const BatchHvConfig* cands = hv_batch_candidates(&nc);
+    // staged shapes first (usually the fastest); a shape whose warm-up launch
+    // takes more than twice the best mean so far is dropped untimed
+    std::vector<int> order;
+    for (int c = 0; c < nc; ++c)
+      if (cands[c].staged) order.push_back(c);
+    for (int c = 0; c < nc; ++c)
+      if (!cands[c].staged) order.push_back(c);
+    int best = -1;
     float best_ms = 1e30f;
-    for (int c = 0; c < nc; ++c) {
+    for (int c : order) {
       if (!fits(c)) continue;
       set_cand(c);
       float total = 0.f;
+      bool dropped = false;
       for (int rep = 0; rep < 3; ++rep) {
         SMGPU_CUDA_TRY(cudaEventRecord(a, st));
         hv(d_v, d_w, BatchEpi{}, st);
@@ -239,14 +247,21 @@ void smgpu_batch::autotune() {
         float ms = 0.f;
         SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
         if (rep > 0) total += ms;
+        if (rep == 0 && best >= 0 && ms > 2.f * (best_ms / 2)) {
+          if (c < 16) tune_ms[c] = ms;
+          dropped = true;
+          break;
+        }
       }
       SMGPU_CUDA_TRY(cudaGetLastError());
+      if (dropped) continue;
       if (c < 16) tune_ms[c] = total / 2;
       if (total < best_ms) {
         best_ms = total;
         best = c;
       }
     }
+    if (best < 0) best = cand;
     set_cand(best);
   } catch (...) {
     if (a) cudaEventDestroy(a);

@@ -130,11 +130,13 @@ void smgpu_problem::autotune() {
     int nc0 = 0, ns = 0;
     const HvConfig* c0 = hv_candidates(&nc0);
     const HvConfig* cs = hv_staged_candidates(&ns);
+    // staged shapes first: usually the fastest, so the row-tile shapes
+    // behind them are mostly dropped after their first launch (below)
     std::vector<HvConfig> cand;
-    if (form != "staged" || precision == SMGPU_FP64) cand.assign(c0, c0 + nc0);
     if (precision != SMGPU_FP64 && form != "tile")
       for (int k = 0; k < ns; ++k)
         if (hv_staged_fits(cs[k], tt, nnmax_raw)) cand.push_back(cs[k]);
+    if (form != "staged" || precision == SMGPU_FP64) cand.insert(cand.end(), c0, c0 + nc0);
     if (cand.empty()) cand.assign(c0, c0 + nc0);  // the staged form does not fit this problem
     const int nc = (int)cand.size();
     tune_shapes = cand;
@@ -144,6 +146,7 @@ void smgpu_problem::autotune() {
     for (int c = 0; c < nc; ++c) {
       set_config(cand[c].nt, cand[c].rows, cand[c].minb, cand[c].staged);
       float total = 0.f;
+      bool dropped = false;
       for (int rep = 0; rep < 3; ++rep) {
         SMGPU_CUDA_TRY(cudaEventRecord(a, st));
         if (precision == SMGPU_FP64) hv((const double*)d_v, d_w, HvEpilogue<double>{}, st);
@@ -153,8 +156,16 @@ void smgpu_problem::autotune() {
         float ms = 0.f;
         SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
         if (rep > 0) total += ms;  // first launch is the warm-up
+        // a shape whose warm-up launch already takes more than twice the
+        // best time so far cannot win: dropped without the timed launches
+        if (rep == 0 && best >= 0 && ms > 2.f * (best_ms / 2)) {
+          tune_ms[c] = ms;
+          dropped = true;
+          break;
+        }
       }
       SMGPU_CUDA_TRY(cudaGetLastError());
+      if (dropped) continue;
       tune_ms[c] = total / 2;
       if (total < best_ms) {
         best_ms = total;

@@ -178,6 +178,7 @@ void smgpu_multi::autotune() {
     for (int c = 0; c < nc; ++c) {
       cand = c;
       float total = 0.f;
+      bool dropped = false;
       for (int rep = 0; rep < 3; ++rep) {
         SMGPU_CUDA_TRY(cudaEventRecord(a, base.st));
         hv(d_v, d_w, MultiEpilogue{}, base.st);
@@ -186,8 +187,15 @@ void smgpu_multi::autotune() {
         float ms = 0.f;
         SMGPU_CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
         if (rep > 0) total += ms;
+        // a warm-up launch over twice the best mean so far: dropped untimed
+        if (rep == 0 && best_ms < 1e29f && ms > 2.f * (best_ms / 2)) {
+          if (c < 16) tune_ms[c] = ms;
+          dropped = true;
+          break;
+        }
       }
       SMGPU_CUDA_TRY(cudaGetLastError());
+      if (dropped) continue;
       if (c < 16) tune_ms[c] = total / 2;
       if (total < best_ms) {
         best_ms = total;
