@@ -383,39 +383,30 @@ __device__ inline void jacobi_eig(const double* __restrict__ T, int ldt, int n, 
         pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = s;
       }
       __syncthreads();
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        int k = idx / n, i = idx % n;
+      // the rotations applied to A's columns p, q and, independently, to Z
+      for (int idx = tid; idx < 2 * npair * n; idx += NT) {
+        const bool onz = idx >= npair * n;
+        double* M = onz ? Z_ : A_;
+        const int id2 = onz ? idx - npair * n : idx;
+        int k = id2 / n, i = id2 % n;
         if (ss[k] == 0.0) continue;
         int p = pp[k], q = qq[k];
         double c = cc[k], s = ss[k];
-        double aip = A_[(int64_t)p * n + i], aiq = A_[(int64_t)q * n + i];
-        A_[(int64_t)p * n + i] = c * aip - s * aiq;
-        A_[(int64_t)q * n + i] = s * aip + c * aiq;
+        double aip = M[(int64_t)p * n + i], aiq = M[(int64_t)q * n + i];
+        M[(int64_t)p * n + i] = c * aip - s * aiq;
+        M[(int64_t)q * n + i] = s * aip + c * aiq;
       }
       __syncthreads();
+      // then to A's rows p, q; the pair's own off-diagonal entries, which
+      // the rotation annihilates, are written as exact zeros
       for (int idx = tid; idx < npair * n; idx += NT) {
         int k = idx / n, j = idx % n;
         if (ss[k] == 0.0) continue;
         int p = pp[k], q = qq[k];
         double c = cc[k], s = ss[k];
         double apj = A_[(int64_t)j * n + p], aqj = A_[(int64_t)j * n + q];
-        A_[(int64_t)j * n + p] = c * apj - s * aqj;
-        A_[(int64_t)j * n + q] = s * apj + c * aqj;
-      }
-      __syncthreads();
-      for (int k = tid; k < npair; k += NT)
-        if (ss[k] != 0.0) {
-          A_[(int64_t)qq[k] * n + pp[k]] = 0.0;
-          A_[(int64_t)pp[k] * n + qq[k]] = 0.0;
-        }
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        int k = idx / n, i = idx % n;
-        if (ss[k] == 0.0) continue;
-        int p = pp[k], q = qq[k];
-        double c = cc[k], s = ss[k];
-        double zip = Z_[(int64_t)p * n + i], ziq = Z_[(int64_t)q * n + i];
-        Z_[(int64_t)p * n + i] = c * zip - s * ziq;
-        Z_[(int64_t)q * n + i] = s * zip + c * ziq;
+        A_[(int64_t)j * n + p] = (j == q) ? 0.0 : c * apj - s * aqj;
+        A_[(int64_t)j * n + q] = (j == p) ? 0.0 : s * apj + c * aqj;
       }
       __syncthreads();
     }
@@ -492,17 +483,23 @@ __device__ void jacobi_sweeps(R* A_, R* Z_, int n, R thr, int maxsweep, R* cc, R
         pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = sn;
       }
       __syncthreads();
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        const int k = idx / n, i = idx % n;
+      // the rotations applied to A's columns p, q and, independently, to Z
+      for (int idx = tid; idx < 2 * npair * n; idx += NT) {
+        const bool onz = idx >= npair * n;
+        const int id2 = onz ? idx - npair * n : idx;
+        const int k = id2 / n, i = id2 % n;
         const R sk = ss[k];
         if (sk == R(0)) continue;
         const int p = pp[k], q = qq[k];
         const R ck = cc[k];
-        const R aip = A_[(int64_t)p * n + i], aiq = A_[(int64_t)q * n + i];
-        A_[(int64_t)p * n + i] = ck * aip - sk * aiq;
-        A_[(int64_t)q * n + i] = sk * aip + ck * aiq;
+        R* M = onz ? Z_ : A_;
+        const R aip = M[(int64_t)p * n + i], aiq = M[(int64_t)q * n + i];
+        M[(int64_t)p * n + i] = ck * aip - sk * aiq;
+        M[(int64_t)q * n + i] = sk * aip + ck * aiq;
       }
       __syncthreads();
+      // then to A's rows p, q; the pair's own off-diagonal entries, which
+      // the rotation annihilates, are written as exact zeros
       for (int idx = tid; idx < npair * n; idx += NT) {
         const int k = idx / n, j = idx % n;
         const R sk = ss[k];
@@ -510,24 +507,8 @@ __device__ void jacobi_sweeps(R* A_, R* Z_, int n, R thr, int maxsweep, R* cc, R
         const int p = pp[k], q = qq[k];
         const R ck = cc[k];
         const R apj = A_[(int64_t)j * n + p], aqj = A_[(int64_t)j * n + q];
-        A_[(int64_t)j * n + p] = ck * apj - sk * aqj;
-        A_[(int64_t)j * n + q] = sk * apj + ck * aqj;
-      }
-      __syncthreads();
-      for (int k = tid; k < npair; k += NT)
-        if (ss[k] != R(0)) {
-          A_[(int64_t)qq[k] * n + pp[k]] = R(0);
-          A_[(int64_t)pp[k] * n + qq[k]] = R(0);
-        }
-      for (int idx = tid; idx < npair * n; idx += NT) {
-        const int k = idx / n, i = idx % n;
-        const R sk = ss[k];
-        if (sk == R(0)) continue;
-        const int p = pp[k], q = qq[k];
-        const R ck = cc[k];
-        const R zip = Z_[(int64_t)p * n + i], ziq = Z_[(int64_t)q * n + i];
-        Z_[(int64_t)p * n + i] = ck * zip - sk * ziq;
-        Z_[(int64_t)q * n + i] = sk * zip + ck * ziq;
+        A_[(int64_t)j * n + p] = (j == q) ? R(0) : ck * apj - sk * aqj;
+        A_[(int64_t)j * n + q] = (j == p) ? R(0) : sk * apj + ck * aqj;
       }
       __syncthreads();
     }
@@ -727,11 +708,15 @@ __device__ inline void jacobi_eig_df(const double* __restrict__ T, int ldt, int 
         pp[k] = p; qq[k] = q; cc[k] = c; ss[k] = sn;
       }
       __syncthreads();
-      // rows p, q of A, then columns, then Z; x' = c x - s y, y' = s x + c y
-      for (int pass = 0; pass < 3; ++pass) {
-        float2* M = pass == 2 ? Z_ : A_;
-        for (int idx = tid; idx < npair * n; idx += NT) {
-          const int k = idx / n, i = idx % n;
+      // rows p, q of A together with those of Z (independent), then the
+      // columns of A; x' = c x - s y, y' = s x + c y
+      for (int pass = 0; pass < 2; ++pass) {
+        const int nwork = (pass == 0 ? 2 : 1) * npair * n;
+        for (int idx = tid; idx < nwork; idx += NT) {
+          const bool onz = idx >= npair * n;
+          float2* M = onz ? Z_ : A_;
+          const int id2 = onz ? idx - npair * n : idx;
+          const int k = id2 / n, i = id2 % n;
           const float2 sk = ss[k];
           if (sk.x == 0.f && sk.y == 0.f) continue;
           const float2 ck = cc[k];
